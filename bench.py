@@ -1,0 +1,362 @@
+"""Throughput of the MPCD + active-colloid step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp64]
+
+Workload (the 64^3 single system): 64^3 cells, fluid density 10 (2,621,440
+particles, Maxwell-Boltzmann at kT=1, zero net momentum), 500 colloids of radius
+2 (diameter 4) with the displaced-fluid mass, WCA sigma=4 eps=1, v0=0.01,
+Dr=0.001, SRD angle 90 deg, MPCD step 0.1 with 10 MD substeps.  Synthetic
+initial state from the library's own keyed initialiser (seed 0 + rank).
+
+One step = one MPCD step (rotation_mpcd, run, 10 substeps) over the whole system.
+value = fluid particle-steps/s with the state resident in HBM (CUDA graph per
+step, CUDA events on the library's stream).  e2e = the same metric through the
+public API from pinned host buffers: upload of the state, setup, K steps each
+followed by a device->host read of the step's diagnostics, download of the final
+state.  roofline: the dominant kernel (the fluid streaming pass) timed per launch
+with CUDA events over a second timed region, against its algorithmic bytes
+(72 B per particle: read position and displacement, write position).
+
+Multi-GPU: one independent replica per rank (different seed), no collective
+in the data path ("scaling": "weak").
+
+--impl reference: the reference's CPU algorithm on the host cores (the oracle port
+of cpp/, one single-threaded process per core on a bounded sample).
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L, DENSITY, NC, RADIUS = 64, 10, 500, 2.0
+STREAM_BYTES = 72  # per particle per streaming launch (FP64: read x 24 + w 24, write x 24)
+STEP_BYTES = 808   # per particle per MPCD step, FP64 byte model (10 x 72 + 88)
+
+
+def workload(seed=0):
+    import numpy as np
+    M = DENSITY * 4.0 / 3.0 * np.pi * RADIUS ** 3
+    return dict(L=L, n_fluid=L ** 3 * DENSITY, n_colloid=NC,
+                kw=dict(n_sub=10, ndt=0.1, kbt=1.0, kbt1=1.0, mass_fl=1.0, mass_colloid=M, sig_colloid=4.0,
+                        eps=1.0, sigma=2 * RADIUS, I_colloid=0.4 * M * RADIUS ** 2, v0=0.01, theta_deg=90.0,
+                        Dr=0.001, seed=seed, init_gap=0.5))
+
+
+def config_dict(precision):
+    return {"workload": "MPCD 64^3 cells, density 10 (2,621,440 fluid particles), 500 colloids r=2, "
+                        "10 MD substeps per MPCD step",
+            "box": [L, L, L], "n_fluid": L ** 3 * DENSITY, "n_colloid": NC, "n_sub": 10, "precision": precision,
+            "l2": "state (>190 MB) larger than the 129 MB L2; no flush between steps",
+            "init": "library keyed initialiser, Maxwell-Boltzmann, seed = rank"}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self, dev=0):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or f[0] != str(dev):
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_particle():
+    """DRAM bytes per particle of one streaming launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_stream_fp64_traffic.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_particle"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------- CPU baseline
+
+def synthetic_state(seed, n_fluid, L_=L, nc=NC, radius=RADIUS, gap=0.5, kbt=1.0, M=None):
+    """Host-built initial state with the workload's shapes and distributions:
+    colloids by random sequential addition (gap >= 0.5), fluid uniform outside the
+    colloids, Maxwell-Boltzmann velocities with zero net momentum, isotropic
+    orientations."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(1000 + seed)
+    M = DENSITY * 4.0 / 3.0 * np.pi * radius ** 3 if M is None else M
+    X = np.empty((nc, 3))
+    k = 0
+    while k < nc:
+        t = rng.uniform(0, L_, 3)
+        d = X[:k] - t
+        d -= L_ * np.round(d / L_)
+        if k == 0 or np.min(np.einsum("ij,ij->i", d, d)) >= (2 * radius + gap) ** 2:
+            X[k] = t
+            k += 1
+    tree = cKDTree(X, boxsize=L_)
+    pos = np.empty((0, 3))
+    while len(pos) < n_fluid:
+        cand = rng.uniform(0, L_, (int((n_fluid - len(pos)) * 1.2) + 16, 3))
+        dist, _ = tree.query(cand)
+        pos = np.concatenate([pos, cand[dist >= radius]])
+    pos = pos[:n_fluid]
+    vel = rng.normal(0, np.sqrt(kbt), (n_fluid, 3))
+    vel -= vel.mean(0)
+    V = rng.normal(0, np.sqrt(kbt / M), (nc, 3))
+    V -= V.mean(0)
+    W = rng.normal(0, np.sqrt(kbt / (0.4 * M * radius ** 2)), (nc, 3))
+    ra = rng.normal(size=(nc, 3))
+    ra /= np.linalg.norm(ra, axis=1)[:, None]
+    return dict(pos_fl=pos, vel_fl=vel, pos_colloid=X, vel_colloid=V, ang_vel_colloid=W, ra=ra)
+
+
+def _cpu_worker(args):
+    """Time `steps` oracle steps of the workload on one core (separate process)."""
+    seed, steps, n_fluid_sample = args
+    from oracle import oracle as O
+    w = workload(seed)
+    o = O.Oracle(L=w["L"], n_fluid=n_fluid_sample, n_colloid=w["n_colloid"], rng_mode=O.RNG_KEYED,
+                 **{k: v for k, v in w["kw"].items() if k != "init_gap"})
+    for k, v in synthetic_state(seed, n_fluid_sample).items():
+        o.set(k, v)
+    o.setup()
+    o.step()  # warm
+    t0 = time.perf_counter()
+    o.run_steps(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return n_fluid_sample * steps / dt
+
+
+def cpu_baseline(processes, steps, n_fluid):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes) as pool:
+        rates = pool.map(_cpu_worker, [(s, steps, n_fluid) for s in range(processes)])
+    return sum(rates), rates
+
+
+# ---------------------------------------------------------------- our arm
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+
+    import brownian_gb300 as bg
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = workload(seed=rank)
+    N = w["n_fluid"]
+    sim = bg.Simulation(w["L"], N, w["n_colloid"], precision=bg.FP64, **w["kw"])
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.initialize(bg.INIT_PHYSICAL)
+    sim.setup()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (also captures the step graph)
+    sim.step(args.warmup)
+    # ---- timed region A: graph replay, inputs resident in HBM
+    barrier()
+    clocks = Clocks()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = sim.launch_count
+    e0.record(stream)
+    sim.step(args.steps)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop(dev)
+    ms = e0.elapsed_time(e1)
+    gpu_launches = sim.launch_count - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N * args.steps / (ms / 1e3)
+
+    # ---- timed region B: the same steps, each kernel bracketed by CUDA events
+    sim.profile(True)
+    barrier()
+    sim.step(args.steps)
+    barrier()
+    prof = sim.profile_read()
+    sim.profile(False)
+    st_launches, st_ms = prof.get("k_stream", (0, 0.0))
+    t_launch = st_ms / max(st_launches, 1) / 1e3
+    achieved = STREAM_BYTES * N / t_launch / 1e9 if st_launches else None
+    peak, peak_kind = measured_peak_hbm()
+    tpp = ncu_traffic_per_particle()
+    shares = {k: round(v[1] / sum(x[1] for x in prof.values()), 4) for k, v in prof.items()}
+
+    # ---- timed region C: end to end through the public API from pinned host buffers
+    host = sim.get_state()
+    pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in host.items()}
+    out = {k: torch.empty(v.shape, dtype=torch.float64).pin_memory().numpy() for k, v in host.items()}
+    barrier()
+    t0 = time.perf_counter()
+    sim.set_state(pinned["pos_fl"], pinned["vel_fl"], pinned["pos_colloid"], pinned["vel_colloid"],
+                  pinned["ang_vel_colloid"], pinned["ra"])
+    sim.setup()
+    for _ in range(args.steps):
+        sim.step(1)
+        sim.diag()
+    got = sim.get_state()
+    for k in out:
+        out[k][...] = got[k]
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    state_bytes = sum(v.nbytes for k, v in host.items() if k != "f")
+    diag_bytes = 8 * 14
+    e2e = {"value": world * N * args.steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": state_bytes / args.steps,
+           "d2h_bytes_per_step": (state_bytes + host["f"].nbytes) / args.steps + diag_bytes,
+           "timed": "set_state + setup + K x (step + diag) + get_state, host pinned buffers"}
+    d = sim.diag()
+    sim.close()
+
+    if rank != 0:
+        return None
+    line = {
+        "metric": "MPCD fluid particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(config_dict("fp64"), parallelism=f"replicas x{world}"),
+        "hbm_roofline_frac_step": value / world * STEP_BYTES / (peak * 1e9),
+        "roofline": {"bound": "hbm", "kernel": "k_stream (fluid streaming + wall collisions)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": STREAM_BYTES * N,
+                     "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+                     "launch_ms": t_launch * 1e3, "launches": st_launches},
+        "kernel_share": shares,
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clk,
+        "diag_end": {"temperature_fluid": d["temperature_fluid"], "momentum": d["momentum"]},
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    n_full = L ** 3 * DENSITY
+    sample_n = args.cpu_sample or n_full
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        procs = os.cpu_count() or 1
+        total = 0.0
+        t0 = time.perf_counter()
+        for _ in range(args.warmup):
+            pass  # each timed worker does its own warm-up step
+        rate, rates = cpu_baseline(procs, args.steps, sample_n)
+        wall = time.perf_counter() - t0
+        line = {"impl": "reference", "metric": "MPCD fluid particle-steps/s", "value": rate,
+                "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": dict(config_dict("fp64"), parallelism=f"{procs} CPU processes"),
+                "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": procs, "kind": "port",
+                                 "sample": f"{procs} independent single-threaded oracle processes (restatement of "
+                                           f"cpp/), each {args.steps} MPCD steps of the 64^3 system with "
+                                           f"{sample_n} fluid particles, after one warm-up step; wall {wall:.1f} s"},
+                "e2e": {"value": rate, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    # CPU baseline of our arm: start the oracle process before any GPU call (spawn)
+    cpu = None
+    if rank == 0:
+        t0 = time.perf_counter()
+        rate, _ = cpu_baseline(1, args.cpu_steps, sample_n)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"one single-threaded oracle process (restatement of cpp/), {args.cpu_steps} MPCD steps of "
+                         f"the 64^3 system with {sample_n} fluid particles after one warm-up step "
+                         f"({time.perf_counter() - t0:.1f} s wall incl. set-up)"}
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    line = run_ours(args, rank, world, dist)
+    if line is not None:
+        line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

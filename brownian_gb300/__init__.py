@@ -1,0 +1,248 @@
+"""brownian_gb300: the MPCD + active-colloid time step on GB300 (sm_103a).
+
+Python mirror of the C ABI in include/brownian_gb300.h.  `Simulation` holds one
+device-resident system; its methods carry the names of the reference routines
+(cpp/ of shashankgandham/brownian): initialize, setup (the prologue of main),
+rotation_mpcd, run, substep, step.  `active_brownian` is the reference's main()
+loop.  There is no CPU path: every call runs the sm_103a kernels of
+lib/libbrownian_gb300.so, and importing the package fails if that library is
+missing or cannot load.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libbrownian_gb300.so")
+
+OK, ERR_PARAM, ERR_CUDA, ERR_CAPACITY, ERR_RANGE, ERR_STATE, ERR_NOMEM = range(7)
+FP64, FP32C = 0, 1
+INIT_REFERENCE, INIT_PHYSICAL = 0, 1
+
+# every symbol include/brownian_gb300.h declares
+EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", "mpcd_set_state", "mpcd_get_state",
+           "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
+           "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
+           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count"]
+
+
+class MPCDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("Lx", C.c_int), ("Ly", C.c_int), ("Lz", C.c_int),
+        ("n_fluid", C.c_int), ("n_colloid", C.c_int), ("n_sub", C.c_int),
+        ("kbt", C.c_double), ("kbt1", C.c_double), ("ndt", C.c_double),
+        ("mass_fl", C.c_double), ("mass_colloid", C.c_double), ("sig_colloid", C.c_double),
+        ("eps", C.c_double), ("sigma", C.c_double), ("I_colloid", C.c_double), ("v0", C.c_double),
+        ("theta_deg", C.c_double), ("Dr", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int),
+        ("max_per_cell", C.c_int), ("vmax", C.c_double), ("init_gap", C.c_double),
+    ]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("step", C.c_int64), ("ke_fluid", C.c_double), ("ke_colloid", C.c_double),
+        ("ang_ke_colloid", C.c_double), ("potential_colloid", C.c_double), ("energy_colloid", C.c_double),
+        ("momentum", C.c_double * 3), ("momentum_fluid", C.c_double * 3), ("temperature_fluid", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: (list(getattr(self, k)) if k.startswith("momentum") else getattr(self, k)) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run brownian_gb300.build.build() (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        L.mpcd_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+        L.mpcd_destroy.argtypes = [vp]
+        L.mpcd_last_error.argtypes = [vp]
+        L.mpcd_last_error.restype = C.c_char_p
+        L.mpcd_set_stream.argtypes = [vp, vp]
+        L.mpcd_set_state.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+        L.mpcd_get_state.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
+        L.mpcd_set_step.argtypes = [vp, C.c_int64]
+        L.mpcd_get_step.argtypes = [vp]
+        L.mpcd_get_step.restype = C.c_int64
+        L.mpcd_initialize.argtypes = [vp, C.c_int]
+        for n in ["mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run"]:
+            getattr(L, n).argtypes = [vp]
+        L.mpcd_substep.argtypes = [vp, C.c_int]
+        L.mpcd_step.argtypes = [vp, C.c_int]
+        L.mpcd_diag.argtypes = [vp, C.POINTER(Diag)]
+        L.mpcd_get_rotation_binning.argtypes = [vp, ip, ip, dp]
+        L.mpcd_get_shell_count.argtypes = [vp, ip]
+        L.mpcd_profile_enable.argtypes = [vp, C.c_int]
+        L.mpcd_profile_read.argtypes = [vp, C.c_void_p, C.POINTER(C.c_int64), dp, C.c_int]
+        L.mpcd_launch_count.argtypes = [vp]
+        L.mpcd_launch_count.restype = C.c_int64
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _f64(a, n):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != (n, 3):
+        raise ValueError(f"expected shape ({n}, 3), got {a.shape}")
+    return a
+
+
+def displaced_mass(radius, density, mass_fl=1.0):
+    """Mass of the fluid a sphere displaces (the configs' colloid mass)."""
+    return density * mass_fl * 4.0 / 3.0 * np.pi * radius ** 3
+
+
+class Simulation:
+    """One MPCD + active-colloid system resident on the GPU."""
+
+    def __init__(self, L, n_fluid, n_colloid, *, n_sub=10, kbt=1.0, kbt1=1.0, ndt=0.1, mass_fl=1.0,
+                 mass_colloid=654.1, sig_colloid=5.0, eps=1.0, sigma=None, I_colloid=None, v0=0.0,
+                 theta_deg=130.0, Dr=0.0, seed=77777, precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5):
+        Lx, Ly, Lz = (L, L, L) if np.isscalar(L) else L
+        sigma = 0.8 * sig_colloid if sigma is None else sigma          # cpp/active_brownian.cpp:7
+        I_colloid = 0.1 * mass_colloid * sigma * sigma if I_colloid is None else I_colloid
+        self.params = Params(Lx, Ly, Lz, n_fluid, n_colloid, n_sub, kbt, kbt1, ndt, mass_fl, mass_colloid,
+                             sig_colloid, eps, sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell,
+                             vmax, init_gap)
+        self.N, self.Nc = n_fluid, n_colloid
+        self.C = Lx * Ly * Lz
+        self.dt = ndt / n_sub
+        h = C.c_void_p()
+        r = lib().mpcd_create(C.byref(self.params), C.byref(h))
+        if r:
+            raise MPCDError(r, "mpcd_create rejected the parameters or could not allocate")
+        self.h = h
+
+    # ---------------------------------------------------------------- plumbing
+    def _ck(self, r):
+        if r:
+            raise MPCDError(r, lib().mpcd_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpcd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        """Launch on an external cudaStream_t (e.g. torch.cuda.Stream().cuda_stream)."""
+        self._ck(lib().mpcd_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    # ---------------------------------------------------------------- state
+    def set_state(self, pos_fl=None, vel_fl=None, pos_colloid=None, vel_colloid=None, ang_vel_colloid=None, ra=None):
+        a = [_f64(pos_fl, self.N), _f64(vel_fl, self.N), _f64(pos_colloid, self.Nc), _f64(vel_colloid, self.Nc),
+             _f64(ang_vel_colloid, self.Nc), _f64(ra, self.Nc)]
+        self._ck(lib().mpcd_set_state(self.h, *[_dp(x) for x in a]))
+
+    def get_state(self):
+        out = {k: np.empty((self.N, 3)) for k in ("pos_fl", "vel_fl")}
+        out.update({k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra", "f")})
+        self._ck(lib().mpcd_get_state(self.h, *[_dp(out[k]) for k in ("pos_fl", "vel_fl", "pos_colloid",
+                                                                      "vel_colloid", "ang_vel_colloid", "ra", "f")]))
+        return out
+
+    @property
+    def step_count(self):
+        return lib().mpcd_get_step(self.h)
+
+    @step_count.setter
+    def step_count(self, v):
+        self._ck(lib().mpcd_set_step(self.h, v))
+
+    # ---------------------------------------------------------------- routines
+    def initialize(self, style=INIT_REFERENCE):
+        self._ck(lib().mpcd_initialize(self.h, style))
+
+    def setup(self):
+        self._ck(lib().mpcd_setup(self.h))
+
+    def rotation_mpcd(self):
+        self._ck(lib().mpcd_rotation_mpcd(self.h))
+
+    def run(self):
+        self._ck(lib().mpcd_run(self.h))
+
+    def substep(self, l):
+        self._ck(lib().mpcd_substep(self.h, l))
+
+    def step(self, nsteps=1):
+        self._ck(lib().mpcd_step(self.h, nsteps))
+
+    def diag(self):
+        d = Diag()
+        self._ck(lib().mpcd_diag(self.h, C.byref(d)))
+        return d.as_dict()
+
+    # ---------------------------------------------------------------- observables
+    def rotation_binning(self):
+        cell_of = np.empty(self.N, dtype=np.int32)
+        occ = np.empty(self.C, dtype=np.int32)
+        shift = np.empty(3)
+        self._ck(lib().mpcd_get_rotation_binning(self.h, cell_of.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                 occ.ctypes.data_as(C.POINTER(C.c_int32)), _dp(shift)))
+        return cell_of, occ, shift
+
+    def shell_count(self):
+        o = np.empty(self.Nc, dtype=np.int32)
+        self._ck(lib().mpcd_get_shell_count(self.h, o.ctypes.data_as(C.POINTER(C.c_int32))))
+        return o
+
+    # ---------------------------------------------------------------- profiling
+    def profile(self, on=True):
+        self._ck(lib().mpcd_profile_enable(self.h, 1 if on else 0))
+
+    def profile_read(self):
+        cap = 64
+        names = (C.c_char * 48 * cap)()
+        launches = (C.c_int64 * cap)()
+        ms = (C.c_double * cap)()
+        n = lib().mpcd_profile_read(self.h, names, launches, ms, cap)
+        return {bytes(names[i]).split(b"\0", 1)[0].decode(): (launches[i], ms[i]) for i in range(min(n, cap))}
+
+    @property
+    def launch_count(self):
+        return lib().mpcd_launch_count(self.h)
+
+
+def active_brownian(sim, nsteps, style=INIT_REFERENCE, diag_every=1):
+    """The reference's main() (cpp/active_brownian.cpp:9-60): initialise, the
+    prologue (create_box, neighbour lists, forces; tumble is part of initialize),
+    then nsteps MPCD steps; returns the per-step diagnostics."""
+    sim.initialize(style)
+    sim.setup()
+    out = []
+    for s in range(nsteps):
+        sim.step(1)
+        if diag_every and (s + 1) % diag_every == 0:
+            out.append(sim.diag())
+    return out

@@ -1,0 +1,685 @@
+// Host side of the C ABI (include/brownian_gb300.h): the context that owns the
+// device-resident state, the constants derived from the parameters, the launch
+// sequence of one MPCD step (captured once into a CUDA graph and replayed), the
+// routine-level entry points, initialisation and diagnostics.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/brownian_gb300.h"
+#include "kernels.cuh"
+
+using namespace bgb;
+
+namespace {
+
+struct ProfEvent {
+  const char *name;
+  cudaEvent_t a, b;
+};
+
+struct DevAlloc {
+  std::vector<void *> ptrs;
+  cudaError_t err = cudaSuccess;
+  template <typename T>
+  T *get(size_t n) {
+    void *p = nullptr;
+    if (err == cudaSuccess) {
+      err = cudaMalloc(&p, n * sizeof(T) + 16);
+      if (err == cudaSuccess) {
+        ptrs.push_back(p);
+        cudaMemset(p, 0, n * sizeof(T) + 16);
+      }
+    }
+    return (T *)p;
+  }
+  void release() {
+    for (void *p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+}  // namespace
+
+struct mpcd_ctx {
+  mpcd_params p;
+  SysF64 S;
+  DevAlloc mem;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaGraphExec_t step_exec = nullptr;
+  int step_launches = 0;
+  bool setup_done = false;
+  std::string err;
+  int64_t launches = 0;
+  bool profile = false;
+  std::vector<ProfEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::map<std::string, std::pair<int64_t, double>> prof;
+  StepState *ss_host = nullptr;  // pinned
+  double *inv_n = nullptr;
+  double *part = nullptr;        // reduction partials
+  int part_blocks = 256;
+  double *staging = nullptr;     // AoS transfer buffer, allocated on first use
+};
+
+static int fail(mpcd_ctx *c, int code, const std::string &m) {
+  if (c) c->err = m;
+  return code;
+}
+
+#define CUDA_OK(c, call)                                                                     \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return fail((c), MPCD_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+static long long dbits_h(double x) {
+  long long b;
+  memcpy(&b, &x, 8);
+  return b;
+}
+
+static Dim make_dim(int L) {
+  Dim d;
+  d.L = (double)L;
+  d.halfL = d.L / 2;
+  d.lo_bits = dbits_h(ldexp(d.L, -30));
+  d.L_bits = dbits_h(d.L);
+  d.img_bits = dbits_h(0.49 * d.L);
+  return d;
+}
+
+// ---------------------------------------------------------------- launching
+
+static cudaEvent_t pool_event(mpcd_ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+template <typename... KArgs, typename... Args>
+static void launch(mpcd_ctx *c, const char *name, void (*k)(KArgs...), dim3 g, dim3 b, Args... args) {
+  ProfEvent pe{name, nullptr, nullptr};
+  if (c->profile) {
+    pe.a = pool_event(c);
+    pe.b = pool_event(c);
+    cudaEventRecord(pe.a, c->stream);
+  }
+  k<<<g, b, 0, c->stream>>>(args...);
+  c->launches++;
+  if (c->profile) {
+    cudaEventRecord(pe.b, c->stream);
+    c->pending.push_back(pe);
+  }
+}
+
+static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+static int colloid_grid(const mpcd_ctx *c) { return (int)blocks_for((long long)c->S.Nc * 32, 128); }
+
+static void enq_stream(mpcd_ctx *c, int flags, int l) {
+  const char *name = flags == (F_STREAM | F_COLLIDE) ? "k_stream"
+                     : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
+                     : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
+  launch(c, name, stream_kernel(flags), blocks_for(c->S.N, 256), 256, c->S, l);
+}
+
+static void enq_colloid(mpcd_ctx *c, int mode, int l) {
+  int g = colloid_grid(c);
+  launch(c, "k_colloid", k_colloid, g > 0 ? g : 1, 128, c->S, mode, l);
+}
+
+static void enq_rotation(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  launch(c, "k_cell_prep", k_cell_prep, blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256), 256, S);
+  launch(c, "k_rotate", k_rotate, blocks_for(S.N, 256), 256, S);
+}
+
+static void enq_run_fluid(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  if (S.Nc == 0) return;
+  launch(c, "k_run_shell", k_run_shell, 152 * 4, 256, S);
+  launch(c, "k_run_kick", k_run_kick, 152 * 4, 256, S);
+}
+
+// one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
+static void enq_step(mpcd_ctx *c) {
+  const int n = c->S.n_sub;
+  enq_rotation(c);
+  enq_run_fluid(c);
+  for (int l = 1; l <= n; ++l) {
+    enq_colloid(c, (l == 1 ? M_KICK : M_FINISH) | M_ADVANCE, l);
+    enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l);
+  }
+  enq_colloid(c, M_FINISH, n + 1);
+  launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+}
+
+static int collect_profile(mpcd_ctx *c) {
+  if (c->pending.empty()) return MPCD_OK;
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  for (auto &pe : c->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, pe.a, pe.b);
+    auto &slot = c->prof[pe.name];
+    slot.first += 1;
+    slot.second += ms;
+    c->event_pool.push_back(pe.a);
+    c->event_pool.push_back(pe.b);
+  }
+  c->pending.clear();
+  return MPCD_OK;
+}
+
+static const char *err_text(int bits) {
+  if (bits & ERRB_TTABLE) return "more colloids reach one cell than the fluid-to-colloid table holds";
+  if (bits & ERRB_SHELL) return "run() candidate records overflowed";
+  if (bits & ERRB_VRANGE) return "a fluid velocity exceeded vmax (range of the exact cell sums)";
+  if (bits & ERRB_OCCUPANCY) return "a cell holds more than max_per_cell particles";
+  if (bits & ERRB_DISPLACE) return "a wall collision displaced a particle beyond the cell-table margin";
+  if (bits & ERRB_SHELLSLOTS) return "a particle lies in more rear shells than a record holds";
+  if (bits & ERRB_DELTA) return "a colloid momentum exchange left the range of the exact sums";
+  return "device error";
+}
+
+// synchronise, read the device step state, turn error bits into a status
+static int check_device(mpcd_ctx *c) {
+  CUDA_OK(c, cudaMemcpyAsync(c->ss_host, c->S.ss, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  CUDA_OK(c, cudaGetLastError());
+  if (c->profile) collect_profile(c);
+  int bits = c->ss_host->err;
+  if (bits) {
+    int code = (bits & (ERRB_VRANGE | ERRB_DELTA)) ? MPCD_ERR_RANGE : MPCD_ERR_CAPACITY;
+    char buf[160];
+    snprintf(buf, sizeof buf, "device error bits 0x%x: %s", bits, err_text(bits));
+    return fail(c, code, buf);
+  }
+  return MPCD_OK;
+}
+
+static int drop_graph(mpcd_ctx *c) {
+  if (c->step_exec) {
+    cudaGraphExecDestroy(c->step_exec);
+    c->step_exec = nullptr;
+  }
+  return MPCD_OK;
+}
+
+// ---------------------------------------------------------------- lifetime
+
+extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
+  if (!pp || !out) return MPCD_ERR_PARAM;
+  *out = nullptr;
+  const mpcd_params &p = *pp;
+  if (p.Lx < 7 || p.Ly < 7 || p.Lz < 7) return MPCD_ERR_PARAM;  // the 7x7x7 block must not wrap onto itself
+  if (p.n_fluid < 1 || p.n_colloid < 0 || p.n_colloid > 65535 || p.n_sub < 1) return MPCD_ERR_PARAM;
+  if (!(p.ndt > 0) || !(p.kbt > 0) || !(p.mass_fl > 0)) return MPCD_ERR_PARAM;
+  if (p.n_colloid > 0 && (!(p.mass_colloid > 0) || !(p.I_colloid > 0) || !(p.sigma > 0) || !(p.sig_colloid > 0)))
+    return MPCD_ERR_PARAM;
+  if (p.precision != MPCD_FP64) return MPCD_ERR_PARAM;
+  long long C = (long long)p.Lx * p.Ly * p.Lz;
+  if (C > (1ll << 30)) return MPCD_ERR_PARAM;
+
+  mpcd_ctx *c = new mpcd_ctx();
+  c->p = p;
+  SysF64 &S = c->S;
+  memset(&S, 0, sizeof S);
+  S.N = p.n_fluid;
+  S.Nc = p.n_colloid;
+  S.Lx = p.Lx; S.Ly = p.Ly; S.Lz = p.Lz;
+  S.C = (int)C;
+  S.Cpad = S.C + p.Lx * p.Ly + 2 * p.Lx + 4;
+  S.n_sub = p.n_sub;
+  S.dx = make_dim(p.Lx); S.dy = make_dim(p.Ly); S.dz = make_dim(p.Lz);
+  S.key = make_uint2((uint32_t)p.seed, (uint32_t)(p.seed >> 32));
+  // constants, evaluated with the host libm exactly as the reference writes them
+  const double dt = p.ndt / (double)p.n_sub;
+  S.dt = dt;
+  S.inv_dt = 1.0 / dt;
+  S.mass_fl = p.mass_fl; S.mass_colloid = p.mass_colloid; S.I_colloid = p.I_colloid; S.kbt = p.kbt;
+  S.sig2q = pow(p.sigma, 2) * 0.25;                       // cpp/fluid_colloid_collision.cpp:35
+  S.rsh2 = pow(p.sigma * 0.5 + 0.5, 2);                   // cpp/run.cpp:18
+  S.sig_colloid = p.sig_colloid; S.eps = p.eps;
+  S.r_cutoff = pow(2, 1.0 / 6.0) * p.sig_colloid;         // cpp/update.cpp:3
+  S.fc = 4.0 * p.eps * (12.0 * (pow(p.sig_colloid, 12) / pow(S.r_cutoff, 13)) -
+                        6.0 * (pow(p.sig_colloid, 6) / pow(S.r_cutoff, 7)));
+  S.ufc = 4.0 * p.eps * (pow(p.sig_colloid / S.r_cutoff, 12) - pow(p.sig_colloid / S.r_cutoff, 6)) + S.fc * S.r_cutoff;
+  S.sig12 = pow(p.sig_colloid, 12);
+  S.sig6 = pow(p.sig_colloid, 6);
+  const double dt2 = dt * dt;
+  S.ddt = 0.5 * dt2 / p.mass_colloid;                      // cpp/update.cpp:48
+  S.dtb2 = dt / (p.mass_colloid * 2);                      // cpp/update.cpp:63
+  S.v0 = p.v0; S.Dr = p.Dr;
+  S.rotdiff_s = sqrt(2.0 * p.Dr * dt);
+  const double theta = 2 * asin(1) * (p.theta_deg / 180.0); // cpp/rotation_mpcd.cpp:19
+  S.ct = cos(theta); S.st = sin(theta); S.ict = 1 - cos(theta);
+  S.two_pi = 4.0 * asin(1.0);
+  S.sqrt_kt_m = sqrt(p.kbt / p.mass_fl);
+  S.m_beta = p.mass_fl / p.kbt;
+  S.cs = 3.0 * p.kbt * dt2 / p.mass_fl;
+  const double margin = 0.5;
+  S.rT_coll = (float)(p.sigma * 0.5 + margin + 0.01);
+  S.rT_shell = (float)(p.sigma * 0.5 + 0.5 + margin + 0.01);
+  S.disp_margin2 = margin * margin;
+  S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
+  const double vmax = p.vmax > 0 ? p.vmax : 24.0 * sqrt(p.kbt / p.mass_fl);
+  const double wmax = vmax * dt;
+  S.kw = 62 - (int)ceil(log2((double)S.max_per_cell * wmax));
+  S.kw2 = 62 - (int)ceil(log2((double)S.max_per_cell * 3.0 * wmax * wmax));
+  S.inv_sw = ldexp(1.0, -S.kw);
+  S.inv_sw2 = ldexp(1.0, -S.kw2);
+  S.wlim_bits = dbits_h(wmax);
+  S.w2lim_bits = dbits_h(3.0 * wmax * wmax);
+
+  DevAlloc &m = c->mem;
+  const size_t N = S.N, Nc = S.Nc > 0 ? S.Nc : 1;
+  S.px = m.get<double>(N); S.py = m.get<double>(N); S.pz = m.get<double>(N);
+  S.wx = m.get<double>(N); S.wy = m.get<double>(N); S.wz = m.get<double>(N);
+  S.rotcell = m.get<int>(N);
+  S.acc = m.get<CellAcc>(S.Cpad);
+  S.cell_ab = m.get<double>((size_t)S.C * 12);
+  for (int b = 0; b < 2; ++b) {
+    S.X[b] = m.get<double>(3 * Nc);
+    S.Xf[b] = m.get<float4>(Nc);
+    S.cbox[b] = m.get<int>(Nc);
+    S.Tcnt[b] = m.get<int>(S.C);
+    S.Tlist[b] = m.get<uint16_t>((size_t)S.C * TCAP);
+  }
+  S.V = m.get<double>(3 * Nc); S.W = m.get<double>(3 * Nc); S.ra = m.get<double>(3 * Nc); S.f = m.get<double>(3 * Nc);
+  S.exch = m.get<ExchAcc>(Nc);
+  S.shell_cnt = m.get<int>(Nc);
+  S.pot_part = m.get<double>(Nc);
+  // run() candidates: particles within sigma/2 + 1/2 of a colloid, with room to spare
+  const double rsh = p.sigma * 0.5 + 0.5, density = (double)S.N / (double)S.C;
+  double est = (double)S.Nc * (4.0 / 3.0 * M_PI * rsh * rsh * rsh * density * 2.0 + 64.0);
+  S.shell_cap = (int)(est < (double)S.N ? est : (double)S.N) + 1024;
+  S.shell = m.get<ShellRec>(S.shell_cap);
+  S.ss = m.get<StepState>(1);
+  c->inv_n = m.get<double>(S.max_per_cell + 1);
+  S.inv_n = c->inv_n;
+  c->part = m.get<double>((size_t)c->part_blocks * 8);
+  if (m.err != cudaSuccess) {
+    std::string e = cudaGetErrorString(m.err);
+    m.release();
+    delete c;
+    return m.err == cudaErrorMemoryAllocation ? MPCD_ERR_NOMEM : MPCD_ERR_CUDA;
+  }
+  std::vector<double> inv(S.max_per_cell + 1, 0.0);
+  for (int n = 1; n <= S.max_per_cell; ++n) inv[n] = 1.0 / n;
+  cudaMemcpy(c->inv_n, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
+  if (cudaMallocHost(&c->ss_host, sizeof(StepState)) != cudaSuccess) {
+    m.release();
+    delete c;
+    return MPCD_ERR_NOMEM;
+  }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    m.release();
+    cudaFreeHost(c->ss_host);
+    delete c;
+    return MPCD_ERR_CUDA;
+  }
+  c->own_stream = true;
+  cudaDeviceSynchronize();
+  *out = c;
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_destroy(mpcd_ctx *c) {
+  if (!c) return MPCD_ERR_PARAM;
+  cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  for (auto &pe : c->pending) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
+  c->mem.release();
+  if (c->staging) cudaFree(c->staging);
+  if (c->ss_host) cudaFreeHost(c->ss_host);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MPCD_OK;
+}
+
+extern "C" const char *mpcd_last_error(const mpcd_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int mpcd_set_stream(mpcd_ctx *c, void *stream) {
+  if (!c) return MPCD_ERR_PARAM;
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  drop_graph(c);
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+  } else {
+    CUDA_OK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  return MPCD_OK;
+}
+
+// ---------------------------------------------------------------- state
+
+static int cur_buf(const mpcd_ctx *c) {
+  long long g = c->ss_host->step * c->S.n_sub - 1;
+  return (int)(g & 1);
+}
+
+static int read_ss(mpcd_ctx *c) {
+  CUDA_OK(c, cudaMemcpyAsync(c->ss_host, c->S.ss, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  return MPCD_OK;
+}
+
+static int upload_colloid_pos(mpcd_ctx *c, const double *xyz) {
+  const SysF64 &S = c->S;
+  int b = cur_buf(c);
+  std::vector<float4> xf(S.Nc);
+  std::vector<int> cb(S.Nc);
+  for (int j = 0; j < S.Nc; ++j) {
+    xf[j] = make_float4((float)xyz[3 * j], (float)xyz[3 * j + 1], (float)xyz[3 * j + 2], 0.f);
+    // int(x) + Lx*int(y) + Lx*Ly*int(z) of cpp/parameters.hpp:59
+    cb[j] = (int)xyz[3 * j] + S.Lx * ((int)xyz[3 * j + 1] + S.Ly * (int)xyz[3 * j + 2]);
+  }
+  CUDA_OK(c, cudaMemcpyAsync(S.X[b], xyz, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(c, cudaMemcpyAsync(S.Xf[b], xf.data(), sizeof(float4) * S.Nc, cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(c, cudaMemcpyAsync(S.cbox[b], cb.data(), sizeof(int) * S.Nc, cudaMemcpyHostToDevice, c->stream));
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  return MPCD_OK;
+}
+
+static int ensure_staging(mpcd_ctx *c) {
+  if (!c->staging) {
+    cudaError_t e = cudaMalloc(&c->staging, sizeof(double) * 3 * (size_t)c->S.N);
+    if (e != cudaSuccess) return fail(c, MPCD_ERR_NOMEM, "staging buffer");
+  }
+  return MPCD_OK;
+}
+
+// host AoS xyz -> device SoA: one copy of the caller's buffer (a DMA when it is
+// pinned), then a transpose on the device
+static int upload_soa(mpcd_ctx *c, const double *aos, double *dx, double *dy, double *dz, double scale) {
+  int r;
+  if ((r = ensure_staging(c))) return r;
+  const int N = c->S.N;
+  CUDA_OK(c, cudaMemcpyAsync(c->staging, aos, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, c->stream));
+  launch(c, "k_aos_to_soa", k_aos_to_soa, blocks_for(N, 256), 256, (const double *)c->staging, dx, dy, dz, N, scale);
+  return MPCD_OK;
+}
+
+static int download_soa(mpcd_ctx *c, double *aos, const double *dx, const double *dy, const double *dz, double div) {
+  int r;
+  if ((r = ensure_staging(c))) return r;
+  const int N = c->S.N;
+  launch(c, "k_soa_to_aos", k_soa_to_aos, blocks_for(N, 256), 256, c->staging, dx, dy, dz, N, div);
+  CUDA_OK(c, cudaMemcpyAsync(aos, c->staging, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  return MPCD_OK;
+}
+
+static int invalidate_tables(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  for (int b = 0; b < 2; ++b) CUDA_OK(c, cudaMemsetAsync(S.Tcnt[b], 0, sizeof(int) * S.C, c->stream));
+  CUDA_OK(c, cudaMemsetAsync(S.acc, 0, sizeof(CellAcc) * S.Cpad, c->stream));
+  if (S.Nc) CUDA_OK(c, cudaMemsetAsync(S.exch, 0, sizeof(ExchAcc) * S.Nc, c->stream));
+  c->setup_done = false;
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_set_state(mpcd_ctx *c, const double *pos_fl, const double *vel_fl, const double *pos_colloid,
+                              const double *vel_colloid, const double *ang_vel_colloid, const double *ra) {
+  if (!c) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  const SysF64 &S = c->S;
+  if (pos_fl && (r = upload_soa(c, pos_fl, S.px, S.py, S.pz, 0.0))) return r;
+  if (vel_fl && (r = upload_soa(c, vel_fl, S.wx, S.wy, S.wz, S.dt))) return r;  // w = fl(v*dt)
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  if (S.Nc) {
+    if (pos_colloid && (r = upload_colloid_pos(c, pos_colloid))) return r;
+    if (vel_colloid) CUDA_OK(c, cudaMemcpy(S.V, vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+    if (ang_vel_colloid) CUDA_OK(c, cudaMemcpy(S.W, ang_vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+    if (ra) CUDA_OK(c, cudaMemcpy(S.ra, ra, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+  }
+  return invalidate_tables(c);
+}
+
+extern "C" int mpcd_get_state(mpcd_ctx *c, double *pos_fl, double *vel_fl, double *pos_colloid, double *vel_colloid,
+                              double *ang_vel_colloid, double *ra, double *f) {
+  if (!c) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  const SysF64 &S = c->S;
+  if (pos_fl && (r = download_soa(c, pos_fl, S.px, S.py, S.pz, 0.0))) return r;
+  if (vel_fl && (r = download_soa(c, vel_fl, S.wx, S.wy, S.wz, S.dt))) return r;  // v = w/dt
+  if (S.Nc) {
+    int b = cur_buf(c);
+    if (pos_colloid) CUDA_OK(c, cudaMemcpy(pos_colloid, S.X[b], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (vel_colloid) CUDA_OK(c, cudaMemcpy(vel_colloid, S.V, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (ang_vel_colloid) CUDA_OK(c, cudaMemcpy(ang_vel_colloid, S.W, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (ra) CUDA_OK(c, cudaMemcpy(ra, S.ra, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (f) CUDA_OK(c, cudaMemcpy(f, S.f, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+  }
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_set_step(mpcd_ctx *c, int64_t step) {
+  if (!c || step < 0) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  if (c->S.Nc && c->ss_host->step != step) {
+    // the colloid positions live in the buffer of the last finished substep; move them
+    int from = cur_buf(c);
+    int to = (int)((step * c->S.n_sub - 1) & 1);
+    if (from != to) {
+      const SysF64 &S = c->S;
+      CUDA_OK(c, cudaMemcpy(S.X[to], S.X[from], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToDevice));
+      CUDA_OK(c, cudaMemcpy(S.Xf[to], S.Xf[from], sizeof(float4) * S.Nc, cudaMemcpyDeviceToDevice));
+      CUDA_OK(c, cudaMemcpy(S.cbox[to], S.cbox[from], sizeof(int) * S.Nc, cudaMemcpyDeviceToDevice));
+    }
+  }
+  c->ss_host->step = step;
+  CUDA_OK(c, cudaMemcpy(&c->S.ss->step, &step, sizeof(long long), cudaMemcpyHostToDevice));
+  return invalidate_tables(c);
+}
+
+extern "C" int64_t mpcd_get_step(const mpcd_ctx *c) {
+  if (!c) return -1;
+  long long s = 0;
+  cudaStreamSynchronize(c->stream);
+  cudaMemcpy(&s, &c->S.ss->step, sizeof s, cudaMemcpyDeviceToHost);
+  return s;
+}
+
+// ---------------------------------------------------------------- routines
+
+extern "C" int mpcd_setup(mpcd_ctx *c) {
+  if (!c) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  if ((r = invalidate_tables(c))) return r;
+  const int zero = 0;
+  CUDA_OK(c, cudaMemcpyAsync(&c->S.ss->err, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  // create_box + neighbour_list_md + compute_force_md: forces at the current positions,
+  // cell table around each colloid (cpp/active_brownian.cpp:93-96)
+  enq_colloid(c, M_SETUP, 1);
+  // neighbour_list_mpcd seen from the fluid: run() candidates of the first step, and the
+  // SRD binning of its rotation_mpcd
+  enq_stream(c, F_SHELL | F_BINROT, 0);
+  if ((r = check_device(c))) return r;
+  c->setup_done = true;
+  return MPCD_OK;
+}
+
+static int need_setup(mpcd_ctx *c) {
+  if (!c) return MPCD_ERR_PARAM;
+  if (!c->setup_done) return fail(c, MPCD_ERR_STATE, "mpcd_setup must follow set_state/initialize");
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_rotation_mpcd(mpcd_ctx *c) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  enq_rotation(c);
+  return check_device(c);
+}
+
+extern "C" int mpcd_run(mpcd_ctx *c) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  enq_run_fluid(c);
+  enq_colloid(c, M_KICK, 1);
+  return check_device(c);
+}
+
+extern "C" int mpcd_substep(mpcd_ctx *c, int l) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  const int n = c->S.n_sub;
+  if (l < 1 || l > n) return fail(c, MPCD_ERR_PARAM, "substep out of range");
+  enq_colloid(c, M_ADVANCE, l);   // update_pos_md, neighbour_list_md (+ cell table)
+  // update_pos_mpcd, neighbour_list_mpcd, fluid_colloid_collision (fluid side)
+  enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l);
+  // end of fluid_colloid_collision, update_activity_direction, compute_force_md,
+  // update_velocity_colloid
+  enq_colloid(c, M_FINISH, l + 1);
+  if (l == n) launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+  return check_device(c);
+}
+
+extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  if (nsteps < 0) return MPCD_ERR_PARAM;
+  if (c->profile) {
+    for (int s = 0; s < nsteps; ++s) enq_step(c);
+    return check_device(c);
+  }
+  if (!c->step_exec) {
+    cudaGraph_t g;
+    int64_t before = c->launches;
+    CUDA_OK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enq_step(c);
+    CUDA_OK(c, cudaStreamEndCapture(c->stream, &g));
+    c->step_launches = (int)(c->launches - before);
+    c->launches = before;
+    cudaError_t e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(c, MPCD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    CUDA_OK(c, cudaGraphLaunch(c->step_exec, c->stream));
+    c->launches += c->step_launches;
+  }
+  return check_device(c);
+}
+
+// ---------------------------------------------------------------- diagnostics
+
+extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
+  int r;
+  if (!out) return MPCD_ERR_PARAM;
+  if ((r = need_setup(c))) return r;
+  const SysF64 &S = c->S;
+  launch(c, "k_diag_fluid", k_diag_fluid, c->part_blocks, 256, S, c->part);
+  if (S.Nc) enq_colloid(c, M_POT, 1);
+  if ((r = check_device(c))) return r;
+  std::vector<double> part((size_t)c->part_blocks * 5);
+  CUDA_OK(c, cudaMemcpy(part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
+  double sw[3] = {0, 0, 0}, s2 = 0, n = 0;
+  for (int b = 0; b < c->part_blocks; ++b) {
+    for (int k = 0; k < 3; ++k) sw[k] += part[5 * b + k];
+    s2 += part[5 * b + 3];
+    n += part[5 * b + 4];
+  }
+  memset(out, 0, sizeof *out);
+  out->step = c->ss_host->step;
+  const double m = c->p.mass_fl;
+  for (int k = 0; k < 3; ++k) out->momentum_fluid[k] = m * sw[k] / S.dt;
+  out->ke_fluid = 0.5 * m * s2 / (S.dt * S.dt);
+  out->temperature_fluid = n > 0 ? 2.0 * out->ke_fluid / (3.0 * n) / c->p.kbt : 0;
+  double mom[3] = {out->momentum_fluid[0], out->momentum_fluid[1], out->momentum_fluid[2]};
+  if (S.Nc) {
+    std::vector<double> V(3 * S.Nc), W(3 * S.Nc), pot(S.Nc);
+    CUDA_OK(c, cudaMemcpy(V.data(), S.V, sizeof(double) * V.size(), cudaMemcpyDeviceToHost));
+    CUDA_OK(c, cudaMemcpy(W.data(), S.W, sizeof(double) * W.size(), cudaMemcpyDeviceToHost));
+    CUDA_OK(c, cudaMemcpy(pot.data(), S.pot_part, sizeof(double) * pot.size(), cudaMemcpyDeviceToHost));
+    double ke = 0, ake = 0, pe = 0;
+    for (int j = 0; j < S.Nc; ++j) {
+      ke += V[3 * j] * V[3 * j] + V[3 * j + 1] * V[3 * j + 1] + V[3 * j + 2] * V[3 * j + 2];
+      ake += W[3 * j] * W[3 * j] + W[3 * j + 1] * W[3 * j + 1] + W[3 * j + 2] * W[3 * j + 2];
+      for (int k = 0; k < 3; ++k) mom[k] += V[3 * j + k] * c->p.mass_colloid;
+      pe += pot[j];
+    }
+    out->ke_colloid = 0.5 * c->p.mass_colloid * ke;
+    out->ang_ke_colloid = 0.5 * c->p.I_colloid * ake;
+    out->potential_colloid = pe;
+    out->energy_colloid = pe + out->ke_colloid + out->ang_ke_colloid;
+  }
+  for (int k = 0; k < 3; ++k) out->momentum[k] = mom[k];
+  return MPCD_OK;
+}
+
+// ---------------------------------------------------------------- observables
+
+extern "C" int mpcd_get_rotation_binning(mpcd_ctx *c, int32_t *cell_of, int32_t *occupancy, double *shift) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  const SysF64 &S = c->S;
+  if ((r = read_ss(c))) return r;
+  std::vector<int> rc(S.N);
+  CUDA_OK(c, cudaMemcpy(rc.data(), S.rotcell, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
+  if (cell_of)
+    for (int i = 0; i < S.N; ++i) cell_of[i] = rc[i] + 1;
+  if (occupancy) {
+    for (int b = 0; b < S.C; ++b) occupancy[b] = 0;
+    for (int i = 0; i < S.N; ++i)
+      if (rc[i] < S.C) occupancy[rc[i]]++;
+  }
+  if (shift)
+    for (int k = 0; k < 3; ++k) shift[k] = c->ss_host->rr[k];
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_get_shell_count(mpcd_ctx *c, int32_t *cnt) {
+  if (!c || !cnt) return MPCD_ERR_PARAM;
+  if (c->S.Nc) CUDA_OK(c, cudaMemcpy(cnt, c->S.shell_cnt, sizeof(int) * c->S.Nc, cudaMemcpyDeviceToHost));
+  return MPCD_OK;
+}
+
+// ---------------------------------------------------------------- profiling
+
+extern "C" int mpcd_profile_enable(mpcd_ctx *c, int on) {
+  if (!c) return MPCD_ERR_PARAM;
+  if (!on) collect_profile(c);
+  c->profile = on != 0;
+  if (on) c->prof.clear();
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_profile_read(mpcd_ctx *c, char names[][48], int64_t *launches, double *total_ms, int cap) {
+  if (!c) return MPCD_ERR_PARAM;
+  collect_profile(c);
+  int i = 0;
+  for (auto &kv : c->prof) {
+    if (i < cap) {
+      snprintf(names[i], 48, "%s", kv.first.c_str());
+      launches[i] = kv.second.first;
+      total_ms[i] = kv.second.second;
+    }
+    ++i;
+  }
+  return i;
+}
+
+extern "C" int64_t mpcd_launch_count(const mpcd_ctx *c) { return c ? c->launches : -1; }
+
+// initialisation lives in init.cu; it needs the context internals
+#include "init_host.inc"

@@ -1,0 +1,141 @@
+/*
+ * brownian_gb300 — C ABI of the GB300 (sm_103a) MPCD + active-colloid step.
+ *
+ * The reference (shashankgandham/brownian, cpp/) exposes its step as global-state
+ * C++ procedures `void f()` declared at cpp/parameters.hpp:12-14 and driven by
+ * main() in cpp/active_brownian.cpp:9-60.  This library replaces them with an
+ * explicit context: the context owns the device-resident state (structure of
+ * arrays in HBM), every call returns a status, and each reference routine has one
+ * entry point of the same name.  Calls on one context are not thread-safe;
+ * distinct contexts are independent.  All arrays crossing the boundary are plain
+ * host pointers to 0-based xyz triplets of doubles (the reference's 1-based
+ * `point` arrays without their unused slot 0).
+ *
+ * Random numbers are counter-based (Philox4x32-10 keyed by `seed`): the grid
+ * shift of step n, the rotation axis of cell c at step n, the reflection of
+ * particle l off colloid j at substep s, ... are each a fixed function of those
+ * indices, so results do not depend on thread scheduling and a run restarted
+ * from a saved state and step counter continues bit for bit.
+ */
+#ifndef BROWNIAN_GB300_H
+#define BROWNIAN_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+  MPCD_OK = 0,
+  MPCD_ERR_PARAM = 1,     /* invalid parameter or argument                        */
+  MPCD_ERR_CUDA = 2,      /* a CUDA call failed (message in mpcd_last_error)      */
+  MPCD_ERR_CAPACITY = 3,  /* a fixed-capacity table overflowed (no data corrupted) */
+  MPCD_ERR_RANGE = 4,     /* a value left the range the fixed-point sums allow   */
+  MPCD_ERR_STATE = 5,     /* call out of order (e.g. step before setup)           */
+  MPCD_ERR_NOMEM = 6      /* device or host allocation failed                     */
+};
+
+/* precision forms */
+enum { MPCD_FP64 = 0, MPCD_FP32C = 1 };
+
+/* initial-state styles for mpcd_initialize */
+enum {
+  MPCD_INIT_REFERENCE = 0, /* cpp/initialize.cpp: uniform-box velocities, colloid spacing 1.3*sig_colloid,
+                              tumble() orientation of cpp/run.cpp:3-8                                    */
+  MPCD_INIT_PHYSICAL = 1   /* Maxwell-Boltzmann velocities, colloid gap >= init_gap, isotropic orientation */
+};
+
+typedef struct {
+  int Lx, Ly, Lz;          /* periodic box in unit cells (reference: len), each >= 7      */
+  int n_fluid;             /* reference: no_of_fluid                                      */
+  int n_colloid;           /* reference: no_of_colloid                                    */
+  int n_sub;               /* MD substeps per MPCD step (reference: n)                    */
+  double kbt, kbt1;        /* fluid temperature; colloid initial temperature              */
+  double ndt;              /* MPCD time step; the MD substep is dt = ndt / n_sub          */
+  double mass_fl, mass_colloid;
+  double sig_colloid;      /* WCA sigma                                                   */
+  double eps;              /* WCA epsilon                                                 */
+  double sigma;            /* colloid diameter                                            */
+  double I_colloid;        /* colloid moment of inertia                                   */
+  double v0;               /* self-propulsion speed                                       */
+  double theta_deg;        /* SRD rotation angle (reference: 130, cpp/rotation_mpcd.cpp:19) */
+  double Dr;               /* rotational diffusion of the orientation (0: none, as the reference) */
+  uint64_t seed;           /* Philox key                                                  */
+  int precision;           /* MPCD_FP64 or MPCD_FP32C                                     */
+  int max_per_cell;        /* occupancy bound of one cell for the exact cell sums (0: 128) */
+  double vmax;             /* speed bound of one fluid particle for the exact sums (0: 24*sqrt(kbt/mass_fl)) */
+  double init_gap;         /* MPCD_INIT_PHYSICAL: minimum surface gap between colloids    */
+} mpcd_params;
+
+typedef struct {
+  int64_t step;            /* completed MPCD steps                                        */
+  double ke_fluid;         /* cpp/active_brownian.cpp:131                                 */
+  double ke_colloid;       /* :128                                                        */
+  double ang_ke_colloid;   /* :129                                                        */
+  double potential_colloid;/* cpp/update.cpp:23                                           */
+  double energy_colloid;   /* :130                                                        */
+  double momentum[3];      /* fluid + colloid, this step (the reference never resets its sum) */
+  double momentum_fluid[3];
+  double temperature_fluid;/* 2 KE / (3 N kB) in units of kbt                             */
+} mpcd_diag_t;
+
+typedef struct mpcd_ctx mpcd_ctx;
+
+/* ---- lifetime and state (replaces cpp/initialize.cpp:3-29 allocation and the globals of
+ *      cpp/active_brownian.cpp:3-7) ------------------------------------------------------ */
+int mpcd_create(const mpcd_params *p, mpcd_ctx **out);
+int mpcd_destroy(mpcd_ctx *c);
+const char *mpcd_last_error(const mpcd_ctx *c);
+/* launch all work of this context on `stream` (a cudaStream_t; NULL = the context's own) */
+int mpcd_set_stream(mpcd_ctx *c, void *stream);
+
+/* host arrays, 0-based xyz triplets.  Any pointer may be NULL to leave that array as is. */
+int mpcd_set_state(mpcd_ctx *c, const double *pos_fl, const double *vel_fl, const double *pos_colloid,
+                   const double *vel_colloid, const double *ang_vel_colloid, const double *ra);
+int mpcd_get_state(mpcd_ctx *c, double *pos_fl, double *vel_fl, double *pos_colloid, double *vel_colloid,
+                   double *ang_vel_colloid, double *ra, double *f);
+int mpcd_set_step(mpcd_ctx *c, int64_t step);
+int64_t mpcd_get_step(const mpcd_ctx *c);
+
+/* ---- reference routines ------------------------------------------------------------- */
+/* initialize_colloid + initialize_fluid (cpp/initialize.cpp:31-83) and tumble (cpp/run.cpp:3-8) */
+int mpcd_initialize(mpcd_ctx *c, int style);
+/* create_box + neighbour_list_mpcd + neighbour_list_md + compute_force_md, the prologue of
+ * main (cpp/active_brownian.cpp:93-96); required once after set_state/initialize */
+int mpcd_setup(mpcd_ctx *c);
+/* rotation_mpcd (cpp/rotation_mpcd.cpp:3-50) for step counter+1 */
+int mpcd_rotation_mpcd(mpcd_ctx *c);
+/* run (cpp/run.cpp:10-26) */
+int mpcd_run(mpcd_ctx *c);
+/* one pass of the substep body l (1..n_sub) of cpp/active_brownian.cpp:104-113:
+ * update_pos_md, neighbour_list_md, update_pos_mpcd, neighbour_list_mpcd,
+ * fluid_colloid_collision, update_activity_direction, compute_force_md,
+ * update_velocity_colloid */
+int mpcd_substep(mpcd_ctx *c, int l);
+/* nsteps complete MPCD steps (rotation_mpcd, run, n_sub substeps) — the loop of
+ * cpp/active_brownian.cpp:99-132, replayed as one CUDA graph per step */
+int mpcd_step(mpcd_ctx *c, int nsteps);
+/* diagnostics of the state now (cpp/active_brownian.cpp:115-131) */
+int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out);
+
+/* ---- observables for parity checks --------------------------------------------------- */
+/* the last rotation binning: per particle its 1-based cell number as rotation_mpcd computes
+ * it (1 + cell(mod(pos + rr, len)), cpp/rotation_mpcd.cpp:11) and per cell its occupancy
+ * (fluid_no[1..C]); either pointer may be NULL */
+int mpcd_get_rotation_binning(mpcd_ctx *c, int32_t *cell_of, int32_t *occupancy, double *shift);
+/* run(): the rear-shell particle count per colloid of the last run (cnt[1..Nc]) */
+int mpcd_get_shell_count(mpcd_ctx *c, int32_t *cnt);
+
+/* ---- profiling ------------------------------------------------------------------------ */
+/* when enabled, every kernel launch is bracketed by CUDA events on the launch stream */
+int mpcd_profile_enable(mpcd_ctx *c, int on);
+/* per kernel: name, launches, total ms; returns the number of kernels (writes up to cap) */
+int mpcd_profile_read(mpcd_ctx *c, char names[][48], int64_t *launches, double *total_ms, int cap);
+/* kernels launched by this context since creation (all of them are this library's own) */
+int64_t mpcd_launch_count(const mpcd_ctx *c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
