@@ -257,7 +257,7 @@ def run_ours(args, rank, world, dist):
     sim.setup()
     for _ in range(args.steps):
         sim.step(1)
-        sim.diag()
+        dd = sim.diag()
     got = sim.get_state()
     for k in out:
         out[k][...] = got[k]
@@ -294,7 +294,8 @@ def run_ours(args, rank, world, dist):
         "e2e": e2e,
         "gpu_launches": gpu_launches,
         "clocks": clk,
-        "diag_end": {"temperature_fluid": d["temperature_fluid"], "momentum": d["momentum"]},
+        "diag_end": {"temperature_fluid": d["temperature_fluid"], "momentum": d["momentum"],
+                     "wall_events_per_substep": dd["events"] / 10.0, "run_candidates": dd["shell_records"]},
     }
     return line
 
@@ -306,7 +307,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -339,7 +340,7 @@ def main():
 
     # CPU baseline of our arm: start the oracle process before any GPU call (spawn)
     cpu = None
-    if rank == 0:
+    if rank == 0 and args.cpu_steps > 0:
         t0 = time.perf_counter()
         rate, _ = cpu_baseline(1, args.cpu_steps, sample_n)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": 1, "kind": "port",

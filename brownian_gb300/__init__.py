@@ -41,7 +41,7 @@ class Params(C.Structure):
         ("mass_fl", C.c_double), ("mass_colloid", C.c_double), ("sig_colloid", C.c_double),
         ("eps", C.c_double), ("sigma", C.c_double), ("I_colloid", C.c_double), ("v0", C.c_double),
         ("theta_deg", C.c_double), ("Dr", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int),
-        ("max_per_cell", C.c_int), ("vmax", C.c_double), ("init_gap", C.c_double),
+        ("max_per_cell", C.c_int), ("vmax", C.c_double), ("init_gap", C.c_double), ("sort_every", C.c_int),
     ]
 
 
@@ -50,6 +50,7 @@ class Diag(C.Structure):
         ("step", C.c_int64), ("ke_fluid", C.c_double), ("ke_colloid", C.c_double),
         ("ang_ke_colloid", C.c_double), ("potential_colloid", C.c_double), ("energy_colloid", C.c_double),
         ("momentum", C.c_double * 3), ("momentum_fluid", C.c_double * 3), ("temperature_fluid", C.c_double),
+        ("events", C.c_int64), ("shell_records", C.c_int64),
     ]
 
     def as_dict(self):
@@ -116,13 +117,14 @@ class Simulation:
 
     def __init__(self, L, n_fluid, n_colloid, *, n_sub=10, kbt=1.0, kbt1=1.0, ndt=0.1, mass_fl=1.0,
                  mass_colloid=654.1, sig_colloid=5.0, eps=1.0, sigma=None, I_colloid=None, v0=0.0,
-                 theta_deg=130.0, Dr=0.0, seed=77777, precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5):
+                 theta_deg=130.0, Dr=0.0, seed=77777, precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5,
+                 sort_every=0):
         Lx, Ly, Lz = (L, L, L) if np.isscalar(L) else L
         sigma = 0.8 * sig_colloid if sigma is None else sigma          # cpp/active_brownian.cpp:7
         I_colloid = 0.1 * mass_colloid * sigma * sigma if I_colloid is None else I_colloid
         self.params = Params(Lx, Ly, Lz, n_fluid, n_colloid, n_sub, kbt, kbt1, ndt, mass_fl, mass_colloid,
                              sig_colloid, eps, sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell,
-                             vmax, init_gap)
+                             vmax, init_gap, sort_every)
         self.N, self.Nc = n_fluid, n_colloid
         self.C = Lx * Ly * Lz
         self.dt = ndt / n_sub

@@ -66,23 +66,33 @@ struct Dim {
   long long lo_bits;    // bits of 2^-30 L: for L > a >= 2^-30 L, mod(a, L) == a
   long long L_bits;     // bits of L
   long long img_bits;   // bits of 0.49 L: |a| < 0.49 L  =>  img(a, L) == a
+  long long img1_bits;  // bits of 0.51 L: 0.51 L < |a| < 1.49 L  =>  img(a, L) == a - L sign(a)
+  long long img2_bits;  // bits of 1.49 L
 };
 
 // The reference's mod(a, L) = a - L*lround((a - L/2)/L) (cpp/parameters.hpp:75).
-// For a in [2^-30 L, L) the quotient rounds into (-1/2, 1/2), so the result is a;
-// everything else (boundary crossings, a exactly 0 or L, tiny values) takes the
-// reference's own arithmetic, including mod(0, L) == L.
+// The quotient rounds to 0 for a in [2^-30 L, L) (result a), to 1 for a in
+// [L, 1.49 L) (result a - L*1) and to -1 for a in (-0.49 L, -0] (result
+// a - L*(-1)); those subtractions are the reference's own, so the results are
+// bit-identical.  Only a in [0, 2^-30 L), where rounding decides, and values
+// further out take the reference's division (mod(0, L) == L comes from there).
 __device__ __forceinline__ double ref_mod(double a, const Dim &d) {
   long long b = dbits(a);
   if (b >= d.lo_bits && b < d.L_bits) return a;
+  if (b >= d.L_bits && b < d.img2_bits) return __dsub_rn(a, d.L);
+  if (b < 0 && (b & 0x7FFFFFFFFFFFFFFFll) < d.img_bits) return __dsub_rn(a, -d.L);
   double q = __ddiv_rn(__dsub_rn(a, d.halfL), d.L);
   return __dsub_rn(a, __dmul_rn(d.L, (double)llround(q)));
 }
 
-// The reference's img(a, L) = a - L*lround(a/L) (cpp/parameters.hpp:76).
+// The reference's img(a, L) = a - L*lround(a/L) (cpp/parameters.hpp:76).  For
+// |a| < 0.49 L the quotient rounds to 0 (result a); for 0.51 L < |a| < 1.49 L it
+// rounds to sign(a) (result a - L sign(a), one subtraction as in the reference);
+// only the bands around L/2 and beyond take the division.
 __device__ __forceinline__ double ref_img(double a, const Dim &d) {
   long long b = dbits(a) & 0x7FFFFFFFFFFFFFFFll;
   if (b < d.img_bits) return a;
+  if (b > d.img1_bits && b < d.img2_bits) return __dsub_rn(a, a > 0 ? d.L : -d.L);
   return __dsub_rn(a, __dmul_rn(d.L, (double)llround(__ddiv_rn(a, d.L))));
 }
 

@@ -50,8 +50,11 @@ struct mpcd_ctx {
   DevAlloc mem;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaGraphExec_t step_exec = nullptr;
-  int step_launches = 0;
+  cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sorts][fluid buffer]
+  int step_launches[2][2] = {{0, 0}, {0, 0}};
+  int fbuf = 0;                  // fluid buffer holding the current state
+  long long host_step = 0;       // completed steps (mirror of the device counter)
+  int sort_every = 10;           // counting sort by cell every this many steps
   bool setup_done = false;
   std::string err;
   int64_t launches = 0;
@@ -64,6 +67,9 @@ struct mpcd_ctx {
   double *part = nullptr;        // reduction partials
   int part_blocks = 256;
   double *staging = nullptr;     // AoS transfer buffer, allocated on first use
+  int phase = 0;                 // 0: between steps; 1: rotation_mpcd of the next step done
+  int next_sub = 1;              // routine-level: the substep mpcd_substep expects
+  int nblk = 0;                  // 256-cell blocks of the counting sort
 };
 
 static int fail(mpcd_ctx *c, int code, const std::string &m) {
@@ -90,6 +96,8 @@ static Dim make_dim(int L) {
   d.lo_bits = dbits_h(ldexp(d.L, -30));
   d.L_bits = dbits_h(d.L);
   d.img_bits = dbits_h(0.49 * d.L);
+  d.img1_bits = dbits_h(0.51 * d.L);
+  d.img2_bits = dbits_h(1.49 * d.L);
   return d;
 }
 
@@ -124,43 +132,66 @@ static void launch(mpcd_ctx *c, const char *name, void (*k)(KArgs...), dim3 g, d
 
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-static int colloid_grid(const mpcd_ctx *c) { return (int)blocks_for((long long)c->S.Nc * 32, 128); }
+static int colloid_grid(const mpcd_ctx *c) {
+  int g = (int)blocks_for((long long)c->S.Nc * 32, 128);
+  return g > 0 ? g : 1;
+}
 
-static void enq_stream(mpcd_ctx *c, int flags, int l) {
+static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
+  const int fb = c->fbuf;
   const char *name = flags == (F_STREAM | F_COLLIDE) ? "k_stream"
                      : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
                      : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
-  launch(c, name, stream_kernel(flags), blocks_for(c->S.N, 256), 256, c->S, l);
+  // the streaming passes of substeps carry the colloid forces and the next cell
+  // table in their first blocks (8 colloid warps per block)
+  int naux = (flags & F_STREAM) ? (int)blocks_for(c->S.Nc, 8) : 0;
+  launch(c, name, stream_kernel(flags), naux + blocks_for(c->S.N, 256), 256, c->S, l, naux, act, fb);
+  // the particles it left near a sphere surface, one per lane
+  launch(c, "k_events", event_kernel(flags), 1024, 128, c->S, l, fb);
 }
 
-static void enq_colloid(mpcd_ctx *c, int mode, int l) {
-  int g = colloid_grid(c);
-  launch(c, "k_colloid", k_colloid, g > 0 ? g : 1, 128, c->S, mode, l);
+static void enq_fin(mpcd_ctx *c, int mode, int l) {
+  // one thread per colloid, one warp per block so the FP64 work spreads over SMs
+  unsigned g = blocks_for(c->S.Nc, 32);
+  launch(c, "k_fin", k_fin, g > 0 ? g : 1, 32, c->S, mode, l);
 }
 
-static void enq_rotation(mpcd_ctx *c) {
+static unsigned prep_blocks(const SysF64 &S) { return blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256); }
+
+static bool sorts_at(const mpcd_ctx *c, long long step) { return c->sort_every > 0 && step % c->sort_every == 0; }
+
+// rotation_mpcd: per-cell map (and occupancy prefix), then the rotation, every
+// sort_every steps fused with the counting-sort scatter into the other buffer
+static void enq_rotation(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
-  launch(c, "k_cell_prep", k_cell_prep, blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256), 256, S);
-  launch(c, "k_rotate", k_rotate, blocks_for(S.N, 256), 256, S);
+  launch(c, "k_cell_prep", k_cell_prep, prep_blocks(S), 256, S);
+  if (sort) {
+    launch(c, "k_scan_blocks", k_scan_blocks, 1, 1024, S, c->nblk);
+    launch(c, "k_rotate_sort", k_rotate_sort, blocks_for(S.N, 256), 256, S, c->fbuf, 1 - c->fbuf);
+    c->fbuf = 1 - c->fbuf;
+  } else {
+    launch(c, "k_rotate", k_rotate, blocks_for(S.N, 256), 256, S, c->fbuf);
+  }
 }
 
 static void enq_run_fluid(mpcd_ctx *c) {
   const SysF64 &S = c->S;
   if (S.Nc == 0) return;
-  launch(c, "k_run_shell", k_run_shell, 152 * 4, 256, S);
-  launch(c, "k_run_kick", k_run_kick, 152 * 4, 256, S);
+  launch(c, "k_run_shell", k_run_shell, 152 * 4, 256, S, c->fbuf);
+  launch(c, "k_run_kick", k_run_kick, 152 * 4, 256, S, c->fbuf);
 }
 
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
-static void enq_step(mpcd_ctx *c) {
+static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
-  enq_rotation(c);
+  enq_rotation(c, sort);
   enq_run_fluid(c);
+  enq_fin(c, M_KICK | M_ADVANCE, 0);
   for (int l = 1; l <= n; ++l) {
-    enq_colloid(c, (l == 1 ? M_KICK : M_FINISH) | M_ADVANCE, l);
-    enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l);
+    // the orientation update of substep l-1 rides on the streaming pass of substep l
+    enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l, l >= 2);
+    enq_fin(c, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
   }
-  enq_colloid(c, M_FINISH, n + 1);
   launch(c, "k_end_step", k_end_step, 1, 32, c->S);
 }
 
@@ -208,10 +239,12 @@ static int check_device(mpcd_ctx *c) {
 }
 
 static int drop_graph(mpcd_ctx *c) {
-  if (c->step_exec) {
-    cudaGraphExecDestroy(c->step_exec);
-    c->step_exec = nullptr;
-  }
+  for (int s = 0; s < 2; ++s)
+    for (int b = 0; b < 2; ++b)
+      if (c->step_exec[s][b]) {
+        cudaGraphExecDestroy(c->step_exec[s][b]);
+        c->step_exec[s][b] = nullptr;
+      }
   return MPCD_OK;
 }
 
@@ -241,6 +274,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.Cpad = S.C + p.Lx * p.Ly + 2 * p.Lx + 4;
   S.n_sub = p.n_sub;
   S.dx = make_dim(p.Lx); S.dy = make_dim(p.Ly); S.dz = make_dim(p.Lz);
+  S.Lxf = (float)p.Lx; S.Lyf = (float)p.Ly; S.Lzf = (float)p.Lz;
   S.key = make_uint2((uint32_t)p.seed, (uint32_t)(p.seed >> 32));
   // constants, evaluated with the host libm exactly as the reference writes them
   const double dt = p.ndt / (double)p.n_sub;
@@ -256,6 +290,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.ufc = 4.0 * p.eps * (pow(p.sig_colloid / S.r_cutoff, 12) - pow(p.sig_colloid / S.r_cutoff, 6)) + S.fc * S.r_cutoff;
   S.sig12 = pow(p.sig_colloid, 12);
   S.sig6 = pow(p.sig_colloid, 6);
+  S.rcf = (float)S.r_cutoff * 1.0001f + 1e-4f;
   const double dt2 = dt * dt;
   S.ddt = 0.5 * dt2 / p.mass_colloid;                      // cpp/update.cpp:48
   S.dtb2 = dt / (p.mass_colloid * 2);                      // cpp/update.cpp:63
@@ -266,36 +301,53 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.two_pi = 4.0 * asin(1.0);
   S.sqrt_kt_m = sqrt(p.kbt / p.mass_fl);
   S.m_beta = p.mass_fl / p.kbt;
+  S.inv_m_beta = p.kbt / p.mass_fl;
   S.cs = 3.0 * p.kbt * dt2 / p.mass_fl;
-  const double margin = 0.5;
-  S.rT_coll = (float)(p.sigma * 0.5 + margin + 0.01);
-  S.rT_shell = (float)(p.sigma * 0.5 + 0.5 + margin + 0.01);
-  S.disp_margin2 = margin * margin;
+  // cell-table reach: sphere (or run() shell) + a wall collision's displacement
+  // (dt/2 (|v| + |v'|), 0.1 needs speeds near 20 kT units) + a colloid's move in one
+  // substep + FP32 slack; both displacements are checked on the device
+  const double pmargin = 0.1, cmargin = 0.05;
+  S.r_coll = (float)(p.sigma * 0.5);
+  S.r_shell = (float)(p.sigma * 0.5 + 0.5);
+  S.rT_coll = (float)(p.sigma * 0.5 + pmargin + cmargin + 0.01);
+  S.rT_shell = (float)(p.sigma * 0.5 + 0.5 + pmargin + cmargin + 0.01);
+  S.disp_margin2 = pmargin * pmargin;
+  S.cmargin2 = cmargin * cmargin;
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
+  c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   const double vmax = p.vmax > 0 ? p.vmax : 24.0 * sqrt(p.kbt / p.mass_fl);
   const double wmax = vmax * dt;
-  S.kw = 62 - (int)ceil(log2((double)S.max_per_cell * wmax));
-  S.kw2 = 62 - (int)ceil(log2((double)S.max_per_cell * 3.0 * wmax * wmax));
+  // one scale for the sums of w and |w|^2: max_per_cell * max(wmax, 3 wmax^2) * 2^kw < 2^62
+  const double wbound = wmax > 3.0 * wmax * wmax ? wmax : 3.0 * wmax * wmax;
+  S.kw = 62 - (int)ceil(log2((double)S.max_per_cell * wbound));
+  if (S.kw > 62) S.kw = 62;
   S.inv_sw = ldexp(1.0, -S.kw);
-  S.inv_sw2 = ldexp(1.0, -S.kw2);
   S.wlim_bits = dbits_h(wmax);
-  S.w2lim_bits = dbits_h(3.0 * wmax * wmax);
 
   DevAlloc &m = c->mem;
   const size_t N = S.N, Nc = S.Nc > 0 ? S.Nc : 1;
-  S.px = m.get<double>(N); S.py = m.get<double>(N); S.pz = m.get<double>(N);
-  S.wx = m.get<double>(N); S.wy = m.get<double>(N); S.wz = m.get<double>(N);
+  for (int b = 0; b < 2; ++b) {
+    for (int k = 0; k < 6; ++k) S.fl[b][k] = m.get<double>(N);
+    S.pid[b] = m.get<int>(N);
+  }
+  S.newpos = m.get<int>(N);
   S.rotcell = m.get<int>(N);
+  c->nblk = (int)blocks_for(S.Cpad, 256);
+  S.cell_off = m.get<int>(S.Cpad);
+  S.cursor = m.get<int>(S.Cpad);
+  S.blk_off = m.get<int>(prep_blocks(S) + 1);
   S.acc = m.get<CellAcc>(S.Cpad);
   S.cell_ab = m.get<double>((size_t)S.C * 12);
   for (int b = 0; b < 2; ++b) {
     S.X[b] = m.get<double>(3 * Nc);
     S.Xf[b] = m.get<float4>(Nc);
     S.cbox[b] = m.get<int>(Nc);
-    S.Tcnt[b] = m.get<int>(S.C);
+    S.Tcnt[b] = m.get<unsigned long long>(S.C);
     S.Tlist[b] = m.get<uint16_t>((size_t)S.C * TCAP);
   }
   S.V = m.get<double>(3 * Nc); S.W = m.get<double>(3 * Nc); S.ra = m.get<double>(3 * Nc); S.f = m.get<double>(3 * Nc);
+  S.fnew = m.get<double>(3 * Nc);
+  S.xi = m.get<double>(3 * Nc);
   S.exch = m.get<ExchAcc>(Nc);
   S.shell_cnt = m.get<int>(Nc);
   S.pot_part = m.get<double>(Nc);
@@ -304,6 +356,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   double est = (double)S.Nc * (4.0 / 3.0 * M_PI * rsh * rsh * rsh * density * 2.0 + 64.0);
   S.shell_cap = (int)(est < (double)S.N ? est : (double)S.N) + 1024;
   S.shell = m.get<ShellRec>(S.shell_cap);
+  S.events_cap = S.N / 16 + 65536;
+  S.events = m.get<int>(S.events_cap);
   S.ss = m.get<StepState>(1);
   c->inv_n = m.get<double>(S.max_per_cell + 1);
   S.inv_n = c->inv_n;
@@ -405,31 +459,39 @@ static int ensure_staging(mpcd_ctx *c) {
 
 // host AoS xyz -> device SoA: one copy of the caller's buffer (a DMA when it is
 // pinned), then a transpose on the device
-static int upload_soa(mpcd_ctx *c, const double *aos, double *dx, double *dy, double *dz, double scale) {
+static int upload_soa(mpcd_ctx *c, const double *aos, double *dx, double *dy, double *dz, int *id, int *newpos,
+                      double scale) {
   int r;
   if ((r = ensure_staging(c))) return r;
   const int N = c->S.N;
   CUDA_OK(c, cudaMemcpyAsync(c->staging, aos, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, c->stream));
-  launch(c, "k_aos_to_soa", k_aos_to_soa, blocks_for(N, 256), 256, (const double *)c->staging, dx, dy, dz, N, scale);
+  launch(c, "k_aos_to_soa", k_aos_to_soa, blocks_for(N, 256), 256, (const double *)c->staging, dx, dy, dz, id, newpos,
+         N, scale);
   return MPCD_OK;
 }
 
-static int download_soa(mpcd_ctx *c, double *aos, const double *dx, const double *dy, const double *dz, double div) {
+static int download_soa(mpcd_ctx *c, double *aos, const double *dx, const double *dy, const double *dz, const int *id,
+                        double div) {
   int r;
   if ((r = ensure_staging(c))) return r;
   const int N = c->S.N;
-  launch(c, "k_soa_to_aos", k_soa_to_aos, blocks_for(N, 256), 256, c->staging, dx, dy, dz, N, div);
+  launch(c, "k_soa_to_aos", k_soa_to_aos, blocks_for(N, 256), 256, c->staging, dx, dy, dz, id, N, div);
   CUDA_OK(c, cudaMemcpyAsync(aos, c->staging, sizeof(double) * 3 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
   CUDA_OK(c, cudaStreamSynchronize(c->stream));
   return MPCD_OK;
 }
 
+// the fluid buffer holding the current state
+static Fluid cur_fluid(const mpcd_ctx *c) { return fluid_at(c->S, c->fbuf); }
+
 static int invalidate_tables(mpcd_ctx *c) {
   const SysF64 &S = c->S;
-  for (int b = 0; b < 2; ++b) CUDA_OK(c, cudaMemsetAsync(S.Tcnt[b], 0, sizeof(int) * S.C, c->stream));
+  for (int b = 0; b < 2; ++b) CUDA_OK(c, cudaMemsetAsync(S.Tcnt[b], 0, sizeof(unsigned long long) * S.C, c->stream));
   CUDA_OK(c, cudaMemsetAsync(S.acc, 0, sizeof(CellAcc) * S.Cpad, c->stream));
   if (S.Nc) CUDA_OK(c, cudaMemsetAsync(S.exch, 0, sizeof(ExchAcc) * S.Nc, c->stream));
   c->setup_done = false;
+  c->phase = 0;
+  c->next_sub = 1;
   return MPCD_OK;
 }
 
@@ -439,8 +501,14 @@ extern "C" int mpcd_set_state(mpcd_ctx *c, const double *pos_fl, const double *v
   int r;
   if ((r = read_ss(c))) return r;
   const SysF64 &S = c->S;
-  if (pos_fl && (r = upload_soa(c, pos_fl, S.px, S.py, S.pz, 0.0))) return r;
-  if (vel_fl && (r = upload_soa(c, vel_fl, S.wx, S.wy, S.wz, S.dt))) return r;  // w = fl(v*dt)
+  if ((pos_fl == nullptr) != (vel_fl == nullptr))
+    return fail(c, MPCD_ERR_PARAM, "pos_fl and vel_fl are set together (the device keeps particles in cell order)");
+  c->phase = 0;
+  if (pos_fl) {
+    Fluid F = cur_fluid(c);
+    if ((r = upload_soa(c, pos_fl, F.x, F.y, F.z, F.id, S.newpos, 0.0))) return r;
+    if ((r = upload_soa(c, vel_fl, F.wx, F.wy, F.wz, nullptr, nullptr, S.dt))) return r;  // w = fl(v*dt)
+  }
   CUDA_OK(c, cudaStreamSynchronize(c->stream));
   if (S.Nc) {
     if (pos_colloid && (r = upload_colloid_pos(c, pos_colloid))) return r;
@@ -457,8 +525,9 @@ extern "C" int mpcd_get_state(mpcd_ctx *c, double *pos_fl, double *vel_fl, doubl
   int r;
   if ((r = read_ss(c))) return r;
   const SysF64 &S = c->S;
-  if (pos_fl && (r = download_soa(c, pos_fl, S.px, S.py, S.pz, 0.0))) return r;
-  if (vel_fl && (r = download_soa(c, vel_fl, S.wx, S.wy, S.wz, S.dt))) return r;  // v = w/dt
+  Fluid F = cur_fluid(c);
+  if (pos_fl && (r = download_soa(c, pos_fl, F.x, F.y, F.z, F.id, 0.0))) return r;
+  if (vel_fl && (r = download_soa(c, vel_fl, F.wx, F.wy, F.wz, F.id, S.dt))) return r;  // v = w/dt
   if (S.Nc) {
     int b = cur_buf(c);
     if (pos_colloid) CUDA_OK(c, cudaMemcpy(pos_colloid, S.X[b], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
@@ -509,12 +578,15 @@ extern "C" int mpcd_setup(mpcd_ctx *c) {
   CUDA_OK(c, cudaMemcpyAsync(&c->S.ss->err, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   // create_box + neighbour_list_md + compute_force_md: forces at the current positions,
   // cell table around each colloid (cpp/active_brownian.cpp:93-96)
-  enq_colloid(c, M_SETUP, 1);
+  launch(c, "k_colloid_setup", k_colloid_setup, colloid_grid(c), 128, c->S);
   // neighbour_list_mpcd seen from the fluid: run() candidates of the first step, and the
   // SRD binning of its rotation_mpcd
-  enq_stream(c, F_SHELL | F_BINROT, 0);
+  c->host_step = c->ss_host->step;
+  enq_stream(c, F_SHELL | F_BINROT, 0, 0);
   if ((r = check_device(c))) return r;
   c->setup_done = true;
+  c->phase = 0;
+  c->next_sub = 1;
   return MPCD_OK;
 }
 
@@ -527,15 +599,20 @@ static int need_setup(mpcd_ctx *c) {
 extern "C" int mpcd_rotation_mpcd(mpcd_ctx *c) {
   int r;
   if ((r = need_setup(c))) return r;
-  enq_rotation(c);
+  if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "rotation_mpcd starts a step: finish the substeps of this one");
+  enq_rotation(c, sorts_at(c, c->host_step));
+  c->phase = 1;
+  c->next_sub = 0;
   return check_device(c);
 }
 
 extern "C" int mpcd_run(mpcd_ctx *c) {
   int r;
   if ((r = need_setup(c))) return r;
+  if (c->phase != 1 || c->next_sub != 0) return fail(c, MPCD_ERR_STATE, "run follows rotation_mpcd of the same step");
   enq_run_fluid(c);
-  enq_colloid(c, M_KICK, 1);
+  enq_fin(c, M_KICK, 0);
+  c->next_sub = 1;
   return check_device(c);
 }
 
@@ -544,13 +621,20 @@ extern "C" int mpcd_substep(mpcd_ctx *c, int l) {
   if ((r = need_setup(c))) return r;
   const int n = c->S.n_sub;
   if (l < 1 || l > n) return fail(c, MPCD_ERR_PARAM, "substep out of range");
-  enq_colloid(c, M_ADVANCE, l);   // update_pos_md, neighbour_list_md (+ cell table)
-  // update_pos_mpcd, neighbour_list_mpcd, fluid_colloid_collision (fluid side)
-  enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l);
-  // end of fluid_colloid_collision, update_activity_direction, compute_force_md,
-  // update_velocity_colloid
-  enq_colloid(c, M_FINISH, l + 1);
-  if (l == n) launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+  if (c->phase != 1 || c->next_sub != l)
+    return fail(c, MPCD_ERR_STATE, "substeps follow rotation_mpcd and run, in order 1..n_sub");
+  enq_fin(c, M_ADVANCE, l - 1);   // update_pos_md, neighbour_list_md
+  // update_pos_mpcd, neighbour_list_mpcd, fluid_colloid_collision (fluid side), and
+  // compute_force_md at the new colloid positions
+  enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l, 0);
+  // end of fluid_colloid_collision, update_activity_direction, update_velocity_colloid
+  enq_fin(c, M_FINISH | M_ACT, l);
+  c->next_sub = l + 1;
+  if (l == n) {
+    launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+    c->phase = 0;
+    c->host_step += 1;
+  }
   return check_device(c);
 }
 
@@ -558,25 +642,35 @@ extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
   int r;
   if ((r = need_setup(c))) return r;
   if (nsteps < 0) return MPCD_ERR_PARAM;
+  if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "a step begun routine by routine is unfinished");
   if (c->profile) {
-    for (int s = 0; s < nsteps; ++s) enq_step(c);
+    for (int s = 0; s < nsteps; ++s) {
+      enq_step(c, sorts_at(c, c->host_step));
+      c->host_step += 1;
+    }
     return check_device(c);
   }
-  if (!c->step_exec) {
-    cudaGraph_t g;
-    int64_t before = c->launches;
-    CUDA_OK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enq_step(c);
-    CUDA_OK(c, cudaStreamEndCapture(c->stream, &g));
-    c->step_launches = (int)(c->launches - before);
-    c->launches = before;
-    cudaError_t e = cudaGraphInstantiate(&c->step_exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(c, MPCD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  }
   for (int s = 0; s < nsteps; ++s) {
-    CUDA_OK(c, cudaGraphLaunch(c->step_exec, c->stream));
-    c->launches += c->step_launches;
+    // one graph per (sorts this step, fluid buffer): the kernels' buffer arguments
+    // are fixed at capture
+    const int sort = sorts_at(c, c->host_step) ? 1 : 0, b = c->fbuf;
+    if (!c->step_exec[sort][b]) {
+      cudaGraph_t g;
+      int64_t before = c->launches;
+      CUDA_OK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      enq_step(c, sort != 0);
+      CUDA_OK(c, cudaStreamEndCapture(c->stream, &g));
+      c->fbuf = b;  // capture only recorded the launches
+      c->step_launches[sort][b] = (int)(c->launches - before);
+      c->launches = before;
+      cudaError_t e = cudaGraphInstantiate(&c->step_exec[sort][b], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(c, MPCD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    CUDA_OK(c, cudaGraphLaunch(c->step_exec[sort][b], c->stream));
+    c->launches += c->step_launches[sort][b];
+    if (sort) c->fbuf = 1 - b;
+    c->host_step += 1;
   }
   return check_device(c);
 }
@@ -589,7 +683,7 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   if ((r = need_setup(c))) return r;
   const SysF64 &S = c->S;
   launch(c, "k_diag_fluid", k_diag_fluid, c->part_blocks, 256, S, c->part);
-  if (S.Nc) enq_colloid(c, M_POT, 1);
+  if (S.Nc) launch(c, "k_colloid_pot", k_colloid_pot, colloid_grid(c), 128, S);
   if ((r = check_device(c))) return r;
   std::vector<double> part((size_t)c->part_blocks * 5);
   CUDA_OK(c, cudaMemcpy(part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
@@ -605,6 +699,11 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   for (int k = 0; k < 3; ++k) out->momentum_fluid[k] = m * sw[k] / S.dt;
   out->ke_fluid = 0.5 * m * s2 / (S.dt * S.dt);
   out->temperature_fluid = n > 0 ? 2.0 * out->ke_fluid / (3.0 * n) / c->p.kbt : 0;
+  // wall-collision candidates handled exactly, summed since the last call
+  out->events = c->ss_host->ev_total;
+  const long long zero64 = 0;
+  CUDA_OK(c, cudaMemcpy(&c->S.ss->ev_total, &zero64, sizeof zero64, cudaMemcpyHostToDevice));
+  out->shell_records = c->ss_host->nshell;
   double mom[3] = {out->momentum_fluid[0], out->momentum_fluid[1], out->momentum_fluid[2]};
   if (S.Nc) {
     std::vector<double> V(3 * S.Nc), W(3 * S.Nc), pot(S.Nc);
@@ -634,10 +733,12 @@ extern "C" int mpcd_get_rotation_binning(mpcd_ctx *c, int32_t *cell_of, int32_t 
   if ((r = need_setup(c))) return r;
   const SysF64 &S = c->S;
   if ((r = read_ss(c))) return r;
-  std::vector<int> rc(S.N);
+  if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "the binning is that of the next step; call between steps");
+  std::vector<int> rc(S.N), id(S.N);
   CUDA_OK(c, cudaMemcpy(rc.data(), S.rotcell, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
+  CUDA_OK(c, cudaMemcpy(id.data(), cur_fluid(c).id, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
   if (cell_of)
-    for (int i = 0; i < S.N; ++i) cell_of[i] = rc[i] + 1;
+    for (int i = 0; i < S.N; ++i) cell_of[id[i]] = rc[i] + 1;
   if (occupancy) {
     for (int b = 0; b < S.C; ++b) occupancy[b] = 0;
     for (int i = 0; i < S.N; ++i)

@@ -11,9 +11,10 @@ namespace bgb {
 // Maxwell-Boltzmann with standard deviation vscale (Box-Muller).  Writes the raw
 // velocity into wx/wy/wz; k_vfinish turns it into a displacement.
 __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, double vscale, double rmin,
-                                                   int max_attempts) {
+                                                   int max_attempts, int fb) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.N) return;
+  const Fluid F = fluid_at(S, fb);
   const int b = (int)((S.ss->step * S.n_sub - 1) & 1);
   const double *Xc = S.X[b];
   const float4 *xs = S.Xf[b];
@@ -41,7 +42,9 @@ __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, d
     }
   }
   if (!placed) atomicOr(&S.ss->err, ERRB_OCCUPANCY);
-  S.px[i] = tx; S.py[i] = ty; S.pz[i] = tz;
+  F.x[i] = tx; F.y[i] = ty; F.z[i] = tz;
+  F.id[i] = i;
+  S.newpos[i] = i;
   uint4 r = draw4(S.key, DOM_INIT_FVEL, 0, (uint32_t)(i + 1), 0, 0);
   double vx, vy, vz;
   if (style == 0) {
@@ -55,15 +58,16 @@ __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, d
     sincospi(2.0 * u01(r.w), &s1, &c1);
     vx = r0 * c0 * vscale; vy = r0 * s0 * vscale; vz = r1 * c1 * vscale;
   }
-  S.wx[i] = vx; S.wy[i] = vy; S.wz[i] = vz;
+  F.wx[i] = vx; F.wy[i] = vy; F.wz[i] = vz;
 }
 
 // per-block sums of the raw velocities, fixed order
-__global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part) {
+__global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part, int fb) {
   __shared__ double sh[3][256];
   double a[3] = {0, 0, 0};
+  const Fluid F = fluid_at(S, fb);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.N; i += gridDim.x * blockDim.x) {
-    a[0] += S.wx[i]; a[1] += S.wy[i]; a[2] += S.wz[i];
+    a[0] += F.wx[i]; a[1] += F.wy[i]; a[2] += F.wz[i];
   }
   for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] = a[k];
   __syncthreads();
@@ -77,33 +81,39 @@ __global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part) {
 }
 
 // vel = vel - avr_vel, then the stored displacement w = fl(vel*dt)
-__global__ void __launch_bounds__(256) k_vfinish(const SysF64 S, double ax, double ay, double az) {
+__global__ void __launch_bounds__(256) k_vfinish(const SysF64 S, double ax, double ay, double az, int fb) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.N) return;
-  S.wx[i] = __dmul_rn(__dsub_rn(S.wx[i], ax), S.dt);
-  S.wy[i] = __dmul_rn(__dsub_rn(S.wy[i], ay), S.dt);
-  S.wz[i] = __dmul_rn(__dsub_rn(S.wz[i], az), S.dt);
+  const Fluid F = fluid_at(S, fb);
+  F.wx[i] = __dmul_rn(__dsub_rn(F.wx[i], ax), S.dt);
+  F.wy[i] = __dmul_rn(__dsub_rn(F.wy[i], ay), S.dt);
+  F.wz[i] = __dmul_rn(__dsub_rn(F.wz[i], az), S.dt);
 }
 
-// AoS xyz triplets (the reference's point arrays) <-> the device's SoA, with the
-// velocity <-> displacement conversion w = fl(v*dt), v = w/dt.  scale: 0 copies,
-// otherwise multiplies (to SoA) or divides (from SoA) by it.
-__global__ void __launch_bounds__(256) k_aos_to_soa(const double *aos, double *x, double *y, double *z, int n,
-                                                   double scale) {
+// AoS xyz triplets (the reference's point arrays, in particle order) <-> the
+// device's SoA (in cell order), with the velocity <-> displacement conversion
+// w = fl(v*dt), v = w/dt.  scale: 0 copies, otherwise multiplies (to SoA) or
+// divides (from SoA) by it.  Upload puts particle i at position i (id[i] = i when
+// id is given); download scatters position i back to particle id[i].
+__global__ void __launch_bounds__(256) k_aos_to_soa(const double *aos, double *x, double *y, double *z, int *id,
+                                                   int *newpos, int n, double scale) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double a = aos[3 * (size_t)i], b = aos[3 * (size_t)i + 1], c = aos[3 * (size_t)i + 2];
   if (scale != 0.0) { a = __dmul_rn(a, scale); b = __dmul_rn(b, scale); c = __dmul_rn(c, scale); }
   x[i] = a; y[i] = b; z[i] = c;
+  if (id) id[i] = i;
+  if (newpos) newpos[i] = i;
 }
 
 __global__ void __launch_bounds__(256) k_soa_to_aos(double *aos, const double *x, const double *y, const double *z,
-                                                   int n, double scale) {
+                                                   const int *id, int n, double scale) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double a = x[i], b = y[i], c = z[i];
   if (scale != 0.0) { a = __ddiv_rn(a, scale); b = __ddiv_rn(b, scale); c = __ddiv_rn(c, scale); }
-  aos[3 * (size_t)i] = a; aos[3 * (size_t)i + 1] = b; aos[3 * (size_t)i + 2] = c;
+  const size_t o = 3 * (size_t)id[i];
+  aos[o] = a; aos[o + 1] = b; aos[o + 2] = c;
 }
 
 }  // namespace bgb

@@ -23,7 +23,7 @@ constexpr int SHELL_J = 8;   // colloids per run() candidate record
 // one run() candidate: a particle whose binned cell is in the 342-cell block of
 // each listed colloid and which lies within sigma/2 + 1/2 of it
 struct ShellRec {
-  int p;
+  int p;  // particle id
   uint8_t n, pass;
   uint16_t j[SHELL_J];
 };
@@ -47,6 +47,8 @@ struct StepState {
   long long step;   // completed MPCD steps
   int err;          // error bits
   int nshell;       // run() candidate records written
+  int nevents;      // particles the streaming pass left to k_events
+  long long ev_total;  // events summed over substeps (diagnostics)
   double rr[3];     // grid shift of the SRD binning the next streaming pass performs
 };
 
@@ -54,6 +56,7 @@ struct SysF64 {
   // sizes
   int N, Nc, C, Cpad;
   int Lx, Ly, Lz, n_sub;
+  float Lxf, Lyf, Lzf;
   Dim dx, dy, dz;
   uint2 key;
   // constants (host-computed with the host libm, as the reference computes them)
@@ -62,6 +65,7 @@ struct SysF64 {
   double sig2q;        // pow(sigma, 2)*0.25            cpp/fluid_colloid_collision.cpp:35
   double rsh2;         // pow(sigma*0.5 + 0.5, 2)        cpp/run.cpp:18
   double r_cutoff, fc, ufc, sig12, sig6, eps, sig_colloid;
+  float rcf;           // FP32 prefilter radius of the WCA pair search
   double ddt;          // 0.5*dt*dt/mass_colloid         cpp/update.cpp:48
   double dtb2;         // dt/(mass_colloid*2)            cpp/update.cpp:63
   double v0, Dr, rotdiff_s;
@@ -69,18 +73,27 @@ struct SysF64 {
   double two_pi;       // 4.0*asin(1.0)
   double sqrt_kt_m;    // sqrt(kbt/mass_fl)
   double m_beta;       // mass_fl/kbt
+  double inv_m_beta;   // kbt/mass_fl
   double cs;           // 3 kbt dt^2 / mass_fl (thermostat in displacement units)
   double inv_dt;
-  float rT_coll, rT_shell;   // cell-table reach (with margin), FP32
-  double disp_margin2;       // squared bound on collision displacement
-  int kw, kw2;               // fixed-point scales of the cell sums
-  double inv_sw, inv_sw2;    // 2^-kw, 2^-kw2
+  float rT_coll, rT_shell;   // cell-table reach (sphere or shell + margins), FP32
+  float r_coll, r_shell;     // sphere radius sigma/2 and shell radius sigma/2 + 1/2, FP32
+  double disp_margin2;       // squared bound on the displacement of one wall collision
+  double cmargin2;           // squared bound on a colloid's displacement in one substep
+  int kw;                    // fixed-point scale of the cell sums (w and |w|^2)
+  double inv_sw;             // 2^-kw
   long long wlim_bits;       // |w| component bound (bits of vmax*dt)
-  long long w2lim_bits;      // |w|^2 bound
   int max_per_cell;
-  // fluid (SoA)
-  double *px, *py, *pz, *wx, *wy, *wz;
-  int *rotcell;
+  // fluid (SoA), two buffers: the SRD pass of each step writes the particles into the
+  // other buffer sorted by their SRD cell (a counting sort), so a warp's particles sit
+  // in one or two cells; id[] carries each particle's identity through the sorts
+  double *fl[2][6];    // [buffer][x, y, z, wx, wy, wz]
+  int *pid[2];         // [buffer][position] -> particle id
+  int *newpos;         // particle id -> position in the buffer the last sort wrote
+  int *rotcell;        // position in the current buffer -> cell of the next SRD binning
+  int *cell_off;       // [Cpad] first slot of each cell within its block of 256 cells
+  int *cursor;         // [Cpad] slots taken per cell during the sort
+  int *blk_off;        // [ceil(Cpad/256)] block sums, then their exclusive prefix
   // cells
   CellAcc *acc;        // [Cpad]
   double *cell_ab;     // [C][12]: A (row-major 3x3), b
@@ -90,17 +103,37 @@ struct SysF64 {
   float4 *Xf[2];       // FP32 copies for prefilters
   int *cbox[2];        // 0-based linear cell of each colloid (may alias or exceed C)
   double *V, *W, *ra, *f;   // [Nc][3]
+  double *fnew;             // [Nc][3] force at the positions of the substep in flight
+  double *xi;               // [Nc][3] rotational-diffusion normals of the substep in flight
   ExchAcc *exch;       // [Nc]
   int *shell_cnt;      // [Nc]
-  // fluid-to-colloid table, double-buffered like X
-  int *Tcnt[2];        // [C]
-  uint16_t *Tlist[2];  // [C][TCAP]
+  // fluid-to-colloid table, double-buffered like X: per cell (substep << 32) | count,
+  // entries of another substep read as empty, so the table is never cleared
+  unsigned long long *Tcnt[2];  // [C]
+  uint16_t *Tlist[2];           // [C][TCAP]
   // run() candidates
   ShellRec *shell;
   int shell_cap;
+  // particles near a sphere surface in the substep in flight
+  int *events;
+  int events_cap;
   // step state
   StepState *ss;
   double *pot_part;    // [Nc] per-colloid share of the WCA potential
 };
+
+// view of one fluid buffer
+struct Fluid {
+  double *x, *y, *z, *wx, *wy, *wz;
+  int *id;
+};
+
+__device__ __host__ __forceinline__ Fluid fluid_at(const SysF64 &S, int b) {
+  Fluid f;
+  f.x = S.fl[b][0]; f.y = S.fl[b][1]; f.z = S.fl[b][2];
+  f.wx = S.fl[b][3]; f.wy = S.fl[b][4]; f.wz = S.fl[b][5];
+  f.id = S.pid[b];
+  return f;
+}
 
 }  // namespace bgb

@@ -66,6 +66,7 @@ typedef struct {
   int max_per_cell;        /* occupancy bound of one cell for the exact cell sums (0: 128) */
   double vmax;             /* speed bound of one fluid particle for the exact sums (0: 24*sqrt(kbt/mass_fl)) */
   double init_gap;         /* MPCD_INIT_PHYSICAL: minimum surface gap between colloids    */
+  int sort_every;          /* reorder the fluid by cell every this many steps (0: 10; <0: never) */
 } mpcd_params;
 
 typedef struct {
@@ -78,6 +79,8 @@ typedef struct {
   double momentum[3];      /* fluid + colloid, this step (the reference never resets its sum) */
   double momentum_fluid[3];
   double temperature_fluid;/* 2 KE / (3 N kB) in units of kbt                             */
+  int64_t events;          /* particles found at a colloid wall since the last mpcd_diag   */
+  int64_t shell_records;   /* run() candidate particles recorded for the next step        */
 } mpcd_diag_t;
 
 typedef struct mpcd_ctx mpcd_ctx;

@@ -20,7 +20,7 @@ def _kw(**over):
     return kw
 
 
-def make_pair(L, N, Nc, crafted=None, **over):
+def make_pair(L, N, Nc, crafted=None, sort_every=0, **over):
     import brownian_gb300 as bg
     from oracle import oracle as O
     kw = _kw(**over)
@@ -31,7 +31,7 @@ def make_pair(L, N, Nc, crafted=None, **over):
     if crafted is not None:
         crafted(o)
     st = o.state()
-    sim = bg.Simulation(L, N, Nc, **kw)
+    sim = bg.Simulation(L, N, Nc, sort_every=sort_every, **kw)
     sim.set_state(st["pos_fl"], st["vel_fl"], st["pos_colloid"], st["vel_colloid"], st["ang_vel_colloid"], st["ra"])
     o.setup()
     sim.setup()
@@ -72,9 +72,10 @@ def test_setup_forces_bit_exact():
     assert np.array_equal(g["f"], o.get("f"))
 
 
-@pytest.mark.parametrize("steps", [1, 5])
-def test_steps_match_oracle_small(steps):
-    o, sim = make_pair(10, 10000, 3)
+@pytest.mark.parametrize("steps,sort_every", [(1, 0), (5, 0), (5, 1), (5, -1)])
+def test_steps_match_oracle_small(steps, sort_every):
+    """sort_every: 0 the default period, 1 a counting sort by cell every step, -1 never"""
+    o, sim = make_pair(10, 10000, 3, sort_every=sort_every)
     sim.step(steps)
     o.run_steps(steps)
     assert_close(sim, o)
