@@ -1,6 +1,6 @@
 """Throughput of the MPCD + active-colloid step on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp64]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision fp64|fp32c]
 
 Workload (the 64^3 single system): 64^3 cells, fluid density 10 (2,621,440
 particles, Maxwell-Boltzmann at kT=1, zero net momentum), 500 colloids of radius
@@ -37,8 +37,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L, DENSITY, NC, RADIUS = 64, 10, 500, 2.0
-STREAM_BYTES = 72  # per particle per streaming launch (FP64: read x 24 + w 24, write x 24)
-STEP_BYTES = 808   # per particle per MPCD step, FP64 byte model (10 x 72 + 88)
+# algorithmic bytes per particle: one streaming launch, and one MPCD step (10 substeps + rotation)
+STREAM_BYTES = {"fp64": 72,   # read x 24 + w 24, write x 24
+                "fp32c": 44}  # read cell+offset record 16 + velocity 12, write record 16
+STEP_BYTES = {"fp64": 808, "fp32c": 496}
 
 
 def workload(seed=0):
@@ -117,12 +119,12 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_particle():
+def ncu_traffic_per_particle(precision):
     """DRAM bytes per particle of one streaming launch from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_stream_fp64_traffic.json")
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as f:
-            return float(json.load(f)["dram_bytes_per_particle"])
+            return float(json.load(f)[f"k_stream_{precision}"]["dram_bytes_per_particle"])
     except (OSError, KeyError, ValueError):
         return None
 
@@ -191,66 +193,140 @@ def cpu_baseline(processes, steps, n_fluid):
 
 # ---------------------------------------------------------------- our arm
 
-def run_ours(args, rank, world, dist):
-    import numpy as np
+def _barrier(dist):
+    import torch
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_sim(precision, rank):
     import torch
 
     import brownian_gb300 as bg
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
     w = workload(seed=rank)
-    N = w["n_fluid"]
-    sim = bg.Simulation(w["L"], N, w["n_colloid"], precision=bg.FP64, **w["kw"])
+    sim = bg.Simulation(w["L"], w["n_fluid"], w["n_colloid"],
+                        precision=bg.FP64 if precision == "fp64" else bg.FP32C, **w["kw"])
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
     sim.initialize(bg.INIT_PHYSICAL)
     sim.setup()
+    return sim, stream
 
-    def barrier():
-        torch.cuda.synchronize()
-        if dist is not None:
-            dist.barrier()
 
-    # warm-up (also captures the step graph)
-    sim.step(args.warmup)
-    # ---- timed region A: graph replay, inputs resident in HBM
-    barrier()
+def measure_resident(sim, stream, precision, args, world, dist, with_clocks=True):
+    """Timed region A (graph replay, state resident) and B (per-kernel CUDA events)."""
+    import torch
+    N = sim.N
+    sim.step(args.warmup)  # also captures the step graphs
+    _barrier(dist)
     clocks = Clocks()
-    clocks.start()
+    if with_clocks:
+        clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = sim.launch_count
     e0.record(stream)
     sim.step(args.steps)
     e1.record(stream)
-    barrier()
-    clk = clocks.stop(dev)
-    ms = e0.elapsed_time(e1)
+    _barrier(dist)
+    clk = clocks.stop(int(os.environ.get("LOCAL_RANK", "0"))) if with_clocks else None
+    ms = _max_over_ranks(e0.elapsed_time(e1), dist)
     gpu_launches = sim.launch_count - launches0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     value = world * N * args.steps / (ms / 1e3)
-
-    # ---- timed region B: the same steps, each kernel bracketed by CUDA events
+    # B: the same steps, each kernel bracketed by CUDA events on the library's stream
     sim.profile(True)
-    barrier()
+    _barrier(dist)
     sim.step(args.steps)
-    barrier()
+    _barrier(dist)
     prof = sim.profile_read()
     sim.profile(False)
     st_launches, st_ms = prof.get("k_stream", (0, 0.0))
     t_launch = st_ms / max(st_launches, 1) / 1e3
-    achieved = STREAM_BYTES * N / t_launch / 1e9 if st_launches else None
+    achieved = STREAM_BYTES[precision] * N / t_launch / 1e9 if st_launches else None
     peak, peak_kind = measured_peak_hbm()
-    tpp = ncu_traffic_per_particle()
-    shares = {k: round(v[1] / sum(x[1] for x in prof.values()), 4) for k, v in prof.items()}
+    tpp = ncu_traffic_per_particle(precision)
+    total = sum(x[1] for x in prof.values())
+    shares = {k: {"share": round(v[1] / total, 4), "launches": v[0], "us_per_launch": round(v[1] / v[0] * 1e3, 2)}
+              for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    roof = {"bound": "hbm", "kernel": "k_stream (fluid streaming + wall-collision flagging)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+            "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": STREAM_BYTES[precision] * N,
+            "peak_source": f"{peak_kind} hbm_gbs (burst copy)", "launch_ms": t_launch * 1e3,
+            "launches": st_launches}
+    return dict(value=value, ms=ms, gpu_launches=gpu_launches, clocks=clk, roofline=roof, shares=shares,
+                step_frac=value / world * STEP_BYTES[precision] / (peak * 1e9))
+
+
+def form_statistics(steps, lag):
+    """Both precision forms from the same initial state: momentum drift, fluid
+    temperature and colloid MSD at `lag` steps (unwrapped, averaged over colloids
+    and time origins every 10 steps)."""
+    import numpy as np
+    out = {}
+    for prec in ("fp64", "fp32c"):
+        sim, _ = make_sim(prec, 0)
+        d0 = sim.diag()
+        X = [sim.get_colloids()["pos_colloid"]]
+        temps = []
+        for s in range(steps):
+            sim.step(1)
+            X.append(sim.get_colloids()["pos_colloid"])
+            if (s + 1) % 10 == 0:
+                temps.append(sim.diag()["temperature_fluid"])
+        d1 = sim.diag()
+        sim.close()
+        X = np.array(X)
+        dX = np.diff(X, axis=0)
+        dX -= L * np.round(dX / L)
+        U = np.concatenate([X[:1], X[:1] + np.cumsum(dX, axis=0)])
+        origins = range(0, steps - lag + 1, 10)
+        per_colloid = np.mean([np.sum((U[o + lag] - U[o]) ** 2, axis=1) for o in origins], axis=0)
+        scale = sim.N * np.sqrt(8.0 / np.pi)  # sum |p_i| of a thermal fluid (m = kT = 1)
+        out[prec] = {"msd": float(np.mean(per_colloid)),
+                     "msd_stderr": float(np.std(per_colloid) / np.sqrt(len(per_colloid))),
+                     "temperature": float(np.mean(temps)),
+                     "momentum_drift_rel": float(np.max(np.abs(np.array(d1["momentum"]) - np.array(d0["momentum"])))
+                                                 / scale)}
+    a, b = out["fp64"], out["fp32c"]
+    return {"steps": steps, "msd_lag": lag, "fp64": a, "fp32c": b,
+            "msd_rel_diff": (b["msd"] - a["msd"]) / a["msd"],
+            "msd_rel_stderr_fp64": a["msd_stderr"] / a["msd"],
+            "temperature_diff": b["temperature"] - a["temperature"],
+            "momentum_drift_rel_fp32c": b["momentum_drift_rel"]}
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    forms = [args.precision] + [p for p in ("fp64", "fp32c") if p != args.precision and args.both]
+    res = {}
+    for prec in forms:
+        sim, stream = make_sim(prec, rank)
+        res[prec] = measure_resident(sim, stream, prec, args, world, dist, with_clocks=(prec == args.precision))
+        if prec == args.precision:
+            head_sim = sim
+        else:
+            sim.close()
+    sim = head_sim
+    N = sim.N
+    r = res[args.precision]
 
     # ---- timed region C: end to end through the public API from pinned host buffers
     host = sim.get_state()
     pinned = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in host.items()}
     out = {k: torch.empty(v.shape, dtype=torch.float64).pin_memory().numpy() for k, v in host.items()}
-    barrier()
+    _barrier(dist)
     t0 = time.perf_counter()
     sim.set_state(pinned["pos_fl"], pinned["vel_fl"], pinned["pos_colloid"], pinned["vel_colloid"],
                   pinned["ang_vel_colloid"], pinned["ra"])
@@ -261,12 +337,8 @@ def run_ours(args, rank, world, dist):
     got = sim.get_state()
     for k in out:
         out[k][...] = got[k]
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    _barrier(dist)
+    e2e_s = _max_over_ranks(time.perf_counter() - t0, dist)
     state_bytes = sum(v.nbytes for k, v in host.items() if k != "f")
     diag_bytes = 8 * 14
     e2e = {"value": world * N * args.steps / e2e_s, "unit": "particle-steps/s",
@@ -275,28 +347,33 @@ def run_ours(args, rank, world, dist):
            "timed": "set_state + setup + K x (step + diag) + get_state, host pinned buffers"}
     d = sim.diag()
     sim.close()
+    stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
 
     if rank != 0:
         return None
     line = {
-        "metric": "MPCD fluid particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(config_dict("fp64"), parallelism=f"replicas x{world}"),
-        "hbm_roofline_frac_step": value / world * STEP_BYTES / (peak * 1e9),
-        "roofline": {"bound": "hbm", "kernel": "k_stream (fluid streaming + wall collisions)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None,
-                     "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": STREAM_BYTES * N,
-                     "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "launch_ms": t_launch * 1e3, "launches": st_launches},
-        "kernel_share": shares,
+        "metric": "MPCD fluid particle-steps/s", "value": r["value"], "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "config": dict(config_dict(args.precision), parallelism=f"replicas x{world}"),
+        "hbm_roofline_frac_step": r["step_frac"],
+        "roofline": r["roofline"],
+        "kernel_share": r["shares"],
         "e2e": e2e,
-        "gpu_launches": gpu_launches,
-        "clocks": clk,
+        "gpu_launches": r["gpu_launches"],
+        "clocks": r["clocks"],
         "diag_end": {"temperature_fluid": d["temperature_fluid"], "momentum": d["momentum"],
                      "wall_events_per_substep": dd["events"] / 10.0, "run_candidates": dd["shell_records"]},
     }
+    for prec in forms[1:]:
+        o = res[prec]
+        line[f"form_{prec}"] = {"value": o["value"], "unit": "particle-steps/s", "ms_per_step": o["ms"] / args.steps,
+                                "speedup_vs_" + args.precision: o["value"] / r["value"],
+                                "hbm_roofline_frac_step": o["step_frac"], "roofline": o["roofline"],
+                                "kernel_share": o["shares"], "gpu_launches": o["gpu_launches"]}
+    if stats:
+        line["fp32c_vs_fp64"] = stats
     return line
 
 
@@ -306,7 +383,10 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"], help="form of the headline line")
+    ap.add_argument("--both", type=int, default=1, help="also time the other precision form (sub-object)")
+    ap.add_argument("--stat-steps", type=int, default=200,
+                    help="steps of the FP32c-vs-FP64 statistics run (MSD at lag 100; <=100: skip)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
     args = ap.parse_args()

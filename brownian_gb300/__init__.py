@@ -24,7 +24,8 @@ INIT_REFERENCE, INIT_PHYSICAL = 0, 1
 EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", "mpcd_set_state", "mpcd_get_state",
            "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
            "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
-           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count"]
+           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch"]
+LAUNCH_EVENTS, LAUNCH_FIN = 0, 1
 
 
 class MPCDError(RuntimeError):
@@ -90,6 +91,7 @@ def lib():
         L.mpcd_profile_read.argtypes = [vp, C.c_void_p, C.POINTER(C.c_int64), dp, C.c_int]
         L.mpcd_launch_count.argtypes = [vp]
         L.mpcd_launch_count.restype = C.c_int64
+        L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -173,6 +175,13 @@ class Simulation:
                                                                       "vel_colloid", "ang_vel_colloid", "ra", "f")]))
         return out
 
+    def get_colloids(self):
+        """The colloid arrays only (no fluid transfer)."""
+        out = {k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra", "f")}
+        self._ck(lib().mpcd_get_state(self.h, None, None, *[_dp(out[k]) for k in ("pos_colloid", "vel_colloid",
+                                                                                 "ang_vel_colloid", "ra", "f")]))
+        return out
+
     @property
     def step_count(self):
         return lib().mpcd_get_step(self.h)
@@ -230,6 +239,11 @@ class Simulation:
         ms = (C.c_double * cap)()
         n = lib().mpcd_profile_read(self.h, names, launches, ms, cap)
         return {bytes(names[i]).split(b"\0", 1)[0].decode(): (launches[i], ms[i]) for i in range(min(n, cap))}
+
+    def set_launch(self, which, grid=0, block=32):
+        """Launch shape of the event (LAUNCH_EVENTS) or colloid-finish (LAUNCH_FIN)
+        kernel; grid 0 is the default, one block per SM."""
+        self._ck(lib().mpcd_set_launch(self.h, which, grid, block))
 
     @property
     def launch_count(self):

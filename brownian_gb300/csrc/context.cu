@@ -67,9 +67,13 @@ struct mpcd_ctx {
   double *part = nullptr;        // reduction partials
   int part_blocks = 256;
   double *staging = nullptr;     // AoS transfer buffer, allocated on first use
+  double *staging2 = nullptr;    // second one (FP32 form: velocities)
   int phase = 0;                 // 0: between steps; 1: rotation_mpcd of the next step done
   int next_sub = 1;              // routine-level: the substep mpcd_substep expects
   int nblk = 0;                  // 256-cell blocks of the counting sort
+  int n_sm = 152;                // multiprocessors of the device
+  int ev_grid = 0, ev_block = 32;    // k_events launch shape (grid 0: one block per SM)
+  int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
 };
 
 static int fail(mpcd_ctx *c, int code, const std::string &m) {
@@ -130,6 +134,13 @@ static void launch(mpcd_ctx *c, const char *name, void (*k)(KArgs...), dim3 g, d
   }
 }
 
+// a copy ordered on the context's stream (which does not synchronise with the
+// legacy default stream), complete on return
+static cudaError_t scopy(const mpcd_ctx *c, void *dst, const void *src, size_t n, cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n, kind, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 static int colloid_grid(const mpcd_ctx *c) {
@@ -143,17 +154,29 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
                      : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
                      : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
   // the streaming passes of substeps carry the colloid forces and the next cell
-  // table in their first blocks (8 colloid warps per block)
-  int naux = (flags & F_STREAM) ? (int)blocks_for(c->S.Nc, 8) : 0;
-  launch(c, name, stream_kernel(flags), naux + blocks_for(c->S.N, 256), 256, c->S, l, naux, act, fb);
+  // table in their first blocks (one colloid per block)
+  int naux = (flags & F_STREAM) ? c->S.Nc : 0;
+  const bool f32 = c->S.precision == MPCD_FP32C;
+  launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags), naux + blocks_for(c->S.N, 256), 256, c->S, l,
+         naux, act, fb);
   // the particles it left near a sphere surface, one per lane
-  launch(c, "k_events", event_kernel(flags), 1024, 128, c->S, l, fb);
+  launch(c, "k_events", f32 ? event_kernel32(flags) : event_kernel(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm,
+         c->ev_block, c->S, l, fb);
 }
 
 static void enq_fin(mpcd_ctx *c, int mode, int l) {
-  // one thread per colloid, one warp per block so the FP64 work spreads over SMs
-  unsigned g = blocks_for(c->S.Nc, 32);
-  launch(c, "k_fin", k_fin, g > 0 ? g : 1, 32, c->S, mode, l);
+  // one warp per colloid (warp j / grid of block j % grid): each SM's FP64 unit
+  // serves the chains of a few colloids only
+  int g = c->fin_grid > 0 ? c->fin_grid : c->n_sm;
+  const int nc = c->S.Nc > 0 ? c->S.Nc : 1;
+  if (g > nc) g = nc;
+  int w = c->fin_block / 32;
+  if ((long long)g * w < nc) w = (int)blocks_for(nc, g);
+  if (w > 4) {
+    w = 4;
+    g = (int)blocks_for(nc, 4);
+  }
+  launch(c, "k_fin", k_fin, g, 32 * w, c->S, mode, l);
 }
 
 static unsigned prep_blocks(const SysF64 &S) { return blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256); }
@@ -164,21 +187,24 @@ static bool sorts_at(const mpcd_ctx *c, long long step) { return c->sort_every >
 // sort_every steps fused with the counting-sort scatter into the other buffer
 static void enq_rotation(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
-  launch(c, "k_cell_prep", k_cell_prep, prep_blocks(S), 256, S);
+  const bool f32 = S.precision == MPCD_FP32C;
+  launch(c, "k_cell_prep", f32 ? k_cell_prep32 : k_cell_prep, prep_blocks(S), 256, S);
   if (sort) {
     launch(c, "k_scan_blocks", k_scan_blocks, 1, 1024, S, c->nblk);
-    launch(c, "k_rotate_sort", k_rotate_sort, blocks_for(S.N, 256), 256, S, c->fbuf, 1 - c->fbuf);
+    launch(c, "k_rotate_sort", f32 ? k_rotate_sort32 : k_rotate_sort, blocks_for(S.N, 256), 256, S, c->fbuf,
+           1 - c->fbuf);
     c->fbuf = 1 - c->fbuf;
   } else {
-    launch(c, "k_rotate", k_rotate, blocks_for(S.N, 256), 256, S, c->fbuf);
+    launch(c, "k_rotate", f32 ? k_rotate32 : k_rotate, blocks_for(S.N, 256), 256, S, c->fbuf);
   }
 }
 
 static void enq_run_fluid(mpcd_ctx *c) {
   const SysF64 &S = c->S;
   if (S.Nc == 0) return;
-  launch(c, "k_run_shell", k_run_shell, 152 * 4, 256, S, c->fbuf);
-  launch(c, "k_run_kick", k_run_kick, 152 * 4, 256, S, c->fbuf);
+  const bool f32 = S.precision == MPCD_FP32C;
+  launch(c, "k_run_shell", f32 ? k_run_shell32 : k_run_shell, 152 * 4, 256, S, c->fbuf);
+  launch(c, "k_run_kick", f32 ? k_run_kick32 : k_run_kick, 152 * 4, 256, S, c->fbuf);
 }
 
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
@@ -259,7 +285,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   if (!(p.ndt > 0) || !(p.kbt > 0) || !(p.mass_fl > 0)) return MPCD_ERR_PARAM;
   if (p.n_colloid > 0 && (!(p.mass_colloid > 0) || !(p.I_colloid > 0) || !(p.sigma > 0) || !(p.sig_colloid > 0)))
     return MPCD_ERR_PARAM;
-  if (p.precision != MPCD_FP64) return MPCD_ERR_PARAM;
+  if (p.precision != MPCD_FP64 && p.precision != MPCD_FP32C) return MPCD_ERR_PARAM;
+  if (p.precision == MPCD_FP32C && (p.Lx > 1023 || p.Ly > 1023 || p.Lz > 1023)) return MPCD_ERR_PARAM;
   long long C = (long long)p.Lx * p.Ly * p.Lz;
   if (C > (1ll << 30)) return MPCD_ERR_PARAM;
 
@@ -316,7 +343,11 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   const double vmax = p.vmax > 0 ? p.vmax : 24.0 * sqrt(p.kbt / p.mass_fl);
-  const double wmax = vmax * dt;
+  S.precision = p.precision;
+  S.dtf = (float)dt;
+  S.vmaxf = (float)vmax;
+  // the FP64 form sums displacements w = v dt, the FP32 form velocities
+  const double wmax = p.precision == MPCD_FP64 ? vmax * dt : vmax;
   // one scale for the sums of w and |w|^2: max_per_cell * max(wmax, 3 wmax^2) * 2^kw < 2^62
   const double wbound = wmax > 3.0 * wmax * wmax ? wmax : 3.0 * wmax * wmax;
   S.kw = 62 - (int)ceil(log2((double)S.max_per_cell * wbound));
@@ -327,7 +358,12 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   DevAlloc &m = c->mem;
   const size_t N = S.N, Nc = S.Nc > 0 ? S.Nc : 1;
   for (int b = 0; b < 2; ++b) {
-    for (int k = 0; k < 6; ++k) S.fl[b][k] = m.get<double>(N);
+    if (p.precision == MPCD_FP64) {
+      for (int k = 0; k < 6; ++k) S.fl[b][k] = m.get<double>(N);
+    } else {
+      S.q[b] = m.get<uint4>(N);
+      for (int k = 0; k < 3; ++k) S.v32[b][k] = m.get<float>(N);
+    }
     S.pid[b] = m.get<int>(N);
   }
   S.newpos = m.get<int>(N);
@@ -337,10 +373,13 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.cursor = m.get<int>(S.Cpad);
   S.blk_off = m.get<int>(prep_blocks(S) + 1);
   S.acc = m.get<CellAcc>(S.Cpad);
-  S.cell_ab = m.get<double>((size_t)S.C * 12);
+  if (p.precision == MPCD_FP64) S.cell_ab = m.get<double>((size_t)S.C * 12);
+  else S.cell_ab32 = m.get<float>((size_t)S.C * 12);
   for (int b = 0; b < 2; ++b) {
     S.X[b] = m.get<double>(3 * Nc);
     S.Xf[b] = m.get<float4>(Nc);
+    S.Xcq[b] = m.get<float4>(Nc);
+    S.Xco[b] = m.get<float4>(Nc);
     S.cbox[b] = m.get<int>(Nc);
     S.Tcnt[b] = m.get<unsigned long long>(S.C);
     S.Tlist[b] = m.get<uint16_t>((size_t)S.C * TCAP);
@@ -370,7 +409,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   }
   std::vector<double> inv(S.max_per_cell + 1, 0.0);
   for (int n = 1; n <= S.max_per_cell; ++n) inv[n] = 1.0 / n;
-  cudaMemcpy(c->inv_n, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
+  scopy(c, c->inv_n, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
   if (cudaMallocHost(&c->ss_host, sizeof(StepState)) != cudaSuccess) {
     m.release();
     delete c;
@@ -383,6 +422,12 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     return MPCD_ERR_CUDA;
   }
   c->own_stream = true;
+  {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0)
+      c->n_sm = nsm;
+  }
   cudaDeviceSynchronize();
   *out = c;
   return MPCD_OK;
@@ -396,6 +441,7 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   for (auto e : c->event_pool) cudaEventDestroy(e);
   c->mem.release();
   if (c->staging) cudaFree(c->staging);
+  if (c->staging2) cudaFree(c->staging2);
   if (c->ss_host) cudaFreeHost(c->ss_host);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -449,9 +495,13 @@ static int upload_colloid_pos(mpcd_ctx *c, const double *xyz) {
   return MPCD_OK;
 }
 
-static int ensure_staging(mpcd_ctx *c) {
+static int ensure_staging(mpcd_ctx *c, bool two = false) {
   if (!c->staging) {
     cudaError_t e = cudaMalloc(&c->staging, sizeof(double) * 3 * (size_t)c->S.N);
+    if (e != cudaSuccess) return fail(c, MPCD_ERR_NOMEM, "staging buffer");
+  }
+  if (two && !c->staging2) {
+    cudaError_t e = cudaMalloc(&c->staging2, sizeof(double) * 3 * (size_t)c->S.N);
     if (e != cudaSuccess) return fail(c, MPCD_ERR_NOMEM, "staging buffer");
   }
   return MPCD_OK;
@@ -504,7 +554,14 @@ extern "C" int mpcd_set_state(mpcd_ctx *c, const double *pos_fl, const double *v
   if ((pos_fl == nullptr) != (vel_fl == nullptr))
     return fail(c, MPCD_ERR_PARAM, "pos_fl and vel_fl are set together (the device keeps particles in cell order)");
   c->phase = 0;
-  if (pos_fl) {
+  if (pos_fl && S.precision == MPCD_FP32C) {
+    if ((r = ensure_staging(c, true))) return r;
+    const size_t nb = sizeof(double) * 3 * (size_t)S.N;
+    CUDA_OK(c, cudaMemcpyAsync(c->staging, pos_fl, nb, cudaMemcpyHostToDevice, c->stream));
+    CUDA_OK(c, cudaMemcpyAsync(c->staging2, vel_fl, nb, cudaMemcpyHostToDevice, c->stream));
+    launch(c, "k_aos_to_q", k_aos_to_q, blocks_for(S.N, 256), 256, S, (const double *)c->staging,
+           (const double *)c->staging2, c->fbuf);
+  } else if (pos_fl) {
     Fluid F = cur_fluid(c);
     if ((r = upload_soa(c, pos_fl, F.x, F.y, F.z, F.id, S.newpos, 0.0))) return r;
     if ((r = upload_soa(c, vel_fl, F.wx, F.wy, F.wz, nullptr, nullptr, S.dt))) return r;  // w = fl(v*dt)
@@ -512,9 +569,9 @@ extern "C" int mpcd_set_state(mpcd_ctx *c, const double *pos_fl, const double *v
   CUDA_OK(c, cudaStreamSynchronize(c->stream));
   if (S.Nc) {
     if (pos_colloid && (r = upload_colloid_pos(c, pos_colloid))) return r;
-    if (vel_colloid) CUDA_OK(c, cudaMemcpy(S.V, vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
-    if (ang_vel_colloid) CUDA_OK(c, cudaMemcpy(S.W, ang_vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
-    if (ra) CUDA_OK(c, cudaMemcpy(S.ra, ra, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+    if (vel_colloid) CUDA_OK(c, scopy(c, S.V, vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+    if (ang_vel_colloid) CUDA_OK(c, scopy(c, S.W, ang_vel_colloid, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
+    if (ra) CUDA_OK(c, scopy(c, S.ra, ra, sizeof(double) * 3 * S.Nc, cudaMemcpyHostToDevice));
   }
   return invalidate_tables(c);
 }
@@ -525,16 +582,25 @@ extern "C" int mpcd_get_state(mpcd_ctx *c, double *pos_fl, double *vel_fl, doubl
   int r;
   if ((r = read_ss(c))) return r;
   const SysF64 &S = c->S;
-  Fluid F = cur_fluid(c);
-  if (pos_fl && (r = download_soa(c, pos_fl, F.x, F.y, F.z, F.id, 0.0))) return r;
-  if (vel_fl && (r = download_soa(c, vel_fl, F.wx, F.wy, F.wz, F.id, S.dt))) return r;  // v = w/dt
+  if (S.precision == MPCD_FP32C && (pos_fl || vel_fl)) {
+    if ((r = ensure_staging(c, true))) return r;
+    const size_t nb = sizeof(double) * 3 * (size_t)S.N;
+    launch(c, "k_q_to_aos", k_q_to_aos, blocks_for(S.N, 256), 256, S, c->staging, c->staging2, c->fbuf);
+    if (pos_fl) CUDA_OK(c, cudaMemcpyAsync(pos_fl, c->staging, nb, cudaMemcpyDeviceToHost, c->stream));
+    if (vel_fl) CUDA_OK(c, cudaMemcpyAsync(vel_fl, c->staging2, nb, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  } else {
+    Fluid F = cur_fluid(c);
+    if (pos_fl && (r = download_soa(c, pos_fl, F.x, F.y, F.z, F.id, 0.0))) return r;
+    if (vel_fl && (r = download_soa(c, vel_fl, F.wx, F.wy, F.wz, F.id, S.dt))) return r;  // v = w/dt
+  }
   if (S.Nc) {
     int b = cur_buf(c);
-    if (pos_colloid) CUDA_OK(c, cudaMemcpy(pos_colloid, S.X[b], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
-    if (vel_colloid) CUDA_OK(c, cudaMemcpy(vel_colloid, S.V, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
-    if (ang_vel_colloid) CUDA_OK(c, cudaMemcpy(ang_vel_colloid, S.W, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
-    if (ra) CUDA_OK(c, cudaMemcpy(ra, S.ra, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
-    if (f) CUDA_OK(c, cudaMemcpy(f, S.f, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (pos_colloid) CUDA_OK(c, scopy(c, pos_colloid, S.X[b], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (vel_colloid) CUDA_OK(c, scopy(c, vel_colloid, S.V, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (ang_vel_colloid) CUDA_OK(c, scopy(c, ang_vel_colloid, S.W, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (ra) CUDA_OK(c, scopy(c, ra, S.ra, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
+    if (f) CUDA_OK(c, scopy(c, f, S.f, sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToHost));
   }
   return MPCD_OK;
 }
@@ -549,21 +615,37 @@ extern "C" int mpcd_set_step(mpcd_ctx *c, int64_t step) {
     int to = (int)((step * c->S.n_sub - 1) & 1);
     if (from != to) {
       const SysF64 &S = c->S;
-      CUDA_OK(c, cudaMemcpy(S.X[to], S.X[from], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToDevice));
-      CUDA_OK(c, cudaMemcpy(S.Xf[to], S.Xf[from], sizeof(float4) * S.Nc, cudaMemcpyDeviceToDevice));
-      CUDA_OK(c, cudaMemcpy(S.cbox[to], S.cbox[from], sizeof(int) * S.Nc, cudaMemcpyDeviceToDevice));
+      CUDA_OK(c, scopy(c, S.X[to], S.X[from], sizeof(double) * 3 * S.Nc, cudaMemcpyDeviceToDevice));
+      CUDA_OK(c, scopy(c, S.Xf[to], S.Xf[from], sizeof(float4) * S.Nc, cudaMemcpyDeviceToDevice));
+      CUDA_OK(c, scopy(c, S.cbox[to], S.cbox[from], sizeof(int) * S.Nc, cudaMemcpyDeviceToDevice));
     }
   }
   c->ss_host->step = step;
-  CUDA_OK(c, cudaMemcpy(&c->S.ss->step, &step, sizeof(long long), cudaMemcpyHostToDevice));
+  CUDA_OK(c, scopy(c, &c->S.ss->step, &step, sizeof(long long), cudaMemcpyHostToDevice));
   return invalidate_tables(c);
+}
+
+extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
+  if (!c) return MPCD_ERR_PARAM;
+  if (grid > 65535 || (grid > 0 && (block < 32 || block > 128 || block % 32)))
+    return fail(c, MPCD_ERR_PARAM, "launch shape: block a multiple of 32 in [32, 128], grid <= 65535");
+  if (which == MPCD_LAUNCH_EVENTS) {
+    c->ev_grid = grid > 0 ? grid : 0;
+    c->ev_block = grid > 0 ? block : 32;
+  } else if (which == MPCD_LAUNCH_FIN) {
+    c->fin_grid = grid > 0 ? grid : 0;
+    c->fin_block = grid > 0 ? block : 32;
+  } else {
+    return fail(c, MPCD_ERR_PARAM, "unknown launch");
+  }
+  return drop_graph(c);
 }
 
 extern "C" int64_t mpcd_get_step(const mpcd_ctx *c) {
   if (!c) return -1;
   long long s = 0;
   cudaStreamSynchronize(c->stream);
-  cudaMemcpy(&s, &c->S.ss->step, sizeof s, cudaMemcpyDeviceToHost);
+  scopy(c, &s, &c->S.ss->step, sizeof s, cudaMemcpyDeviceToHost);
   return s;
 }
 
@@ -686,7 +768,7 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   if (S.Nc) launch(c, "k_colloid_pot", k_colloid_pot, colloid_grid(c), 128, S);
   if ((r = check_device(c))) return r;
   std::vector<double> part((size_t)c->part_blocks * 5);
-  CUDA_OK(c, cudaMemcpy(part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
+  CUDA_OK(c, scopy(c, part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
   double sw[3] = {0, 0, 0}, s2 = 0, n = 0;
   for (int b = 0; b < c->part_blocks; ++b) {
     for (int k = 0; k < 3; ++k) sw[k] += part[5 * b + k];
@@ -696,20 +778,21 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   memset(out, 0, sizeof *out);
   out->step = c->ss_host->step;
   const double m = c->p.mass_fl;
-  for (int k = 0; k < 3; ++k) out->momentum_fluid[k] = m * sw[k] / S.dt;
-  out->ke_fluid = 0.5 * m * s2 / (S.dt * S.dt);
+  const double per = S.precision == MPCD_FP64 ? S.dt : 1.0;  // the FP64 form sums w = v dt
+  for (int k = 0; k < 3; ++k) out->momentum_fluid[k] = m * sw[k] / per;
+  out->ke_fluid = 0.5 * m * s2 / (per * per);
   out->temperature_fluid = n > 0 ? 2.0 * out->ke_fluid / (3.0 * n) / c->p.kbt : 0;
   // wall-collision candidates handled exactly, summed since the last call
   out->events = c->ss_host->ev_total;
   const long long zero64 = 0;
-  CUDA_OK(c, cudaMemcpy(&c->S.ss->ev_total, &zero64, sizeof zero64, cudaMemcpyHostToDevice));
+  CUDA_OK(c, scopy(c, &c->S.ss->ev_total, &zero64, sizeof zero64, cudaMemcpyHostToDevice));
   out->shell_records = c->ss_host->nshell;
   double mom[3] = {out->momentum_fluid[0], out->momentum_fluid[1], out->momentum_fluid[2]};
   if (S.Nc) {
     std::vector<double> V(3 * S.Nc), W(3 * S.Nc), pot(S.Nc);
-    CUDA_OK(c, cudaMemcpy(V.data(), S.V, sizeof(double) * V.size(), cudaMemcpyDeviceToHost));
-    CUDA_OK(c, cudaMemcpy(W.data(), S.W, sizeof(double) * W.size(), cudaMemcpyDeviceToHost));
-    CUDA_OK(c, cudaMemcpy(pot.data(), S.pot_part, sizeof(double) * pot.size(), cudaMemcpyDeviceToHost));
+    CUDA_OK(c, scopy(c, V.data(), S.V, sizeof(double) * V.size(), cudaMemcpyDeviceToHost));
+    CUDA_OK(c, scopy(c, W.data(), S.W, sizeof(double) * W.size(), cudaMemcpyDeviceToHost));
+    CUDA_OK(c, scopy(c, pot.data(), S.pot_part, sizeof(double) * pot.size(), cudaMemcpyDeviceToHost));
     double ke = 0, ake = 0, pe = 0;
     for (int j = 0; j < S.Nc; ++j) {
       ke += V[3 * j] * V[3 * j] + V[3 * j + 1] * V[3 * j + 1] + V[3 * j + 2] * V[3 * j + 2];
@@ -735,8 +818,8 @@ extern "C" int mpcd_get_rotation_binning(mpcd_ctx *c, int32_t *cell_of, int32_t 
   if ((r = read_ss(c))) return r;
   if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "the binning is that of the next step; call between steps");
   std::vector<int> rc(S.N), id(S.N);
-  CUDA_OK(c, cudaMemcpy(rc.data(), S.rotcell, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
-  CUDA_OK(c, cudaMemcpy(id.data(), cur_fluid(c).id, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
+  CUDA_OK(c, scopy(c, rc.data(), S.rotcell, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
+  CUDA_OK(c, scopy(c, id.data(), cur_fluid(c).id, sizeof(int) * S.N, cudaMemcpyDeviceToHost));
   if (cell_of)
     for (int i = 0; i < S.N; ++i) cell_of[id[i]] = rc[i] + 1;
   if (occupancy) {
@@ -751,7 +834,7 @@ extern "C" int mpcd_get_rotation_binning(mpcd_ctx *c, int32_t *cell_of, int32_t 
 
 extern "C" int mpcd_get_shell_count(mpcd_ctx *c, int32_t *cnt) {
   if (!c || !cnt) return MPCD_ERR_PARAM;
-  if (c->S.Nc) CUDA_OK(c, cudaMemcpy(cnt, c->S.shell_cnt, sizeof(int) * c->S.Nc, cudaMemcpyDeviceToHost));
+  if (c->S.Nc) CUDA_OK(c, scopy(c, cnt, c->S.shell_cnt, sizeof(int) * c->S.Nc, cudaMemcpyDeviceToHost));
   return MPCD_OK;
 }
 

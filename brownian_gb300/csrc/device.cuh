@@ -1,0 +1,440 @@
+// Device code shared by the FP64 and FP32-compensated forms: the reference's
+// cell and block rules, the epoch-tagged fluid-to-colloid tables, the exact
+// exchange sums, the stochastic reflection, and the per-colloid work (WCA forces,
+// orientation update, table build) that both forms run in FP64.
+#pragma once
+#include "kernels.cuh"
+
+namespace bgb {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// ----------------------------------------------------------------- cell helpers
+
+static __device__ __forceinline__ int lin_cell(const SysF64 &S, int ix, int iy, int iz) { return ix + S.Lx * (iy + S.Ly * iz); }
+
+static __device__ __forceinline__ bool off_ok(int d, int L) {
+  int m = d % L;
+  if (m < 0) m += L;
+  return m <= 3 || m >= L - 3;
+}
+
+// Is cell `lin` one of the 342 neighbour boxes of cell `cb` (create_box,
+// cpp/neighbour_list.cpp:12-25: periodic offsets -3..3 per axis, own box
+// excluded)?  Cell numbers >= C (a coordinate exactly at L past the last row)
+// have no neighbour entries in the reference.
+static __device__ __forceinline__ bool in_block(const SysF64 &S, int cb, int lin) {
+  if (cb >= S.C || lin >= S.C || cb == lin) return false;
+  int cx = cb % S.Lx, ct = cb / S.Lx, cy = ct % S.Ly, cz = ct / S.Ly;
+  int bx = lin % S.Lx, bt = lin / S.Lx, by = bt % S.Ly, bz = bt / S.Ly;
+  return off_ok(bx - cx, S.Lx) && off_ok(by - cy, S.Ly) && off_ok(bz - cz, S.Lz);
+}
+
+// 1 + cell(pos) - 1: the reference's truncating linear cell of a wrapped position.
+// A wrapped coordinate lies in [0, L], so each integer part is at most L and the
+// cell number stays below Cpad; anything else (NaN, a negative or runaway
+// position) is clamped, flagged, and never used to index past the tables.
+static __device__ __forceinline__ int cell_of_pos(const SysF64 &S, double x, double y, double z, bool &alias) {
+  int ix = trunc_nonneg(x), iy = trunc_nonneg(y), iz = trunc_nonneg(z);
+  bool bad = (ix > S.Lx) | (iy > S.Ly) | (iz > S.Lz) | (dbits(x) < 0) | (dbits(y) < 0) | (dbits(z) < 0);
+  if (bad) {
+    atomicOr(&S.ss->err, ERRB_VRANGE);
+    ix = min(ix, S.Lx); iy = min(iy, S.Ly); iz = min(iz, S.Lz);
+  }
+  alias = (ix >= S.Lx) | (iy >= S.Ly) | (iz >= S.Lz);
+  return lin_cell(S, ix, iy, iz);
+}
+
+// count of the cell-table entry if it belongs to substep g
+static __device__ __forceinline__ int tcount(unsigned long long v, long long g) {
+  return (unsigned)(v >> 32) == (unsigned)g ? (int)(unsigned)v : 0;
+}
+
+// append colloid j to cell `cell` of the table of substep e
+static __device__ __forceinline__ void tappend(unsigned long long *Tc, uint16_t *Tl, int cell, long long e, int j, int *err) {
+  const unsigned long long tag = (unsigned long long)(unsigned)e << 32;
+  unsigned long long old = Tc[cell];
+  for (int it = 0; it < 256; ++it) {
+    unsigned long long nv = ((unsigned)(old >> 32) == (unsigned)e) ? old + 1 : (tag | 1ull);
+    unsigned long long prev = atomicCAS(&Tc[cell], old, nv);
+    if (prev == old) {
+      int slot = (int)(unsigned)nv - 1;
+      if (slot < TCAP) Tl[(size_t)cell * TCAP + slot] = (uint16_t)j;
+      else atomicOr(err, ERRB_TTABLE);
+      return;
+    }
+    old = prev;
+  }
+  atomicOr(err, ERRB_TTABLE);
+}
+
+// FP32 copy of a double by truncating the mantissa (integer pipe); relative
+// error below 2^-23
+static __device__ __forceinline__ float d2f_trunc(double x) {
+  long long b = dbits(x);
+  int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return 0.f;
+  int fe = e - 1023 + 127;
+  if (fe <= 0) return 0.f;
+  if (fe >= 255) return __int_as_float(0x7f800000);
+  unsigned m = (unsigned)((b >> 29) & 0x7FFFFF);
+  return __uint_as_float(((unsigned)((unsigned long long)b >> 32) & 0x80000000u) | ((unsigned)fe << 23) | m);
+}
+
+static __device__ __forceinline__ float wrap_half(float d, float L) {
+  if (d > 0.5f * L) d -= L;
+  else if (d < -0.5f * L) d += L;
+  return d;
+}
+
+// ----------------------------------------------------------- exact exchange sums
+
+static __device__ __forceinline__ void exch_add(ExchAcc *e, int comp, double v, int *err) {
+  if ((dbits(v) & 0x7FFFFFFFFFFFFFFFll) >= 0x4130000000000000ll) atomicOr(err, ERRB_DELTA);  // |v| >= 2^20
+  long long hi = to_fix(v, 20);
+  double res = __dsub_rn(v, (double)hi * 0x1p-20);
+  long long lo = to_fix(res, 72);
+  atomicAdd((unsigned long long *)&e->hi[comp], (unsigned long long)hi);
+  atomicAdd((unsigned long long *)&e->lo[comp], (unsigned long long)lo);
+}
+
+static __device__ __forceinline__ double exch_val(const ExchAcc &e, int comp) {
+  return __dadd_rn((double)e.hi[comp] * 0x1p-20, (double)e.lo[comp] * 0x1p-72);
+}
+
+// ------------------------------------------------------- stochastic reflection
+
+struct CollDraw {
+  uint2 key;
+  uint32_t a, b, t;
+  int idx;
+  uint4 buf;
+};
+
+static __device__ __forceinline__ double cd_next(CollDraw &d) {
+  int s = d.idx & 3;
+  if (s == 0) d.buf = draw4(d.key, DOM_COLL, (uint32_t)(d.idx >> 2), d.a, d.b, d.t);
+  d.idx++;
+  uint32_t w = s == 0 ? d.buf.x : s == 1 ? d.buf.y : s == 2 ? d.buf.z : d.buf.w;
+  return u01(w);
+}
+
+// stochastic_reflection (cpp/fluid_colloid_collision.cpp:7-24): Rayleigh normal
+// speed along rs plus one Gaussian tangential component along unit(un x t)
+static __device__ d3 stochastic_reflection(const SysF64 &S, CollDraw &d, d3 rf, d3 rs) {
+  double u = cd_next(d);
+  double om = __dsub_rn(1.0, u);
+  double random_e = __dmul_rn(om, om);
+  // vector / |vector| as one reciprocal and three products (within an ulp of the
+  // reference's three divisions); likewise /m_beta as * kT/m
+  d3 n = mul3s(rs, __drcp_rn(__dsqrt_rn(norm2_ref(rs.x, rs.y, rs.z))));
+  double val = __dsqrt_rn(__dmul_rn(-log(random_e), S.inv_m_beta));
+  d3 un = mul3s(n, val);
+  double t0 = cd_next(d), t1 = cd_next(d), t2 = cd_next(d);
+  d3 t = mk(ref_img(__dsub_rn(__dmul_rn(t0, S.dx.L), rf.x), S.dx), ref_img(__dsub_rn(__dmul_rn(t1, S.dy.L), rf.y), S.dy),
+            ref_img(__dsub_rn(__dmul_rn(t2, S.dz.L), rf.z), S.dz));
+  d3 ut = cross_ref(un, t);
+  ut = mul3s(ut, __drcp_rn(__dsqrt_rn(norm2_ref(ut.x, ut.y, ut.z))));
+  double x1 = 0, x2 = 0, z = 2.0;
+  // polar Box-Muller rejection; each try is a fixed function of the key, and a
+  // try is rejected with probability 1 - pi/4, so 256 tries never run out
+  for (int it = 0; z > 1.0 && it < 256; ++it) {
+    x1 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
+    x2 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
+    z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+  }
+  z = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(z)), z));
+  double v1 = __dmul_rn(__dmul_rn(x1, z), S.sqrt_kt_m);
+  return add3(mul3s(ut, v1), un);
+}
+
+// ------------------------------------------------------------ particle stream
+
+// Colloids the cell table lists for cell `lin`, visited in ascending index
+// (the reference visits colloids in order, fluid_colloid_collision.cpp:30).
+struct CandIter {
+  const uint16_t *lst;
+  int cnt, last;
+  bool brute;  // aliased cell: scan all colloids with the exact block rule
+  int lin;
+};
+
+static __device__ __forceinline__ int cand_next(const SysF64 &S, CandIter &it, const int *cbox) {
+  if (it.brute) {
+    for (int j = it.last + 1; j < S.Nc; ++j)
+      if (in_block(S, cbox[j], it.lin)) { it.last = j; return j; }
+    return -1;
+  }
+  int best = 0x7FFFFFFF;
+  for (int k = 0; k < it.cnt; ++k) {
+    int j = it.lst[k];
+    if (j > it.last && j < best) best = j;
+  }
+  if (best == 0x7FFFFFFF) return -1;
+  it.last = best;
+  return best;
+}
+
+// Is the particle within radius r (r2 = the reference's squared threshold) of
+// colloid j?  FP32 on copies first; the exact FP64 test of the reference only
+// within 1e-3 of the sphere, where FP32 could decide differently (the FP32
+// copies are within 2^-22 L of the doubles).
+static __device__ __forceinline__ bool within(const SysF64 &S, const double *Xc, float4 c, int j, double x, double y, double z,
+                                       float r, double r2) {
+  const float px = d2f_trunc(x), py = d2f_trunc(y), pz = d2f_trunc(z);
+  float dx = wrap_half(c.x - px, S.Lxf), dy = wrap_half(c.y - py, S.Lyf), dz = wrap_half(c.z - pz, S.Lzf);
+  float d2 = dx * dx + dy * dy + dz * dz;
+  float hi = r + 1e-3f, lo = r - 1e-3f;
+  if (d2 > hi * hi) return false;
+  if (d2 < lo * lo) return true;
+  double rx = ref_img(__dsub_rn(Xc[3 * j], x), S.dx), ry = ref_img(__dsub_rn(Xc[3 * j + 1], y), S.dy),
+         rz = ref_img(__dsub_rn(Xc[3 * j + 2], z), S.dz);
+  return norm2_ref(rx, ry, rz) <= r2;
+}
+
+// Everything a particle does near colloids: wall collisions in colloid order
+// (fluid_colloid_collision.cpp:30-45) and, on the last substep, the run()
+// candidate record.  Kept out of line so the common streaming path stays lean.
+static __device__ __noinline__ void near_colloids(const SysF64 &S, int flags, int pid, int lin, bool alias, long long gs,
+                                           int buf, double &x, double &y, double &z, double &wx, double &wy,
+                                           double &wz, bool &wchanged, ShellRec &rec) {
+  const double *Xc = S.X[buf];
+  const float4 *Xf = S.Xf[buf];
+  const int *cbox = S.cbox[buf];
+  CandIter it;
+  it.brute = alias;
+  it.lin = lin;
+  it.last = -1;
+  if (!alias) {
+    int c = tcount(S.Tcnt[buf][lin], gs);
+    it.cnt = c < TCAP ? c : TCAP;
+    it.lst = S.Tlist[buf] + (size_t)lin * TCAP;
+  } else {
+    it.cnt = 0;
+    it.lst = nullptr;
+  }
+  const double x0 = x, y0 = y, z0 = z;
+  d3 vdump = mk(0, 0, 0);
+  bool have_dump = false;
+  if (flags & F_COLLIDE) {
+    for (int j = cand_next(S, it, cbox); j >= 0; j = cand_next(S, it, cbox)) {
+      if (!within(S, Xc, Xf[j], j, x, y, z, S.r_coll, S.sig2q)) continue;
+      d3 Xj = mk(Xc[3 * j], Xc[3 * j + 1], Xc[3 * j + 2]);
+      if (!have_dump) {  // dump_vel_fl: the velocity when the collision routine began
+        vdump = mk(__dmul_rn(wx, S.inv_dt), __dmul_rn(wy, S.inv_dt), __dmul_rn(wz, S.inv_dt));
+        have_dump = true;
+      }
+      // step back half a substep with the current velocity
+      x = ref_mod(__dsub_rn(x, __dmul_rn(wx, 0.5)), S.dx);
+      y = ref_mod(__dsub_rn(y, __dmul_rn(wy, 0.5)), S.dy);
+      z = ref_mod(__dsub_rn(z, __dmul_rn(wz, 0.5)), S.dz);
+      d3 rs = mk(ref_img(__dsub_rn(x, Xj.x), S.dx), ref_img(__dsub_rn(y, Xj.y), S.dy), ref_img(__dsub_rn(z, Xj.z), S.dz));
+      CollDraw d;
+      d.key = S.key; d.a = (uint32_t)(pid + 1); d.b = (uint32_t)(j + 1); d.t = (uint32_t)gs; d.idx = 0;
+      d3 u = stochastic_reflection(S, d, mk(x, y, z), rs);
+      d3 Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]);
+      d3 Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
+      d3 vn = add3(add3(u, Vj), cross_ref(Wj, rs));
+      d3 dv = sub3(vdump, vn);
+      d3 dl = cross_ref(rs, dv);
+      ExchAcc *e = S.exch + j;
+      exch_add(e, 0, dv.x, &S.ss->err); exch_add(e, 1, dv.y, &S.ss->err); exch_add(e, 2, dv.z, &S.ss->err);
+      exch_add(e, 3, dl.x, &S.ss->err); exch_add(e, 4, dl.y, &S.ss->err); exch_add(e, 5, dl.z, &S.ss->err);
+      wx = __dmul_rn(vn.x, S.dt); wy = __dmul_rn(vn.y, S.dt); wz = __dmul_rn(vn.z, S.dt);
+      wchanged = true;
+      // step forward half a substep with the new velocity
+      x = ref_mod(__dadd_rn(x, __dmul_rn(wx, 0.5)), S.dx);
+      y = ref_mod(__dadd_rn(y, __dmul_rn(wy, 0.5)), S.dy);
+      z = ref_mod(__dadd_rn(z, __dmul_rn(wz, 0.5)), S.dz);
+      // the cell table is built with a margin; a move beyond it could hide a colloid
+      double ex = ref_img(__dsub_rn(x, x0), S.dx), ey = ref_img(__dsub_rn(y, y0), S.dy),
+             ez = ref_img(__dsub_rn(z, z0), S.dz);
+      if (norm2_ref(ex, ey, ez) > S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
+    }
+  }
+  if (flags & F_SHELL) {
+    rec.p = pid;
+    rec.n = 0;
+    rec.pass = 0;
+    it.last = -1;
+    for (int j = cand_next(S, it, cbox); j >= 0; j = cand_next(S, it, cbox)) {
+      if (!within(S, Xc, Xf[j], j, x, y, z, S.r_shell, S.rsh2)) continue;
+      if (rec.n < SHELL_J) rec.j[rec.n++] = (uint16_t)j;
+      else atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
+    }
+  }
+}
+
+// |w|^2 * 2^kw from the fixed-point w = wf 2^-kw: wf^2 2^-kw, rounded half up,
+// as a 128-bit square on the integer pipe
+static __device__ __forceinline__ long long sq_fix(long long wf, int kw) {
+  unsigned long long a = (unsigned long long)(wf < 0 ? -wf : wf);
+  unsigned long long lo = a * a, hi = __umul64hi(a, a);
+  unsigned long long lo2 = lo + (1ull << (kw - 1));
+  hi += lo2 < lo;
+  return (long long)((hi << (64 - kw)) | (lo2 >> kw));
+}
+
+// ------------------------------------------------------------- colloid helpers
+
+static __device__ __forceinline__ d3 ldv(const double *a, int j) { return mk(a[3 * j], a[3 * j + 1], a[3 * j + 2]); }
+static __device__ __forceinline__ void stv(double *a, int j, d3 v) { a[3 * j] = v.x; a[3 * j + 1] = v.y; a[3 * j + 2] = v.z; }
+
+// update_activity_direction (cpp/update.cpp:34-46): ra rotated by the Euler matrix
+// of Omega dt; then, with Dr > 0, rotational diffusion ra += sqrt(2 Dr dt)
+// (xi - (xi.ra) ra), renormalised (xi: three normals drawn for that substep)
+// (sb, cb: the sines and cosines of the components of Omega dt)
+static __device__ d3 activity_rot(const SysF64 &S, d3 ra, d3 sb, d3 cb, d3 xi) {
+  d3 m1 = mk(__dmul_rn(cb.y, cb.z), __dmul_rn(-cb.y, sb.z), sb.y);
+  d3 m2 = mk(__dadd_rn(__dmul_rn(__dmul_rn(sb.x, sb.y), cb.z), __dmul_rn(cb.x, sb.z)),
+             __dadd_rn(__dmul_rn(__dmul_rn(-sb.x, sb.y), sb.z), __dmul_rn(cb.x, cb.z)), __dmul_rn(-sb.x, cb.y));
+  d3 m3 = mk(__dadd_rn(__dmul_rn(__dmul_rn(-cb.x, sb.y), cb.z), __dmul_rn(sb.x, sb.z)),
+             __dadd_rn(__dmul_rn(__dmul_rn(cb.x, sb.y), sb.z), __dmul_rn(sb.x, cb.z)), __dmul_rn(cb.x, cb.y));
+  ra = mk(dot_ref(m1, ra), dot_ref(m2, ra), dot_ref(m3, ra));
+  if (S.Dr > 0) {
+    double xa = dot_ref(xi, ra);
+    d3 dn = sub3(xi, mul3s(ra, xa));
+    d3 a = add3(ra, mul3s(dn, S.rotdiff_s));
+    ra = div3s(a, __dsqrt_rn(norm2_ref(a.x, a.y, a.z)));
+  }
+  return ra;
+}
+
+static __device__ d3 activity(const SysF64 &S, d3 ra, d3 W, d3 xi) {
+  d3 b = mul3s(W, S.dt), sb, cb;
+  sincos(b.x, &sb.x, &cb.x);
+  sincos(b.y, &sb.y, &cb.y);
+  sincos(b.z, &sb.z, &cb.z);
+  return activity_rot(S, ra, sb, cb, xi);
+}
+
+static __device__ __forceinline__ float wrapf(float d, float L) { return d - L * rintf(d / L); }
+
+// WCA force on colloid j at positions Xc (compute_force_md, cpp/update.cpp:14-32):
+// partners with r < r_cutoff summed in ascending partner order, which is the
+// order the reference's pair loop adds them to f[j].  FP32 prefilter over all
+// colloids by the warp; exact FP64 pair terms.  Returns the force in every lane;
+// pot receives this colloid's share of the potential (pairs with k > j).
+static __device__ d3 wca_force(const SysF64 &S, const double *Xc, const float4 *Xf, int j, int lane, bool want_pot,
+                        double &pot) {
+  d3 f = mk(0, 0, 0);
+  pot = 0;
+  const float4 xj = Xf[j];
+  const float Lx = S.Lxf, Ly = S.Lyf, Lz = S.Lzf;
+  const float rcf = S.rcf;
+  const d3 Xj = ldv(Xc, j);
+  for (int base = 0; base < S.Nc; base += 32) {
+    int k = base + lane;
+    bool cand = false;
+    if (k < S.Nc && k != j) {
+      float4 xk = Xf[k];
+      float dx = wrapf(xj.x - xk.x, Lx), dy = wrapf(xj.y - xk.y, Ly), dz = wrapf(xj.z - xk.z, Lz);
+      cand = dx * dx + dy * dy + dz * dz < rcf * rcf;
+    }
+    unsigned m = __ballot_sync(FULL, cand);
+    if (!m) continue;
+    d3 ff = mk(0, 0, 0);
+    double pt = 0;
+    bool hit = false;
+    if (cand) {
+      d3 temp = mk(ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
+                   ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz));
+      double r = __dsqrt_rn(norm2_ref(temp.x, temp.y, temp.z));
+      if (r < S.r_cutoff) {
+        hit = true;
+        double p13 = r, p7 = r;
+        for (int i = 1; i < 13; ++i) { p13 = __dmul_rn(p13, r); if (i == 6) p7 = p13; }
+        double t1 = __ddiv_rn(S.sig12, p13), t2 = __ddiv_rn(S.sig6, p7);
+        double mag = __dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(__dmul_rn(12.0, t1), __dmul_rn(6.0, t2))), S.fc);
+        ff = div3s(mul3s(temp, mag), r);
+        if (want_pot && k > j) {
+          double q = __ddiv_rn(S.sig_colloid, r);
+          pt = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(pow(q, 12.0), pow(q, 6.0))), S.ufc),
+                         __dmul_rn(S.fc, r));
+        }
+      }
+    }
+    unsigned hm = __ballot_sync(FULL, hit);
+    while (hm) {
+      int src = __ffs(hm) - 1;
+      hm &= hm - 1;
+      double fx = __shfl_sync(FULL, ff.x, src), fy = __shfl_sync(FULL, ff.y, src), fz = __shfl_sync(FULL, ff.z, src);
+      double pp = __shfl_sync(FULL, pt, src);
+      f = add3(f, mk(fx, fy, fz));
+      pot = __dadd_rn(pot, pp);
+    }
+  }
+  return f;
+}
+
+// Cells of the 342-box block of colloid cell cb (own box excluded) whose box
+// comes within `reach` of the colloid position (minimum image, FP32 with margin):
+// the cells whose particles can be inside the sphere or the run() shell.
+template <typename F>
+static __device__ void for_reach_cells(const SysF64 &S, int cb, float4 xc, float reach, int first, int stride, F fn) {
+  if (cb >= S.C) return;
+  int cx = cb % S.Lx, ct = cb / S.Lx, cy = ct % S.Ly, cz = ct / S.Ly;
+  const float Lx = S.Lxf, Ly = S.Lyf, Lz = S.Lzf;
+  for (int q = first; q < 343; q += stride) {
+    int ox = q % 7 - 3, oy = (q / 7) % 7 - 3, oz = q / 49 - 3;
+    if (!ox && !oy && !oz) continue;
+    int bx = cx + ox, by = cy + oy, bz = cz + oz;
+    bx += bx < 0 ? S.Lx : 0; bx -= bx >= S.Lx ? S.Lx : 0;
+    by += by < 0 ? S.Ly : 0; by -= by >= S.Ly ? S.Ly : 0;
+    bz += bz < 0 ? S.Lz : 0; bz -= bz >= S.Lz ? S.Lz : 0;
+    float ex = fmaxf(fabsf(wrapf(xc.x - ((float)bx + 0.5f), Lx)) - 0.5f, 0.f);
+    float ey = fmaxf(fabsf(wrapf(xc.y - ((float)by + 0.5f), Ly)) - 0.5f, 0.f);
+    float ez = fmaxf(fabsf(wrapf(xc.z - ((float)bz + 0.5f), Lz)) - 0.5f, 0.f);
+    if (ex * ex + ey * ey + ez * ez <= reach * reach) fn(bx + S.Lx * (by + S.Ly * bz));
+  }
+}
+
+// reach of the cell table of substep e: the run() shell on the last substep of a
+// step (its candidates are recorded there), the sphere otherwise
+static __device__ __forceinline__ float table_reach(const SysF64 &S, long long e) {
+  return (e % S.n_sub) == S.n_sub - 1 ? S.rT_shell : S.rT_coll;
+}
+
+// Colloid work that the next substep needs and nothing in this substep changes,
+// done by the first blocks of a streaming pass while the rest streams the fluid:
+// the WCA forces at the positions X_g (compute_force_md) and the cell table of
+// substep g+1, built from X_g with a margin for the colloid's own move.  One
+// colloid per 256-thread block, its independent parts on separate warps so that
+// their FP64 latency chains overlap: warp 0 the forces, warp 1 the orientation,
+// warp 2 the rotational-diffusion draws, warps 3-7 the 343 cells of the table.
+static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, int j, bool act) {
+  const int b = (int)(g & 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    double pot;
+    d3 fn = wca_force(S, S.X[b], S.Xf[b], j, lane, false, pot);
+    if (lane == 0) stv(S.fnew, j, fn);
+    return;
+  }
+  // update_activity_direction of the previous substep: nothing before the end of
+  // this step reads the orientation, so it runs here, off the critical path
+  if (warp == 1) {
+    if (act && lane == 0) stv(S.ra, j, activity(S, ldv(S.ra, j), ldv(S.W, j), ldv(S.xi, j)));
+    return;
+  }
+  if (warp == 2) {
+    if (S.Dr > 0 && lane == 0) {
+    // the three standard normals of this substep's rotational diffusion (Box-Muller)
+    uint4 r = draw4(S.key, DOM_ROTDIFF, 0, (uint32_t)(j + 1), 0, (uint32_t)g);
+    double r0 = sqrt(-2.0 * log(u01(r.x))), r1 = sqrt(-2.0 * log(u01(r.z)));
+    double s0, c0, s1, c1;
+    sincos(__dmul_rn(S.two_pi, u01(r.y)), &s0, &c0);
+    sincos(__dmul_rn(S.two_pi, u01(r.w)), &s1, &c1);
+    stv(S.xi, j, mk(__dmul_rn(r0, c0), __dmul_rn(r0, s0), __dmul_rn(r1, c1)));
+    }
+    return;
+  }
+  const long long e = g + 1;
+  unsigned long long *Tc = S.Tcnt[e & 1];
+  uint16_t *Tl = S.Tlist[e & 1];
+  int *err = &S.ss->err;
+  for_reach_cells(S, S.cbox[b][j], S.Xf[b][j], table_reach(S, e), (int)threadIdx.x - 96, (int)blockDim.x - 96,
+                  [&](int cell) { tappend(Tc, Tl, cell, e, j, err); });
+}
+
+}  // namespace bgb

@@ -11,10 +11,9 @@ namespace bgb {
 // Maxwell-Boltzmann with standard deviation vscale (Box-Muller).  Writes the raw
 // velocity into wx/wy/wz; k_vfinish turns it into a displacement.
 __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, double vscale, double rmin,
-                                                   int max_attempts, int fb) {
+                                                   int max_attempts, InitOut o) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.N) return;
-  const Fluid F = fluid_at(S, fb);
   const int b = (int)((S.ss->step * S.n_sub - 1) & 1);
   const double *Xc = S.X[b];
   const float4 *xs = S.Xf[b];
@@ -42,9 +41,10 @@ __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, d
     }
   }
   if (!placed) atomicOr(&S.ss->err, ERRB_OCCUPANCY);
-  F.x[i] = tx; F.y[i] = ty; F.z[i] = tz;
-  F.id[i] = i;
-  S.newpos[i] = i;
+  const size_t w = (size_t)i * o.stride;
+  o.x[w] = tx; o.y[w] = ty; o.z[w] = tz;
+  if (o.id) o.id[i] = i;
+  if (o.newpos) o.newpos[i] = i;
   uint4 r = draw4(S.key, DOM_INIT_FVEL, 0, (uint32_t)(i + 1), 0, 0);
   double vx, vy, vz;
   if (style == 0) {
@@ -58,16 +58,16 @@ __global__ void __launch_bounds__(256) k_init_fluid(const SysF64 S, int style, d
     sincospi(2.0 * u01(r.w), &s1, &c1);
     vx = r0 * c0 * vscale; vy = r0 * s0 * vscale; vz = r1 * c1 * vscale;
   }
-  F.wx[i] = vx; F.wy[i] = vy; F.wz[i] = vz;
+  o.vx[w] = vx; o.vy[w] = vy; o.vz[w] = vz;
 }
 
 // per-block sums of the raw velocities, fixed order
-__global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part, int fb) {
+__global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part, InitOut o) {
   __shared__ double sh[3][256];
   double a[3] = {0, 0, 0};
-  const Fluid F = fluid_at(S, fb);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.N; i += gridDim.x * blockDim.x) {
-    a[0] += F.wx[i]; a[1] += F.wy[i]; a[2] += F.wz[i];
+    const size_t w = (size_t)i * o.stride;
+    a[0] += o.vx[w]; a[1] += o.vy[w]; a[2] += o.vz[w];
   }
   for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] = a[k];
   __syncthreads();
@@ -80,14 +80,15 @@ __global__ void __launch_bounds__(256) k_vsum(const SysF64 S, double *part, int 
     for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = sh[k][0];
 }
 
-// vel = vel - avr_vel, then the stored displacement w = fl(vel*dt)
-__global__ void __launch_bounds__(256) k_vfinish(const SysF64 S, double ax, double ay, double az, int fb) {
+// vel = vel - avr_vel, then (scale != 0) the stored displacement w = fl(vel*dt)
+__global__ void __launch_bounds__(256) k_vfinish(const SysF64 S, double ax, double ay, double az, InitOut o,
+                                                double scale) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.N) return;
-  const Fluid F = fluid_at(S, fb);
-  F.wx[i] = __dmul_rn(__dsub_rn(F.wx[i], ax), S.dt);
-  F.wy[i] = __dmul_rn(__dsub_rn(F.wy[i], ay), S.dt);
-  F.wz[i] = __dmul_rn(__dsub_rn(F.wz[i], az), S.dt);
+  const size_t w = (size_t)i * o.stride;
+  double vx = __dsub_rn(o.vx[w], ax), vy = __dsub_rn(o.vy[w], ay), vz = __dsub_rn(o.vz[w], az);
+  if (scale != 0.0) { vx = __dmul_rn(vx, scale); vy = __dmul_rn(vy, scale); vz = __dmul_rn(vz, scale); }
+  o.vx[w] = vx; o.vy[w] = vy; o.vz[w] = vz;
 }
 
 // AoS xyz triplets (the reference's point arrays, in particle order) <-> the

@@ -12,6 +12,16 @@ using StreamKernel = void (*)(const SysF64, int, int, int, int);
 StreamKernel stream_kernel(int flags);
 using EventKernel = void (*)(const SysF64, int, int);
 EventKernel event_kernel(int flags);
+// FP32-compensated form (kernels_fp32c.cu)
+StreamKernel stream_kernel32(int flags);
+EventKernel event_kernel32(int flags);
+__global__ void k_cell_prep32(const SysF64 S);
+__global__ void k_rotate32(const SysF64 S, int fb);
+__global__ void k_rotate_sort32(const SysF64 S, int src, int dst);
+__global__ void k_run_shell32(const SysF64 S, int fb);
+__global__ void k_run_kick32(const SysF64 S, int fb);
+__global__ void k_aos_to_q(const SysF64 S, const double *pos, const double *vel, int fb);
+__global__ void k_q_to_aos(const SysF64 S, double *pos, double *vel, int fb);
 __global__ void k_cell_prep(const SysF64 S);
 __global__ void k_scan_blocks(const SysF64 S, int nblk);
 __global__ void k_rotate_sort(const SysF64 S, int src, int dst);
@@ -25,9 +35,16 @@ __global__ void k_end_step(const SysF64 S);
 __global__ void k_diag_fluid(const SysF64 S, double *part);
 
 // initialisation
-__global__ void k_init_fluid(const SysF64 S, int style, double vscale, double rmin, int max_attempts, int fb);
-__global__ void k_vsum(const SysF64 S, double *part, int fb);
-__global__ void k_vfinish(const SysF64 S, double ax, double ay, double az, int fb);
+// where the initial fluid state goes: positions and velocities with an element
+// stride (1: the FP64 SoA buffers; 3: AoS staging converted afterwards)
+struct InitOut {
+  double *x, *y, *z, *vx, *vy, *vz;
+  int stride;
+  int *id, *newpos;
+};
+__global__ void k_init_fluid(const SysF64 S, int style, double vscale, double rmin, int max_attempts, InitOut o);
+__global__ void k_vsum(const SysF64 S, double *part, InitOut o);
+__global__ void k_vfinish(const SysF64 S, double ax, double ay, double az, InitOut o, double scale);
 __global__ void k_aos_to_soa(const double *aos, double *x, double *y, double *z, int *id, int *newpos, int n,
                              double scale);
 __global__ void k_soa_to_aos(double *aos, const double *x, const double *y, const double *z, const int *id, int n,

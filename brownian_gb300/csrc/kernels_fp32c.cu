@@ -1,0 +1,536 @@
+// FP32-compensated form of the MPCD + active-colloid step (sm_103a).
+//
+// The fluid is stored per particle as one 16-byte record {packed cell, offset x,
+// offset y, offset z} (a single 128-bit load) plus FP32 velocities: 28 bytes where
+// the FP64 form keeps 48, and all fluid arithmetic runs on the FP32 pipe.  A
+// position is its integer cell plus an FP32 offset in [0, 1), so it is resolved to
+// 2^-24 of a cell everywhere in the box, and a particle-colloid distance is an
+// exact integer cell difference plus an FP32 offset difference.  What stays in
+// FP64 / exact: the colloids (shared with the FP64 form), the per-cell sums
+// (exact fixed-point integers, so the cell momentum is summed without rounding),
+// the thermostat factor of each cell, the colloid momentum exchange (exact
+// fixed-point) and every diagnostic.
+//
+// Kernels mirror the FP64 form: k_stream32 (stream, FP32 scan of nearby colloids,
+// event list, last-substep binning), k_events32 (wall collisions in FP32, one per
+// lane), k_cell_prep32, k_rotate32 / k_rotate_sort32, k_run_shell32 / k_run_kick32.
+#include "device.cuh"
+
+namespace bgb {
+
+__device__ __forceinline__ void unpack(uint4 r, int &cx, int &cy, int &cz, float &ox, float &oy, float &oz) {
+  cx = (int)(r.x & 1023u); cy = (int)((r.x >> 10) & 1023u); cz = (int)((r.x >> 20) & 1023u);
+  ox = __uint_as_float(r.y); oy = __uint_as_float(r.z); oz = __uint_as_float(r.w);
+}
+
+__device__ __forceinline__ uint4 pack(int cx, int cy, int cz, float ox, float oy, float oz) {
+  return make_uint4((unsigned)cx | ((unsigned)cy << 10) | ((unsigned)cz << 20), __float_as_uint(ox),
+                    __float_as_uint(oy), __float_as_uint(oz));
+}
+
+// keep the offset in [0, 1), carrying whole cells into the periodic cell index
+__device__ __forceinline__ void carry(int &c, float &o, int L) {
+  if (o >= 0.f && o < 1.f) return;
+  float f = floorf(o);
+  o -= f;
+  if (o >= 1.f) { o = 0.f; f += 1.f; }
+  if (!(f == f) || fabsf(f) > 1e6f) { o = 0.f; f = 0.f; }  // NaN / runaway: stays put (flagged by the range test)
+  c += (int)f;
+  c %= L;
+  if (c < 0) c += L;
+}
+
+// particle minus colloid along one axis, minimum image: integer cell difference
+// (exact) plus offset difference
+__device__ __forceinline__ float rel(int c, float o, float cq, float co, int L) {
+  int d = c - (int)cq;
+  if (d > (L >> 1)) d -= L;
+  else if (d < -(L >> 1)) d += L;
+  return (float)d + (o - co);
+}
+
+// uniform in (0,1) from the top 23 bits: (k + 1/2) 2^-23 is exact in FP32, so the
+// value is never 0 or 1 (with 24 bits the top value would round to 1 and a
+// reflection would take log(0))
+__device__ __forceinline__ float u01f(uint32_t w) { return ((float)(w >> 9) + 0.5f) * 1.1920928955078125e-7f; }
+
+// round(v * 2^k) of an FP32 value from its bits (exact when the scale covers the
+// value's last bit)
+__device__ __forceinline__ long long to_fix_f(float v, int k) {
+  unsigned b = __float_as_uint(v);
+  int e = (int)((b >> 23) & 0xFF);
+  if (e == 0) return 0;
+  long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  int sh = e - 150 + k;
+  long long r;
+  if (sh >= 0) r = m << (sh < 62 ? sh : 62);
+  else if (sh > -40) {
+    int s = -sh;
+    r = m >> s;
+    long long rem = m & ((1ll << s) - 1), half = 1ll << (s - 1);
+    if (rem > half || (rem == half && (r & 1))) r += 1;
+  } else r = 0;
+  return (b >> 31) ? -r : r;
+}
+
+// the exact sums of the SRD binning for the next step (rotation_mpcd bins by the
+// shifted position: cell + floor(offset + rr) per axis)
+__device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, int cz, float ox, float oy, float oz,
+                                      float vx, float vy, float vz) {
+  const float *rr = S.ss->rrf;
+  float tx = ox + rr[0], ty = oy + rr[1], tz = oz + rr[2];
+  int bx = cx + (tx < 0.f ? -1 : (tx >= 1.f ? 1 : 0));
+  int by = cy + (ty < 0.f ? -1 : (ty >= 1.f ? 1 : 0));
+  int bz = cz + (tz < 0.f ? -1 : (tz >= 1.f ? 1 : 0));
+  bx += bx < 0 ? S.Lx : 0; bx -= bx >= S.Lx ? S.Lx : 0;
+  by += by < 0 ? S.Ly : 0; by -= by >= S.Ly ? S.Ly : 0;
+  bz += bz < 0 ? S.Lz : 0; bz -= bz >= S.Lz ? S.Lz : 0;
+  const int c = bx + S.Lx * (by + S.Ly * bz);
+  S.rotcell[p] = c;
+  if (!(fabsf(vx) <= S.vmaxf && fabsf(vy) <= S.vmaxf && fabsf(vz) <= S.vmaxf)) atomicOr(&S.ss->err, ERRB_VRANGE);
+  long long fx = to_fix_f(vx, S.kw), fy = to_fix_f(vy, S.kw), fz = to_fix_f(vz, S.kw);
+  long long f2 = sq_fix(fx, S.kw) + sq_fix(fy, S.kw) + sq_fix(fz, S.kw);
+  CellAcc *a = S.acc + c;
+  atomicAdd(&a->n, 1);
+  atomicAdd((unsigned long long *)&a->sx, (unsigned long long)fx);
+  atomicAdd((unsigned long long *)&a->sy, (unsigned long long)fy);
+  atomicAdd((unsigned long long *)&a->sz, (unsigned long long)fz);
+  atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32(const SysF64 S, int l, int naux, int act, int fb) {
+  constexpr int flags = FLAGS;
+  const long long step = S.ss->step;
+  const long long gs = step * S.n_sub + (l - 1);
+  if ((int)blockIdx.x < naux) {
+    if ((int)blockIdx.x < S.Nc) colloid_aux(S, gs, blockIdx.x, act != 0);
+    return;
+  }
+  const Fluid32 F = fluid32_at(S, fb);
+  const int p = (blockIdx.x - naux) * blockDim.x + threadIdx.x;
+  const bool valid = p < S.N;
+  const int buf = (int)(gs & 1);
+  bool ev = false;
+  unsigned members = 0;
+  const uint16_t *lst = nullptr;
+  int cnt = 0;
+  if (valid) {
+    int cx, cy, cz;
+    float ox, oy, oz;
+    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+    if (flags & F_STREAM) {
+      ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
+      carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+    }
+    if (flags & (F_COLLIDE | F_SHELL)) {
+      const int lin = cx + S.Lx * (cy + S.Ly * cz);
+      cnt = tcount(S.Tcnt[buf][lin], gs);
+      if (cnt > 0) {
+        cnt = cnt < TCAP ? cnt : TCAP;
+        lst = S.Tlist[buf] + (size_t)lin * TCAP;
+        const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+        const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
+        for (int k = 0; k < cnt; ++k) {
+          const int j = lst[k];
+          float4 cq = Xq[j], co = Xo[j];
+          float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly), dz = rel(cz, oz, cq.z, co.z, S.Lz);
+          float d2 = dx * dx + dy * dy + dz * dz;
+          if (flags & F_COLLIDE) ev |= d2 <= rc2;
+          if ((flags & F_SHELL) && d2 <= rs2) members |= 1u << k;
+        }
+      }
+    }
+    if (!ev && (flags & F_BINROT)) bin32(S, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+    if (flags & F_STREAM) F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+  }
+  // block-aggregated appends: events and (last substep) run() candidate records
+  __shared__ int s_ev, s_rec, s_evb, s_recb;
+  if (threadIdx.x == 0) { s_ev = 0; s_rec = 0; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const bool has_rec = (flags & F_SHELL) && !ev && members != 0;
+  const unsigned mev = __ballot_sync(FULL, ev), mrec = __ballot_sync(FULL, has_rec);
+  int oev = 0, orec = 0;
+  if (lane == 0) {
+    if (mev) oev = atomicAdd(&s_ev, __popc(mev));
+    if (mrec) orec = atomicAdd(&s_rec, __popc(mrec));
+  }
+  oev = __shfl_sync(FULL, oev, 0);
+  orec = __shfl_sync(FULL, orec, 0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_evb = s_ev ? atomicAdd(&S.ss->nevents, s_ev) : 0;
+    s_recb = s_rec ? atomicAdd(&S.ss->nshell, s_rec) : 0;
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  if (ev) {
+    int i = s_evb + oev + __popc(mev & lt);
+    if (i < S.events_cap) S.events[i] = p;
+    else atomicOr(&S.ss->err, ERRB_SHELL);
+  }
+  if (has_rec) {
+    int i = s_recb + orec + __popc(mrec & lt);
+    if (i < S.shell_cap) {
+      ShellRec *r = S.shell + i;
+      r->p = F.id[p];
+      r->pass = 0;
+      int n = 0, last = -1;
+      for (int it = 0; it < cnt && n < SHELL_J; ++it) {
+        int best = 0x7FFFFFFF;
+        for (int k = 0; k < cnt; ++k) {
+          int j = lst[k];
+          if (((members >> k) & 1u) && j > last && j < best) best = j;
+        }
+        if (best == 0x7FFFFFFF) break;
+        r->j[n++] = (uint16_t)best;
+        last = best;
+      }
+      if (__popc(members) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
+      r->n = (uint8_t)n;
+    } else {
+      atomicOr(&S.ss->err, ERRB_SHELL);
+    }
+  }
+}
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 fm(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ f3 fcross(f3 a, f3 b) { return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+// stochastic_reflection (cpp/fluid_colloid_collision.cpp:7-24) in FP32 with the
+// same keyed draws as the FP64 form: Rayleigh normal speed along rs plus one
+// Gaussian tangential component along unit(un x t)
+__device__ f3 reflect32(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, f3 rf, f3 rs) {
+  int idx = 0;
+  uint4 buf = make_uint4(0, 0, 0, 0);
+  auto next = [&]() {
+    int s = idx & 3;
+    if (s == 0) buf = draw4(S.key, DOM_COLL, (uint32_t)(idx >> 2), a, b, t);
+    idx++;
+    uint32_t w = s == 0 ? buf.x : s == 1 ? buf.y : s == 2 ? buf.z : buf.w;
+    return u01f(w);
+  };
+  float u = next();
+  float om = 1.f - u;
+  float val = sqrtf(-logf(om * om) * (float)S.inv_m_beta);
+  float ir = rsqrtf(rs.x * rs.x + rs.y * rs.y + rs.z * rs.z);
+  f3 un = fm(rs.x * ir * val, rs.y * ir * val, rs.z * ir * val);
+  float t0 = next(), t1 = next(), t2 = next();
+  f3 tt = fm(t0 * S.Lxf - rf.x, t1 * S.Lyf - rf.y, t2 * S.Lzf - rf.z);
+  tt.x -= S.Lxf * rintf(tt.x / S.Lxf); tt.y -= S.Lyf * rintf(tt.y / S.Lyf); tt.z -= S.Lzf * rintf(tt.z / S.Lzf);
+  f3 ut = fcross(un, tt);
+  float iu = rsqrtf(ut.x * ut.x + ut.y * ut.y + ut.z * ut.z);
+  float x1 = 0.f, z = 2.f;
+  for (int it = 0; z > 1.f && it < 256; ++it) {
+    x1 = 2.f * next() - 1.f;
+    float x2 = 2.f * next() - 1.f;
+    z = x1 * x1 + x2 * x2;
+  }
+  z = sqrtf(-2.f * logf(z) / z);
+  float v1 = x1 * z * (float)S.sqrt_kt_m;
+  return fm(ut.x * iu * v1 + un.x, ut.y * iu * v1 + un.y, ut.z * iu * v1 + un.z);
+}
+
+// wall collisions of the listed particles in colloid order, then (last substep)
+// their run() record and binning; one particle per lane
+template <int FLAGS>
+__global__ void __launch_bounds__(128) k_events32(const SysF64 S, int l, int fb) {
+  constexpr int flags = FLAGS;
+  const long long step = S.ss->step;
+  const long long gs = step * S.n_sub + (l - 1);
+  const int buf = (int)(gs & 1);
+  const Fluid32 F = fluid32_at(S, fb);
+  const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+  const int n = min(S.ss->nevents, S.events_cap);
+  const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
+  // event i goes to block i % gridDim.x: the few hundred to few thousand events of
+  // a substep spread over all SMs instead of filling the first few
+  for (int i = blockIdx.x + gridDim.x * threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int p = S.events[i];
+    int cx, cy, cz;
+    float ox, oy, oz;
+    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+    const int lin = cx + S.Lx * (cy + S.Ly * cz);
+    int cnt = tcount(S.Tcnt[buf][lin], gs);
+    cnt = cnt < TCAP ? cnt : TCAP;
+    const uint16_t *lst = S.Tlist[buf] + (size_t)lin * TCAP;
+    const int id = F.id[p];
+    const f3 vdump = fm(vx, vy, vz);
+    if (flags & F_COLLIDE) {
+      for (int last = -1;;) {
+        int j = 0x7FFFFFFF;
+        for (int k = 0; k < cnt; ++k) {
+          int c = lst[k];
+          if (c > last && c < j) j = c;
+        }
+        if (j == 0x7FFFFFFF) break;
+        last = j;
+        float4 cq = Xq[j], co = Xo[j];
+        f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+        if (!(r.x * r.x + r.y * r.y + r.z * r.z <= rc2)) continue;
+        // back half a substep, reflect, forward half a substep
+        ox -= 0.5f * vx * S.dtf; oy -= 0.5f * vy * S.dtf; oz -= 0.5f * vz * S.dtf;
+        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+        f3 rs = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+        f3 rf = fm((float)cx + ox, (float)cy + oy, (float)cz + oz);
+        f3 u = reflect32(S, (uint32_t)(id + 1), (uint32_t)(j + 1), (uint32_t)gs, rf, rs);
+        f3 V = fm((float)S.V[3 * j], (float)S.V[3 * j + 1], (float)S.V[3 * j + 2]);
+        f3 W = fm((float)S.W[3 * j], (float)S.W[3 * j + 1], (float)S.W[3 * j + 2]);
+        f3 wr = fcross(W, rs);
+        vx = u.x + V.x + wr.x; vy = u.y + V.y + wr.y; vz = u.z + V.z + wr.z;
+        f3 dv = fm(vdump.x - vx, vdump.y - vy, vdump.z - vz);
+        f3 dl = fcross(rs, dv);
+        ExchAcc *e = S.exch + j;
+        exch_add(e, 0, (double)dv.x, &S.ss->err); exch_add(e, 1, (double)dv.y, &S.ss->err);
+        exch_add(e, 2, (double)dv.z, &S.ss->err); exch_add(e, 3, (double)dl.x, &S.ss->err);
+        exch_add(e, 4, (double)dl.y, &S.ss->err); exch_add(e, 5, (double)dl.z, &S.ss->err);
+        ox += 0.5f * vx * S.dtf; oy += 0.5f * vy * S.dtf; oz += 0.5f * vz * S.dtf;
+        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+      }
+    }
+    if (flags & F_SHELL) {
+      ShellRec rec;
+      rec.p = id;
+      rec.n = 0;
+      rec.pass = 0;
+      for (int last = -1; rec.n < SHELL_J;) {
+        int j = 0x7FFFFFFF;
+        for (int k = 0; k < cnt; ++k) {
+          int c = lst[k];
+          if (c > last && c < j) j = c;
+        }
+        if (j == 0x7FFFFFFF) break;
+        last = j;
+        float4 cq = Xq[j], co = Xo[j];
+        float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly), dz = rel(cz, oz, cq.z, co.z, S.Lz);
+        if (dx * dx + dy * dy + dz * dz <= rs2) rec.j[rec.n++] = (uint16_t)j;
+      }
+      if (rec.n) {
+        int idx = atomicAdd(&S.ss->nshell, 1);
+        if (idx < S.shell_cap) S.shell[idx] = rec;
+        else atomicOr(&S.ss->err, ERRB_SHELL);
+      }
+    }
+    if (flags & F_BINROT) bin32(S, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+    F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+    F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+  }
+}
+
+StreamKernel stream_kernel32(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_stream32<F_STREAM | F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream32<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_SHELL | F_BINROT: return k_stream32<F_SHELL | F_BINROT>;
+  }
+  return nullptr;
+}
+
+EventKernel event_kernel32(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_events32<F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_events32<F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_SHELL | F_BINROT: return k_events32<F_SHELL | F_BINROT>;
+  }
+  return nullptr;
+}
+
+// SRD collision per cell (cpp/rotation_mpcd.cpp:14-49): cell mean from the exact
+// sums, thermostat factor in FP64, rotation about the random axis in FP32, stored
+// as the FP32 affine map v' = A v + b; plus the occupancy prefix of the counting sort.
+__global__ void __launch_bounds__(256) k_cell_prep32(const SysF64 S) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < S.Nc) S.shell_cnt[c] = 0;
+  CellAcc a = CellAcc{0, 0, 0, 0, 0, 0};
+  if (c < S.Cpad) {
+    a = S.acc[c];
+    S.acc[c] = CellAcc{0, 0, 0, 0, 0, 0};
+    S.cursor[c] = 0;
+  }
+  {
+    __shared__ int wsum[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = a.n, incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int q = 0; q < 8; ++q) {
+      before += q < w ? wsum[q] : 0;
+      total += wsum[q];
+    }
+    if (c < S.Cpad) S.cell_off[c] = before + incl - v;
+    if (threadIdx.x == 0) S.blk_off[blockIdx.x] = total;
+  }
+  if (c >= S.C) return;
+  float *ab = S.cell_ab32 + (size_t)c * 12;
+  const int n = a.n;
+  if (n > S.max_per_cell) atomicOr(&S.ss->err, ERRB_OCCUPANCY);
+  if (n <= 1 || n > S.max_per_cell) {
+    ab[0] = 1; ab[1] = 0; ab[2] = 0; ab[3] = 0; ab[4] = 1; ab[5] = 0; ab[6] = 0; ab[7] = 0; ab[8] = 1;
+    ab[9] = 0; ab[10] = 0; ab[11] = 0;
+    return;
+  }
+  // mean and thermostat factor in FP64 from the exact sums
+  const double inv = S.inv_n[n];
+  const double ux = (double)a.sx * S.inv_sw * inv, uy = (double)a.sy * S.inv_sw * inv, uz = (double)a.sz * S.inv_sw * inv;
+  const double var = (double)a.s2 * S.inv_sw - (double)n * (ux * ux + uy * uy + uz * uz);
+  // S.cs is 3 kT dt^2 / m for the displacement sums of the FP64 form; these are velocity sums
+  const float s = var > 0 ? (float)sqrt(S.cs * S.inv_dt * S.inv_dt * (double)(n - 1) / var) : 1.f;
+  // rotation axis rho = 2 ran - 1, phi = 2 pi ran (cpp/rotation_mpcd.cpp:19-20)
+  uint4 r = draw4(S.key, DOM_AXIS, 0, (uint32_t)(c + 1), 0, (uint32_t)(S.ss->step + 1));
+  const float rho = 2.f * u01f(r.x) - 1.f;
+  float sp, cp;
+  sincospif(2.f * u01f(r.y), &sp, &cp);
+  const float sq = sqrtf(fmaxf(1.f - rho * rho, 0.f));
+  const float r1 = cp * sq, r2 = sp * sq, r3 = rho;
+  const float ct = (float)S.ct, st = (float)S.st, ict = (float)S.ict;
+  const float i1 = ict * r1, i2 = ict * r2, i3 = ict * r3;
+  const float R[9] = {i1 * r1 + ct, i1 * r2 - st * r3, i1 * r3 + st * r2,
+                      i2 * r1 + st * r3, i2 * r2 + ct, i2 * r3 - st * r1,
+                      i3 * r1 - st * r2, i3 * r2 + st * r1, i3 * r3 + ct};
+  const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) ab[k] = s * R[k];
+  ab[9] = fx - (ab[0] * fx + ab[1] * fy + ab[2] * fz);
+  ab[10] = fy - (ab[3] * fx + ab[4] * fy + ab[5] * fz);
+  ab[11] = fz - (ab[6] * fx + ab[7] * fy + ab[8] * fz);
+}
+
+__device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &vy, float &vz) {
+  const float4 *m = reinterpret_cast<const float4 *>(ab);
+  float4 a = m[0], b = m[1], c = m[2];
+  float nx = fmaf(a.x, vx, fmaf(a.y, vy, fmaf(a.z, vz, c.y)));
+  float ny = fmaf(a.w, vx, fmaf(b.x, vy, fmaf(b.y, vz, c.z)));
+  float nz = fmaf(b.z, vx, fmaf(b.w, vy, fmaf(c.x, vz, c.w)));
+  vx = nx; vy = ny; vz = nz;
+}
+
+__global__ void __launch_bounds__(256) k_rotate32(const SysF64 S, int fb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= S.N) return;
+  const int c = S.rotcell[p];
+  if (c >= S.C) return;
+  const Fluid32 F = fluid32_at(S, fb);
+  float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+  apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
+  F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+}
+
+__global__ void __launch_bounds__(256) k_rotate_sort32(const SysF64 S, int src, int dst) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= S.N) return;
+  const Fluid32 F = fluid32_at(S, src), G = fluid32_at(S, dst);
+  const int c = S.rotcell[p];
+  float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+  if (c < S.C) apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, c);
+  const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&S.cursor[c], __popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  const int slot = S.blk_off[c >> 8] + S.cell_off[c] + base + __popc(grp & ((1u << lane) - 1u));
+  const int id = F.id[p];
+  if (slot < 0 || slot >= S.N || id < 0 || id >= S.N) {
+    atomicOr(&S.ss->err, ERRB_OCCUPANCY);
+    return;
+  }
+  G.q[slot] = F.q[p];
+  G.vx[slot] = vx; G.vy[slot] = vy; G.vz[slot] = vz;
+  G.id[slot] = id;
+  S.newpos[id] = slot;
+}
+
+// run() (cpp/run.cpp:17-24) on the FP32 fluid: rear-shell test against V + v0 ra
+__global__ void k_run_shell32(const SysF64 S, int fb) {
+  const int n = min(S.ss->nshell, S.shell_cap);
+  const int b = (int)((S.ss->step * S.n_sub - 1) & 1);
+  const float4 *Xq = S.Xcq[b], *Xo = S.Xco[b];
+  const Fluid32 F = fluid32_at(S, fb);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    ShellRec rec = S.shell[i];
+    int p = S.newpos[rec.p];
+    int cx, cy, cz;
+    float ox, oy, oz;
+    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    uint8_t pass = 0;
+    for (int k = 0; k < rec.n; ++k) {
+      int j = rec.j[k];
+      float4 cq = Xq[j], co = Xo[j];
+      float rx = rel(cx, ox, cq.x, co.x, S.Lx), ry = rel(cy, oy, cq.y, co.y, S.Ly), rz = rel(cz, oz, cq.z, co.z, S.Lz);
+      double Vx = S.V[3 * j] + S.ra[3 * j] * S.v0, Vy = S.V[3 * j + 1] + S.ra[3 * j + 1] * S.v0,
+             Vz = S.V[3 * j + 2] + S.ra[3 * j + 2] * S.v0;
+      if (rx * (float)Vx + ry * (float)Vy + rz * (float)Vz <= 0.f) {
+        pass |= (uint8_t)(1u << k);
+        atomicAdd(&S.shell_cnt[j], 1);
+      }
+    }
+    S.shell[i].pass = pass;
+  }
+}
+
+__global__ void k_run_kick32(const SysF64 S, int fb) {
+  const int n = min(S.ss->nshell, S.shell_cap);
+  const Fluid32 F = fluid32_at(S, fb);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    ShellRec rec = S.shell[i];
+    if (!rec.pass) continue;
+    int p = S.newpos[rec.p];
+    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+    for (int k = 0; k < rec.n; ++k) {
+      if (!((rec.pass >> k) & 1)) continue;
+      int j = rec.j[k];
+      double f = S.mass_colloid / (S.mass_fl * (double)S.shell_cnt[j]) * S.v0;
+      vx -= (float)(S.ra[3 * j] * f); vy -= (float)(S.ra[3 * j + 1] * f); vz -= (float)(S.ra[3 * j + 2] * f);
+    }
+    F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+  }
+}
+
+// AoS doubles (particle order) -> FP32 records; download scatters back by id
+__global__ void __launch_bounds__(256) k_aos_to_q(const SysF64 S, const double *pos, const double *vel, int fb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S.N) return;
+  const Fluid32 F = fluid32_at(S, fb);
+  int c[3];
+  float o[3];
+  const int L[3] = {S.Lx, S.Ly, S.Lz};
+  for (int k = 0; k < 3; ++k) {
+    double x = pos[3 * (size_t)i + k];
+    double fl = floor(x);
+    double off = x - fl;
+    long long ci = (long long)fl;
+    float of = (float)off;
+    if (of >= 1.f) { of = 0.f; ci += 1; }
+    ci %= L[k];
+    if (ci < 0) ci += L[k];
+    c[k] = (int)ci;
+    o[k] = of;
+  }
+  F.q[i] = pack(c[0], c[1], c[2], o[0], o[1], o[2]);
+  F.vx[i] = (float)vel[3 * (size_t)i]; F.vy[i] = (float)vel[3 * (size_t)i + 1]; F.vz[i] = (float)vel[3 * (size_t)i + 2];
+  F.id[i] = i;
+  S.newpos[i] = i;
+}
+
+__global__ void __launch_bounds__(256) k_q_to_aos(const SysF64 S, double *pos, double *vel, int fb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S.N) return;
+  const Fluid32 F = fluid32_at(S, fb);
+  int cx, cy, cz;
+  float ox, oy, oz;
+  unpack(F.q[i], cx, cy, cz, ox, oy, oz);
+  const size_t o = 3 * (size_t)F.id[i];
+  if (pos) { pos[o] = (double)cx + (double)ox; pos[o + 1] = (double)cy + (double)oy; pos[o + 2] = (double)cz + (double)oz; }
+  if (vel) { vel[o] = F.vx[i]; vel[o + 1] = F.vy[i]; vel[o + 2] = F.vz[i]; }
+}
+
+}  // namespace bgb

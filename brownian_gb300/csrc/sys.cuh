@@ -50,6 +50,7 @@ struct StepState {
   int nevents;      // particles the streaming pass left to k_events
   long long ev_total;  // events summed over substeps (diagnostics)
   double rr[3];     // grid shift of the SRD binning the next streaming pass performs
+  float rrf[3];     // the same, FP32
 };
 
 struct SysF64 {
@@ -117,6 +118,18 @@ struct SysF64 {
   // particles near a sphere surface in the substep in flight
   int *events;
   int events_cap;
+  // FP32-compensated fluid (precision MPCD_FP32C): per particle one 16-byte record
+  // {cell x | y << 10 | z << 20, offset x, offset y, offset z} with offsets in
+  // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32
+  // velocities; both buffers as for the FP64 fluid
+  int precision;
+  uint4 *q[2];
+  float *v32[2][3];
+  float *cell_ab32;    // [C][12] SRD map in FP32
+  float dtf;           // dt in FP32
+  float vmaxf;         // speed bound of the exact cell sums
+  float4 *Xcq[2];      // colloid cell (integer-valued floats), double-buffered like X
+  float4 *Xco[2];      // colloid offset within the cell
   // step state
   StepState *ss;
   double *pot_part;    // [Nc] per-colloid share of the WCA potential
@@ -132,6 +145,21 @@ __device__ __host__ __forceinline__ Fluid fluid_at(const SysF64 &S, int b) {
   Fluid f;
   f.x = S.fl[b][0]; f.y = S.fl[b][1]; f.z = S.fl[b][2];
   f.wx = S.fl[b][3]; f.wy = S.fl[b][4]; f.wz = S.fl[b][5];
+  f.id = S.pid[b];
+  return f;
+}
+
+// view of one FP32-compensated fluid buffer
+struct Fluid32 {
+  uint4 *q;
+  float *vx, *vy, *vz;
+  int *id;
+};
+
+__device__ __host__ __forceinline__ Fluid32 fluid32_at(const SysF64 &S, int b) {
+  Fluid32 f;
+  f.q = S.q[b];
+  f.vx = S.v32[b][0]; f.vy = S.v32[b][1]; f.vz = S.v32[b][2];
   f.id = S.pid[b];
   return f;
 }

@@ -138,6 +138,13 @@ int mpcd_profile_read(mpcd_ctx *c, char names[][48], int64_t *launches, double *
 /* kernels launched by this context since creation (all of them are this library's own) */
 int64_t mpcd_launch_count(const mpcd_ctx *c);
 
+/* ---- launch shapes (no counterpart in the reference: tuning of this implementation) -- */
+enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, multiple of 32) */
+       MPCD_LAUNCH_FIN = 1 };  /* colloid finish: grid, block (<= 128, multiple of 32) */
+/* grid <= 0 restores the default (one block per SM); results do not depend on the
+ * shape (every sum is exact); drops the captured step graphs */
+int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
+
 #ifdef __cplusplus
 }
 #endif
