@@ -25,7 +25,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
            "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch"]
-LAUNCH_EVENTS, LAUNCH_FIN = 0, 1
+LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
 
 
 class MPCDError(RuntimeError):

@@ -50,6 +50,8 @@ struct mpcd_ctx {
   DevAlloc mem;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t aux = nullptr;    // second stream: colloid work beside the fluid passes
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sorts][fluid buffer]
   int step_launches[2][2] = {{0, 0}, {0, 0}};
   int fbuf = 0;                  // fluid buffer holding the current state
@@ -119,19 +121,25 @@ static cudaEvent_t pool_event(mpcd_ctx *c) {
 }
 
 template <typename... KArgs, typename... Args>
-static void launch(mpcd_ctx *c, const char *name, void (*k)(KArgs...), dim3 g, dim3 b, Args... args) {
+static void launch_on(mpcd_ctx *c, cudaStream_t s, const char *name, void (*k)(KArgs...), dim3 g, dim3 b,
+                      Args... args) {
   ProfEvent pe{name, nullptr, nullptr};
   if (c->profile) {
     pe.a = pool_event(c);
     pe.b = pool_event(c);
-    cudaEventRecord(pe.a, c->stream);
+    cudaEventRecord(pe.a, s);
   }
-  k<<<g, b, 0, c->stream>>>(args...);
+  k<<<g, b, 0, s>>>(args...);
   c->launches++;
   if (c->profile) {
-    cudaEventRecord(pe.b, c->stream);
+    cudaEventRecord(pe.b, s);
     c->pending.push_back(pe);
   }
+}
+
+template <typename... KArgs, typename... Args>
+static void launch(mpcd_ctx *c, const char *name, void (*k)(KArgs...), dim3 g, dim3 b, Args... args) {
+  launch_on(c, c->stream, name, k, g, b, args...);
 }
 
 // a copy ordered on the context's stream (which does not synchronise with the
@@ -153,15 +161,26 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
   const char *name = flags == (F_STREAM | F_COLLIDE) ? "k_stream"
                      : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
                      : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
-  // the streaming passes of substeps carry the colloid forces and the next cell
-  // table in their first blocks (one colloid per block)
-  int naux = (flags & F_STREAM) ? c->S.Nc : 0;
   const bool f32 = c->S.precision == MPCD_FP32C;
-  launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags), naux + blocks_for(c->S.N, 256), 256, c->S, l,
-         naux, act, fb);
+  // The colloid forces, the next cell table and the orientation work of a substep
+  // need nothing the fluid passes write: they run as a kernel of their own (which
+  // keeps the streaming pass at its own, low register count) on the second,
+  // high-priority stream, whose few blocks start as streaming blocks retire.
+  const bool fork = (flags & F_STREAM) && c->S.Nc > 0;
+  if (fork) {
+    cudaEventRecord(c->ev_fork, c->stream);
+    cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+  }
+  launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags),
+         blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread() : 1)), 256, c->S, l, fb);
+  if (fork) {
+    launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act);
+    cudaEventRecord(c->ev_join, c->aux);
+  }
   // the particles it left near a sphere surface, one per lane
   launch(c, "k_events", f32 ? event_kernel32(flags) : event_kernel(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm,
          c->ev_block, c->S, l, fb);
+  if (fork) cudaStreamWaitEvent(c->stream, c->ev_join, 0);  // k_fin reads the forces and the orientation
 }
 
 static void enq_fin(mpcd_ctx *c, int mode, int l) {
@@ -344,6 +363,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   const double vmax = p.vmax > 0 ? p.vmax : 24.0 * sqrt(p.kbt / p.mass_fl);
   S.precision = p.precision;
+  S.aux_nw = 4;
   S.dtf = (float)dt;
   S.vmaxf = (float)vmax;
   // the FP64 form sums displacements w = v dt, the FP32 form velocities
@@ -422,6 +442,16 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     return MPCD_ERR_CUDA;
   }
   c->own_stream = true;
+  // the side stream has the highest priority: its few blocks are scheduled as soon
+  // as streaming blocks retire instead of after the whole streaming pass
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    mpcd_destroy(c);
+    return MPCD_ERR_CUDA;
+  }
   {
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
@@ -444,6 +474,9 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->staging2) cudaFree(c->staging2);
   if (c->ss_host) cudaFreeHost(c->ss_host);
   if (c->own_stream) cudaStreamDestroy(c->stream);
+  if (c->aux) cudaStreamDestroy(c->aux);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
   return MPCD_OK;
 }
@@ -627,6 +660,12 @@ extern "C" int mpcd_set_step(mpcd_ctx *c, int64_t step) {
 
 extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
   if (!c) return MPCD_ERR_PARAM;
+  if (which == MPCD_LAUNCH_AUX) {
+    if (grid > 0 && block != 64 && block != 128 && block != 256)
+      return fail(c, MPCD_ERR_PARAM, "colloid side work: 64, 128 or 256 threads per colloid");
+    c->S.aux_nw = grid > 0 ? block / 32 : 4;
+    return drop_graph(c);
+  }
   if (grid > 65535 || (grid > 0 && (block < 32 || block > 128 || block % 32)))
     return fail(c, MPCD_ERR_PARAM, "launch shape: block a multiple of 32 in [32, 128], grid <= 65535");
   if (which == MPCD_LAUNCH_EVENTS) {

@@ -45,27 +45,40 @@ static __device__ __forceinline__ int cell_of_pos(const SysF64 &S, double x, dou
   return lin_cell(S, ix, iy, iz);
 }
 
-// count of the cell-table entry if it belongs to substep g
-static __device__ __forceinline__ int tcount(unsigned long long v, long long g) {
-  return (unsigned)(v >> 32) == (unsigned)g ? (int)(unsigned)v : 0;
+// Base index in a shared list for the lanes in mask m of this warp, from one
+// global atomic per block (the whole block must call it): for the run() records
+// of a last substep, about one particle in sixteen, too many for one atomic per
+// warp on a single counter.
+static __device__ __forceinline__ int block_base(int *counter, unsigned m, int lane) {
+  __shared__ int s_tot, s_base;
+  if (threadIdx.x == 0) s_tot = 0;
+  __syncthreads();
+  int off = 0;
+  if (lane == 0 && m) off = atomicAdd(&s_tot, __popc(m));
+  __syncthreads();
+  if (threadIdx.x == 0) s_base = s_tot ? atomicAdd(counter, s_tot) : 0;
+  __syncthreads();
+  return s_base + __shfl_sync(FULL, off, 0);
 }
 
-// append colloid j to cell `cell` of the table of substep e
+// A cell-table entry is (tag << 32) | count with tag = substep + 1: substeps
+// start at -1 (the set-up table), tags at 0, and tags only grow between two
+// invalidations (which zero the tables), so an older entry always has a smaller
+// tag.  Count of the entry if it belongs to substep g:
+static __device__ __forceinline__ int tcount(unsigned long long v, long long g) {
+  return (unsigned)(v >> 32) == (unsigned)(g + 1) ? (int)(unsigned)v : 0;
+}
+
+// append colloid j to cell `cell` of the table of substep e: the maximum turns
+// an entry of an earlier substep into (e, 0) and leaves one of substep e as it
+// is; the add then takes a slot (two atomics on one address from one thread
+// take effect in program order)
 static __device__ __forceinline__ void tappend(unsigned long long *Tc, uint16_t *Tl, int cell, long long e, int j, int *err) {
-  const unsigned long long tag = (unsigned long long)(unsigned)e << 32;
-  unsigned long long old = Tc[cell];
-  for (int it = 0; it < 256; ++it) {
-    unsigned long long nv = ((unsigned)(old >> 32) == (unsigned)e) ? old + 1 : (tag | 1ull);
-    unsigned long long prev = atomicCAS(&Tc[cell], old, nv);
-    if (prev == old) {
-      int slot = (int)(unsigned)nv - 1;
-      if (slot < TCAP) Tl[(size_t)cell * TCAP + slot] = (uint16_t)j;
-      else atomicOr(err, ERRB_TTABLE);
-      return;
-    }
-    old = prev;
-  }
-  atomicOr(err, ERRB_TTABLE);
+  const unsigned long long tag = (unsigned long long)(unsigned)(e + 1) << 32;
+  atomicMax(&Tc[cell], tag);
+  const int slot = (int)(unsigned)atomicAdd(&Tc[cell], 1ull);
+  if (slot < TCAP) Tl[(size_t)cell * TCAP + slot] = (uint16_t)j;
+  else atomicOr(err, ERRB_TTABLE);
 }
 
 // FP32 copy of a double by truncating the mantissa (integer pipe); relative
@@ -309,6 +322,8 @@ static __device__ d3 activity(const SysF64 &S, d3 ra, d3 W, d3 xi) {
 }
 
 static __device__ __forceinline__ float wrapf(float d, float L) { return d - L * rintf(d / L); }
+// the same with a reciprocal of L (for prefilters that carry a margin)
+static __device__ __forceinline__ float wrapf_r(float d, float L, float iL) { return d - L * rintf(d * iL); }
 
 // WCA force on colloid j at positions Xc (compute_force_md, cpp/update.cpp:14-32):
 // partners with r < r_cutoff summed in ascending partner order, which is the
@@ -321,47 +336,59 @@ static __device__ d3 wca_force(const SysF64 &S, const double *Xc, const float4 *
   pot = 0;
   const float4 xj = Xf[j];
   const float Lx = S.Lxf, Ly = S.Lyf, Lz = S.Lzf;
+  const float iLx = __frcp_rn(Lx), iLy = __frcp_rn(Ly), iLz = __frcp_rn(Lz);
   const float rcf = S.rcf;
   const d3 Xj = ldv(Xc, j);
-  for (int base = 0; base < S.Nc; base += 32) {
-    int k = base + lane;
-    bool cand = false;
-    if (k < S.Nc && k != j) {
-      float4 xk = Xf[k];
-      float dx = wrapf(xj.x - xk.x, Lx), dy = wrapf(xj.y - xk.y, Ly), dz = wrapf(xj.z - xk.z, Lz);
-      cand = dx * dx + dy * dy + dz * dz < rcf * rcf;
-    }
-    unsigned m = __ballot_sync(FULL, cand);
-    if (!m) continue;
-    d3 ff = mk(0, 0, 0);
-    double pt = 0;
-    bool hit = false;
-    if (cand) {
-      d3 temp = mk(ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
-                   ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz));
-      double r = __dsqrt_rn(norm2_ref(temp.x, temp.y, temp.z));
-      if (r < S.r_cutoff) {
-        hit = true;
-        double p13 = r, p7 = r;
-        for (int i = 1; i < 13; ++i) { p13 = __dmul_rn(p13, r); if (i == 6) p7 = p13; }
-        double t1 = __ddiv_rn(S.sig12, p13), t2 = __ddiv_rn(S.sig6, p7);
-        double mag = __dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(__dmul_rn(12.0, t1), __dmul_rn(6.0, t2))), S.fc);
-        ff = div3s(mul3s(temp, mag), r);
-        if (want_pot && k > j) {
-          double q = __ddiv_rn(S.sig_colloid, r);
-          pt = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(pow(q, 12.0), pow(q, 6.0))), S.ufc),
-                         __dmul_rn(S.fc, r));
-        }
+  const int nit = (S.Nc + 31) / 32;
+  for (int c0 = 0; c0 < nit; c0 += 32) {
+    const int cend = min(nit, c0 + 32);
+    // FP32 prefilter of up to 1024 partners: independent loads, one bit per pass
+    unsigned mine = 0;
+#pragma unroll 4
+    for (int it = c0; it < cend; ++it) {
+      const int k = it * 32 + lane;
+      if (k < S.Nc && k != j) {
+        const float4 xk = Xf[k];
+        const float dx = wrapf_r(xj.x - xk.x, Lx, iLx), dy = wrapf_r(xj.y - xk.y, Ly, iLy),
+                    dz = wrapf_r(xj.z - xk.z, Lz, iLz);
+        if (dx * dx + dy * dy + dz * dz < rcf * rcf) mine |= 1u << (it - c0);
       }
     }
-    unsigned hm = __ballot_sync(FULL, hit);
-    while (hm) {
-      int src = __ffs(hm) - 1;
-      hm &= hm - 1;
-      double fx = __shfl_sync(FULL, ff.x, src), fy = __shfl_sync(FULL, ff.y, src), fz = __shfl_sync(FULL, ff.z, src);
-      double pp = __shfl_sync(FULL, pt, src);
-      f = add3(f, mk(fx, fy, fz));
-      pot = __dadd_rn(pot, pp);
+    for (int it = c0; it < cend; ++it) {
+      const int k = it * 32 + lane;
+      const bool cand = (mine >> (it - c0)) & 1u;
+      unsigned m = __ballot_sync(FULL, cand);
+      if (!m) continue;
+      d3 ff = mk(0, 0, 0);
+      double pt = 0;
+      bool hit = false;
+      if (cand) {
+        d3 temp = mk(ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
+                     ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz));
+        double r = __dsqrt_rn(norm2_ref(temp.x, temp.y, temp.z));
+        if (r < S.r_cutoff) {
+          hit = true;
+          double p13 = r, p7 = r;
+          for (int i = 1; i < 13; ++i) { p13 = __dmul_rn(p13, r); if (i == 6) p7 = p13; }
+          double t1 = __ddiv_rn(S.sig12, p13), t2 = __ddiv_rn(S.sig6, p7);
+          double mag = __dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(__dmul_rn(12.0, t1), __dmul_rn(6.0, t2))), S.fc);
+          ff = div3s(mul3s(temp, mag), r);
+          if (want_pot && k > j) {
+            double q = __ddiv_rn(S.sig_colloid, r);
+            pt = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(pow(q, 12.0), pow(q, 6.0))), S.ufc),
+                           __dmul_rn(S.fc, r));
+          }
+        }
+      }
+      unsigned hm = __ballot_sync(FULL, hit);
+      while (hm) {
+        int src = __ffs(hm) - 1;
+        hm &= hm - 1;
+        double fx = __shfl_sync(FULL, ff.x, src), fy = __shfl_sync(FULL, ff.y, src), fz = __shfl_sync(FULL, ff.z, src);
+        double pp = __shfl_sync(FULL, pt, src);
+        f = add3(f, mk(fx, fy, fz));
+        pot = __dadd_rn(pot, pp);
+      }
     }
   }
   return f;
@@ -375,6 +402,7 @@ static __device__ void for_reach_cells(const SysF64 &S, int cb, float4 xc, float
   if (cb >= S.C) return;
   int cx = cb % S.Lx, ct = cb / S.Lx, cy = ct % S.Ly, cz = ct / S.Ly;
   const float Lx = S.Lxf, Ly = S.Lyf, Lz = S.Lzf;
+  const float iLx = __frcp_rn(Lx), iLy = __frcp_rn(Ly), iLz = __frcp_rn(Lz);
   for (int q = first; q < 343; q += stride) {
     int ox = q % 7 - 3, oy = (q / 7) % 7 - 3, oz = q / 49 - 3;
     if (!ox && !oy && !oz) continue;
@@ -382,9 +410,9 @@ static __device__ void for_reach_cells(const SysF64 &S, int cb, float4 xc, float
     bx += bx < 0 ? S.Lx : 0; bx -= bx >= S.Lx ? S.Lx : 0;
     by += by < 0 ? S.Ly : 0; by -= by >= S.Ly ? S.Ly : 0;
     bz += bz < 0 ? S.Lz : 0; bz -= bz >= S.Lz ? S.Lz : 0;
-    float ex = fmaxf(fabsf(wrapf(xc.x - ((float)bx + 0.5f), Lx)) - 0.5f, 0.f);
-    float ey = fmaxf(fabsf(wrapf(xc.y - ((float)by + 0.5f), Ly)) - 0.5f, 0.f);
-    float ez = fmaxf(fabsf(wrapf(xc.z - ((float)bz + 0.5f), Lz)) - 0.5f, 0.f);
+    float ex = fmaxf(fabsf(wrapf_r(xc.x - ((float)bx + 0.5f), Lx, iLx)) - 0.5f, 0.f);
+    float ey = fmaxf(fabsf(wrapf_r(xc.y - ((float)by + 0.5f), Ly, iLy)) - 0.5f, 0.f);
+    float ez = fmaxf(fabsf(wrapf_r(xc.z - ((float)bz + 0.5f), Lz, iLz)) - 0.5f, 0.f);
     if (ex * ex + ey * ey + ez * ez <= reach * reach) fn(bx + S.Lx * (by + S.Ly * bz));
   }
 }
@@ -395,46 +423,59 @@ static __device__ __forceinline__ float table_reach(const SysF64 &S, long long e
   return (e % S.n_sub) == S.n_sub - 1 ? S.rT_shell : S.rT_coll;
 }
 
-// Colloid work that the next substep needs and nothing in this substep changes,
-// done by the first blocks of a streaming pass while the rest streams the fluid:
-// the WCA forces at the positions X_g (compute_force_md) and the cell table of
-// substep g+1, built from X_g with a margin for the colloid's own move.  One
-// colloid per 256-thread block, its independent parts on separate warps so that
-// their FP64 latency chains overlap: warp 0 the forces, warp 1 the orientation,
-// warp 2 the rotational-diffusion draws, warps 3-7 the 343 cells of the table.
-static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, int j, bool act) {
+// Colloid work that the next substep needs and nothing in this substep changes
+// (k_aux, on a second stream beside the streaming and event passes of this
+// substep): the WCA forces at the positions X_g (compute_force_md) and the cell
+// table of substep g+1, built from X_g with a margin for the colloid's own move.
+// The colloid has `nw` (2 to 8) warps and `w` is this thread's warp among them:
+// the forces on warp 0, the table on warps 2.. (on warp 0 after the forces when
+// nw = 2); the pending orientation update and this substep's
+// rotational-diffusion draws on warp 1, whose lanes 0-2 take one component each.
+static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, int j, bool act, int w, int nw) {
   const int b = (int)(g & 1);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) {
+  const int lane = threadIdx.x & 31;
+  if (w == 0) {
     double pot;
     d3 fn = wca_force(S, S.X[b], S.Xf[b], j, lane, false, pot);
     if (lane == 0) stv(S.fnew, j, fn);
-    return;
   }
-  // update_activity_direction of the previous substep: nothing before the end of
-  // this step reads the orientation, so it runs here, off the critical path
-  if (warp == 1) {
-    if (act && lane == 0) stv(S.ra, j, activity(S, ldv(S.ra, j), ldv(S.W, j), ldv(S.xi, j)));
-    return;
+  if (w >= 2 || (w == 0 && nw == 2)) {
+    const long long e = g + 1;
+    unsigned long long *Tc = S.Tcnt[e & 1];
+    uint16_t *Tl = S.Tlist[e & 1];
+    int *err = &S.ss->err;
+    const int first = nw == 2 ? lane : (w - 2) * 32 + lane, stride = nw == 2 ? 32 : (nw - 2) * 32;
+    for_reach_cells(S, S.cbox[b][j], S.Xf[b][j], table_reach(S, e), first, stride,
+                    [&](int cell) { tappend(Tc, Tl, cell, e, j, err); });
   }
-  if (warp == 2) {
-    if (S.Dr > 0 && lane == 0) {
-    // the three standard normals of this substep's rotational diffusion (Box-Muller)
+  if (w != 1 || lane >= 3) return;
+  const unsigned grp = 0x7u;
+  const int k = lane;
+  // update_activity_direction of the previous substep (nothing before the end of
+  // this step reads the orientation): lane k takes sin and cos of (Omega dt)_k
+  if (act) {
+    double s, co;
+    sincos(__dmul_rn(S.W[3 * j + k], S.dt), &s, &co);
+    const d3 sb = mk(__shfl_sync(grp, s, 0), __shfl_sync(grp, s, 1), __shfl_sync(grp, s, 2));
+    const d3 cb = mk(__shfl_sync(grp, co, 0), __shfl_sync(grp, co, 1), __shfl_sync(grp, co, 2));
+    const d3 rn = activity_rot(S, ldv(S.ra, j), sb, cb, ldv(S.xi, j));
+    if (k == 0) stv(S.ra, j, rn);
+  }
+  if (S.Dr > 0) {
+    // the three standard normals of this substep's rotational diffusion (Box-Muller):
+    // lane 0 the pair (r0, t0) giving xi_x and xi_y, lane 1 the pair (r1, t1) giving xi_z
+    __syncwarp(grp);
     uint4 r = draw4(S.key, DOM_ROTDIFF, 0, (uint32_t)(j + 1), 0, (uint32_t)g);
-    double r0 = sqrt(-2.0 * log(u01(r.x))), r1 = sqrt(-2.0 * log(u01(r.z)));
-    double s0, c0, s1, c1;
-    sincos(__dmul_rn(S.two_pi, u01(r.y)), &s0, &c0);
-    sincos(__dmul_rn(S.two_pi, u01(r.w)), &s1, &c1);
-    stv(S.xi, j, mk(__dmul_rn(r0, c0), __dmul_rn(r0, s0), __dmul_rn(r1, c1)));
+    const uint32_t ur = k == 0 ? r.x : r.z, ut = k == 0 ? r.y : r.w;
+    double rr = 0, sn = 0, cs = 0;
+    if (k < 2) {
+      rr = sqrt(-2.0 * log(u01(ur)));
+      sincos(__dmul_rn(S.two_pi, u01(ut)), &sn, &cs);
     }
-    return;
+    const double r0 = __shfl_sync(grp, rr, 0), s0 = __shfl_sync(grp, sn, 0), c0 = __shfl_sync(grp, cs, 0);
+    const double r1 = __shfl_sync(grp, rr, 1), c1 = __shfl_sync(grp, cs, 1);
+    if (k == 0) stv(S.xi, j, mk(__dmul_rn(r0, c0), __dmul_rn(r0, s0), __dmul_rn(r1, c1)));
   }
-  const long long e = g + 1;
-  unsigned long long *Tc = S.Tcnt[e & 1];
-  uint16_t *Tl = S.Tlist[e & 1];
-  int *err = &S.ss->err;
-  for_reach_cells(S, S.cbox[b][j], S.Xf[b][j], table_reach(S, e), (int)threadIdx.x - 96, (int)blockDim.x - 96,
-                  [&](int cell) { tappend(Tc, Tl, cell, e, j, err); });
 }
 
 }  // namespace bgb

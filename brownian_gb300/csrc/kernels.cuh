@@ -8,12 +8,13 @@ enum : int { F_STREAM = 1, F_COLLIDE = 2, F_SHELL = 4, F_BINROT = 8 };
 enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8 };
 
 // k_stream<FLAGS> instantiations, by flag set (nullptr for a set not built)
-using StreamKernel = void (*)(const SysF64, int, int, int, int);
+using StreamKernel = void (*)(const SysF64, int, int);
 StreamKernel stream_kernel(int flags);
 using EventKernel = void (*)(const SysF64, int, int);
 EventKernel event_kernel(int flags);
 // FP32-compensated form (kernels_fp32c.cu)
 StreamKernel stream_kernel32(int flags);
+int stream32_per_thread();  // particles per thread of the FP32 streaming pass
 EventKernel event_kernel32(int flags);
 __global__ void k_cell_prep32(const SysF64 S);
 __global__ void k_rotate32(const SysF64 S, int fb);
@@ -29,6 +30,7 @@ __global__ void k_rotate(const SysF64 S, int fb);
 __global__ void k_run_shell(const SysF64 S, int fb);
 __global__ void k_run_kick(const SysF64 S, int fb);
 __global__ void k_fin(const SysF64 S, int mode, int l);
+__global__ void k_aux(const SysF64 S, int l, int act);
 __global__ void k_colloid_setup(const SysF64 S);
 __global__ void k_colloid_pot(const SysF64 S);
 __global__ void k_end_step(const SysF64 S);

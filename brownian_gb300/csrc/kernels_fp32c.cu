@@ -98,103 +98,117 @@ __device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, in
   atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
 }
 
+// STREAM32_U particles per thread (thread t of block b: particles b * 256 U + t +
+// 256 u), their loads issued together so more memory requests are in flight
+#ifndef STREAM32_U
+#define STREAM32_U 2
+#endif
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream32(const SysF64 S, int l, int naux, int act, int fb) {
+__global__ void __launch_bounds__(256) k_stream32(const SysF64 S, int l, int fb) {
   constexpr int flags = FLAGS;
+  constexpr int U = STREAM32_U;
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
-  if ((int)blockIdx.x < naux) {
-    if ((int)blockIdx.x < S.Nc) colloid_aux(S, gs, blockIdx.x, act != 0);
-    return;
-  }
   const Fluid32 F = fluid32_at(S, fb);
-  const int p = (blockIdx.x - naux) * blockDim.x + threadIdx.x;
-  const bool valid = p < S.N;
+  const int p0 = blockIdx.x * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
-  bool ev = false;
-  unsigned members = 0;
-  const uint16_t *lst = nullptr;
-  int cnt = 0;
-  if (valid) {
-    int cx, cy, cz;
-    float ox, oy, oz;
-    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
-    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+  int cx[U], cy[U], cz[U];
+  float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
+  bool valid[U], ev[U];
+  unsigned members[U];
+  int cnt[U], lin[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    valid[u] = p < S.N;
+    ev[u] = false;
+    members[u] = 0;
+    cnt[u] = 0;
+    lin[u] = 0;
+    if (valid[u]) {
+      unpack(F.q[p], cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
+      vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
     if (flags & F_STREAM) {
-      ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
-      carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+      ox[u] = fmaf(vx[u], S.dtf, ox[u]); oy[u] = fmaf(vy[u], S.dtf, oy[u]); oz[u] = fmaf(vz[u], S.dtf, oz[u]);
+      carry(cx[u], ox[u], S.Lx); carry(cy[u], oy[u], S.Ly); carry(cz[u], oz[u], S.Lz);
     }
-    if (flags & (F_COLLIDE | F_SHELL)) {
-      const int lin = cx + S.Lx * (cy + S.Ly * cz);
-      cnt = tcount(S.Tcnt[buf][lin], gs);
-      if (cnt > 0) {
-        cnt = cnt < TCAP ? cnt : TCAP;
-        lst = S.Tlist[buf] + (size_t)lin * TCAP;
-        const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
-        const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
-        for (int k = 0; k < cnt; ++k) {
-          const int j = lst[k];
-          float4 cq = Xq[j], co = Xo[j];
-          float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly), dz = rel(cz, oz, cq.z, co.z, S.Lz);
-          float d2 = dx * dx + dy * dy + dz * dz;
-          if (flags & F_COLLIDE) ev |= d2 <= rc2;
-          if ((flags & F_SHELL) && d2 <= rs2) members |= 1u << k;
-        }
+    lin[u] = cx[u] + S.Lx * (cy[u] + S.Ly * cz[u]);
+    if (flags & (F_COLLIDE | F_SHELL)) cnt[u] = tcount(S.Tcnt[buf][lin[u]], gs);
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
+    if ((flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
+      cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
+      const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+      const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+      const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
+      for (int k = 0; k < cnt[u]; ++k) {
+        const int j = lst[k];
+        const float4 cq = Xq[j], co = Xo[j];
+        const float dx = rel(cx[u], ox[u], cq.x, co.x, S.Lx), dy = rel(cy[u], oy[u], cq.y, co.y, S.Ly),
+                    dz = rel(cz[u], oz[u], cq.z, co.z, S.Lz);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (flags & F_COLLIDE) ev[u] |= d2 <= rc2;
+        if ((flags & F_SHELL) && d2 <= rs2) members[u] |= 1u << k;
       }
     }
-    if (!ev && (flags & F_BINROT)) bin32(S, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
-    if (flags & F_STREAM) F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+    const int p = p0 + 256 * u;
+    if (!ev[u] && (flags & F_BINROT)) bin32(S, p, cx[u], cy[u], cz[u], ox[u], oy[u], oz[u], vx[u], vy[u], vz[u]);
+    if (flags & F_STREAM) F.q[p] = pack(cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
   }
-  // block-aggregated appends: events and (last substep) run() candidate records
-  __shared__ int s_ev, s_rec, s_evb, s_recb;
-  if (threadIdx.x == 0) { s_ev = 0; s_rec = 0; }
-  __syncthreads();
+  // appends: events one atomic per warp (no block barrier), run() candidate
+  // records (last substep) one atomic per block
   const int lane = threadIdx.x & 31;
-  const bool has_rec = (flags & F_SHELL) && !ev && members != 0;
-  const unsigned mev = __ballot_sync(FULL, ev), mrec = __ballot_sync(FULL, has_rec);
-  int oev = 0, orec = 0;
-  if (lane == 0) {
-    if (mev) oev = atomicAdd(&s_ev, __popc(mev));
-    if (mrec) orec = atomicAdd(&s_rec, __popc(mrec));
-  }
-  oev = __shfl_sync(FULL, oev, 0);
-  orec = __shfl_sync(FULL, orec, 0);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_evb = s_ev ? atomicAdd(&S.ss->nevents, s_ev) : 0;
-    s_recb = s_rec ? atomicAdd(&S.ss->nshell, s_rec) : 0;
-  }
-  __syncthreads();
   const unsigned lt = (1u << lane) - 1u;
-  if (ev) {
-    int i = s_evb + oev + __popc(mev & lt);
-    if (i < S.events_cap) S.events[i] = p;
-    else atomicOr(&S.ss->err, ERRB_SHELL);
-  }
-  if (has_rec) {
-    int i = s_recb + orec + __popc(mrec & lt);
-    if (i < S.shell_cap) {
-      ShellRec *r = S.shell + i;
-      r->p = F.id[p];
-      r->pass = 0;
-      int n = 0, last = -1;
-      for (int it = 0; it < cnt && n < SHELL_J; ++it) {
-        int best = 0x7FFFFFFF;
-        for (int k = 0; k < cnt; ++k) {
-          int j = lst[k];
-          if (((members >> k) & 1u) && j > last && j < best) best = j;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    const bool has_rec = (flags & F_SHELL) && valid[u] && !ev[u] && members[u] != 0;
+    const unsigned mev = __ballot_sync(FULL, ev[u]), mrec = __ballot_sync(FULL, has_rec);
+    int bev = 0, brec = 0;
+    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
+    bev = __shfl_sync(FULL, bev, 0);
+    if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
+    if (ev[u]) {
+      const int i = bev + __popc(mev & lt);
+      if (i < S.events_cap) S.events[i] = p;
+      else atomicOr(&S.ss->err, ERRB_SHELL);
+    }
+    if (has_rec) {
+      const int i = brec + __popc(mrec & lt);
+      if (i < S.shell_cap) {
+        // colloids in ascending index, the order run() visits them
+        const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+        ShellRec *r = S.shell + i;
+        r->p = F.id[p];
+        r->pass = 0;
+        int n = 0, last = -1;
+        for (int it = 0; it < cnt[u] && n < SHELL_J; ++it) {
+          int best = 0x7FFFFFFF;
+          for (int k = 0; k < cnt[u]; ++k) {
+            const int j = lst[k];
+            if (((members[u] >> k) & 1u) && j > last && j < best) best = j;
+          }
+          if (best == 0x7FFFFFFF) break;
+          r->j[n++] = (uint16_t)best;
+          last = best;
         }
-        if (best == 0x7FFFFFFF) break;
-        r->j[n++] = (uint16_t)best;
-        last = best;
+        if (__popc(members[u]) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
+        r->n = (uint8_t)n;
+      } else {
+        atomicOr(&S.ss->err, ERRB_SHELL);
       }
-      if (__popc(members) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
-      r->n = (uint8_t)n;
-    } else {
-      atomicOr(&S.ss->err, ERRB_SHELL);
     }
   }
 }
+
+int stream32_per_thread() { return STREAM32_U; }
 
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 fm(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }

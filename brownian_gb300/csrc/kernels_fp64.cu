@@ -47,8 +47,6 @@ __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double 
 
 // FLAGS: F_* bits.  l: substep (1..n_sub) whose streaming this is; 0 for the
 // set-up pass (no streaming; bins for the first step).  fb: the fluid buffer.
-// The first `naux` blocks do colloid_aux for this substep instead (`act`: with
-// the pending orientation update of the previous substep).
 //
 // Per particle: streaming, then an FP32 scan of the colloids its cell table
 // lists.  A particle that may be inside a sphere (or is on the edge of a run()
@@ -56,16 +54,12 @@ __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double 
 // processes with the reference's exact FP64 arithmetic, one event per lane; all
 // other particles finish here (shell record, SRD binning on the last substep).
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int naux, int act, int fb) {
+__global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int fb) {
   constexpr int flags = FLAGS;
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
-  if ((int)blockIdx.x < naux) {
-    if ((int)blockIdx.x < S.Nc) colloid_aux(S, gs, blockIdx.x, act != 0);
-    return;
-  }
   const Fluid F = fluid_at(S, fb);
-  const int p = (blockIdx.x - naux) * blockDim.x + threadIdx.x;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < S.N;
   const int buf = (int)(gs & 1);
   bool ev = false;
@@ -110,34 +104,23 @@ __global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int naux,
     if (!ev && (flags & F_BINROT)) bin_for_rotation(S, p, x, y, z, wx, wy, wz);
     if (flags & F_STREAM) { F.x[p] = x; F.y[p] = y; F.z[p] = z; }
   }
-  // block-aggregated appends: events and (last substep) run() candidate records
-  __shared__ int s_ev, s_rec, s_evb, s_recb;
-  if (threadIdx.x == 0) { s_ev = 0; s_rec = 0; }
-  __syncthreads();
+  // appends: events one atomic per warp (no block barrier), run() candidate
+  // records (last substep) one atomic per block
   const int lane = threadIdx.x & 31;
   const bool has_rec = (flags & F_SHELL) && !ev && members != 0;
   const unsigned mev = __ballot_sync(FULL, ev), mrec = __ballot_sync(FULL, has_rec);
-  int oev = 0, orec = 0;
-  if (lane == 0) {
-    if (mev) oev = atomicAdd(&s_ev, __popc(mev));
-    if (mrec) orec = atomicAdd(&s_rec, __popc(mrec));
-  }
-  oev = __shfl_sync(FULL, oev, 0);
-  orec = __shfl_sync(FULL, orec, 0);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_evb = s_ev ? atomicAdd(&S.ss->nevents, s_ev) : 0;
-    s_recb = s_rec ? atomicAdd(&S.ss->nshell, s_rec) : 0;
-  }
-  __syncthreads();
+  int bev = 0, brec = 0;
+  if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
+  bev = __shfl_sync(FULL, bev, 0);
+  if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
   const unsigned lt = (1u << lane) - 1u;
   if (ev) {
-    int i = s_evb + oev + __popc(mev & lt);
+    int i = bev + __popc(mev & lt);
     if (i < S.events_cap) S.events[i] = p;
     else atomicOr(&S.ss->err, ERRB_SHELL);
   }
   if (has_rec) {
-    int i = s_recb + orec + __popc(mrec & lt);
+    int i = brec + __popc(mrec & lt);
     if (i < S.shell_cap) {
       // colloids in ascending index, the order run() visits them
       ShellRec *r = S.shell + i;
@@ -201,6 +184,14 @@ StreamKernel stream_kernel(int flags) {
     case F_SHELL | F_BINROT: return k_stream<F_SHELL | F_BINROT>;
   }
   return nullptr;
+}
+
+// colloid_aux of substep l (1..n_sub) as a kernel of its own (blocks of
+// S.aux_nw warps, one colloid each); `act`: with the pending orientation update
+// of substep l-1
+__global__ void __launch_bounds__(256) k_aux(const SysF64 S, int l, int act) {
+  const long long gs = S.ss->step * S.n_sub + (l - 1);
+  if ((int)blockIdx.x < S.Nc) colloid_aux(S, gs, blockIdx.x, act != 0, threadIdx.x >> 5, S.aux_nw);
 }
 
 EventKernel event_kernel(int flags) {

@@ -123,6 +123,7 @@ struct SysF64 {
   // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32
   // velocities; both buffers as for the FP64 fluid
   int precision;
+  int aux_nw;  // warps per colloid of the colloid side work (2, 4 or 8)
   uint4 *q[2];
   float *v32[2][3];
   float *cell_ab32;    // [C][12] SRD map in FP32

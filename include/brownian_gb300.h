@@ -140,9 +140,13 @@ int64_t mpcd_launch_count(const mpcd_ctx *c);
 
 /* ---- launch shapes (no counterpart in the reference: tuning of this implementation) -- */
 enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, multiple of 32) */
-       MPCD_LAUNCH_FIN = 1 };  /* colloid finish: grid, block (<= 128, multiple of 32) */
-/* grid <= 0 restores the default (one block per SM); results do not depend on the
- * shape (every sum is exact); drops the captured step graphs */
+       MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32) */
+       MPCD_LAUNCH_AUX = 2 };  /* colloid side work (forces, cell table, orientation; a kernel on a
+                                  second stream beside the streaming and event passes): grid > 0
+                                  sets, block = threads per colloid (64, 128 or 256) */
+/* grid <= 0 restores the default (events and finish: one block per SM; side work:
+ * 128 threads per colloid); results do not depend on the shape (every sum is
+ * exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
 #ifdef __cplusplus
