@@ -24,7 +24,9 @@ INIT_REFERENCE, INIT_PHYSICAL = 0, 1
 EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", "mpcd_set_state", "mpcd_get_state",
            "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
            "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
-           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch"]
+           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
+           "mpcd_fluid_sums_noalloc"]
+NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
 
 
@@ -92,6 +94,7 @@ def lib():
         L.mpcd_launch_count.argtypes = [vp]
         L.mpcd_launch_count.restype = C.c_int64
         L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.mpcd_fluid_sums_noalloc.argtypes = [vp, C.c_int64, C.c_double, vp, vp]
         _lib = L
     return _lib
 

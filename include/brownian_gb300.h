@@ -149,6 +149,23 @@ enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, mu
  * exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
+/* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
+/* For callers that cannot call cudaMalloc: their device memory is all handed out by their
+ * own pool (for example a framework's caching allocator that already holds the GPU), or
+ * they must not take the device synchronisation an allocation can cause mid-pipeline.
+ * Momentum (mass * sum v, three doubles) and kinetic energy (mass/2 * sum |v|^2) of n
+ * particles whose velocities `vel` (device memory, n x 3 doubles, the layout of
+ * mpcd_set_state's vel_fl) the caller owns, written to `out` (device memory, four
+ * doubles), asynchronously on `stream` (NULL: the legacy default stream).  The same sums
+ * as the fluid part of mpcd_diag, with no context.  Its per-block partial sums live in a
+ * fixed 512 KiB array of the library that every GPU loading it holds until exit; nothing
+ * is allocated.  The first call on a device looks up that array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race.  Returns MPCD_ERR_CAPACITY, with a message on
+ * stderr, for n > MPCD_NOALLOC_MAX_PARTICLES. */
+#define MPCD_NOALLOC_MAX_PARTICLES 33554432LL
+int mpcd_fluid_sums_noalloc(const double *vel, int64_t n, double mass, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
