@@ -25,7 +25,9 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
            "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
-           "mpcd_fluid_sums_noalloc"]
+           "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
+           "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count"]
+ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
 
@@ -95,6 +97,16 @@ def lib():
         L.mpcd_launch_count.restype = C.c_int64
         L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.mpcd_fluid_sums_noalloc.argtypes = [vp, C.c_int64, C.c_double, vp, vp]
+        L.mpcd_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
+        L.mpcd_ensemble_destroy.argtypes = [vp]
+        L.mpcd_ensemble_last_error.argtypes = [vp]
+        L.mpcd_ensemble_last_error.restype = C.c_char_p
+        L.mpcd_ensemble_system.argtypes = [vp, C.c_int]
+        L.mpcd_ensemble_system.restype = vp
+        L.mpcd_ensemble_step.argtypes = [vp, C.c_int]
+        L.mpcd_ensemble_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.mpcd_ensemble_launch_count.argtypes = [vp]
+        L.mpcd_ensemble_launch_count.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -117,27 +129,43 @@ def displaced_mass(radius, density, mass_fl=1.0):
     return density * mass_fl * 4.0 / 3.0 * np.pi * radius ** 3
 
 
+def make_params(L, n_fluid, n_colloid, *, n_sub=10, kbt=1.0, kbt1=1.0, ndt=0.1, mass_fl=1.0, mass_colloid=654.1,
+                sig_colloid=5.0, eps=1.0, sigma=None, I_colloid=None, v0=0.0, theta_deg=130.0, Dr=0.0, seed=77777,
+                precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5, sort_every=0):
+    """mpcd_params of one system (defaults: the reference's, cpp/active_brownian.cpp:3-7)."""
+    Lx, Ly, Lz = (L, L, L) if np.isscalar(L) else L
+    sigma = 0.8 * sig_colloid if sigma is None else sigma          # cpp/active_brownian.cpp:7
+    I_colloid = 0.1 * mass_colloid * sigma * sigma if I_colloid is None else I_colloid
+    return Params(Lx, Ly, Lz, n_fluid, n_colloid, n_sub, kbt, kbt1, ndt, mass_fl, mass_colloid, sig_colloid, eps,
+                  sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell, vmax, init_gap, sort_every)
+
+
 class Simulation:
     """One MPCD + active-colloid system resident on the GPU."""
 
-    def __init__(self, L, n_fluid, n_colloid, *, n_sub=10, kbt=1.0, kbt1=1.0, ndt=0.1, mass_fl=1.0,
-                 mass_colloid=654.1, sig_colloid=5.0, eps=1.0, sigma=None, I_colloid=None, v0=0.0,
-                 theta_deg=130.0, Dr=0.0, seed=77777, precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5,
-                 sort_every=0):
-        Lx, Ly, Lz = (L, L, L) if np.isscalar(L) else L
-        sigma = 0.8 * sig_colloid if sigma is None else sigma          # cpp/active_brownian.cpp:7
-        I_colloid = 0.1 * mass_colloid * sigma * sigma if I_colloid is None else I_colloid
-        self.params = Params(Lx, Ly, Lz, n_fluid, n_colloid, n_sub, kbt, kbt1, ndt, mass_fl, mass_colloid,
-                             sig_colloid, eps, sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell,
-                             vmax, init_gap, sort_every)
-        self.N, self.Nc = n_fluid, n_colloid
-        self.C = Lx * Ly * Lz
-        self.dt = ndt / n_sub
+    def __init__(self, L, n_fluid, n_colloid, **kw):
+        self._adopt(make_params(L, n_fluid, n_colloid, **kw))
         h = C.c_void_p()
         r = lib().mpcd_create(C.byref(self.params), C.byref(h))
         if r:
             raise MPCDError(r, "mpcd_create rejected the parameters or could not allocate")
         self.h = h
+        self._owned = True
+
+    def _adopt(self, params):
+        self.params = params
+        self.N, self.Nc = params.n_fluid, params.n_colloid
+        self.C = params.Lx * params.Ly * params.Lz
+        self.dt = params.ndt / params.n_sub
+
+    @classmethod
+    def _view(cls, handle, params):
+        """A system owned by something else (an ensemble); closing the view frees nothing."""
+        s = cls.__new__(cls)
+        s._adopt(params)
+        s.h = C.c_void_p(handle)
+        s._owned = False
+        return s
 
     # ---------------------------------------------------------------- plumbing
     def _ck(self, r):
@@ -146,7 +174,8 @@ class Simulation:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().mpcd_destroy(self.h)
+            if getattr(self, "_owned", True):
+                lib().mpcd_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -251,6 +280,55 @@ class Simulation:
     @property
     def launch_count(self):
         return lib().mpcd_launch_count(self.h)
+
+
+class Ensemble:
+    """Many independent FP32-compensated systems stepped together, one launch per
+    stage over all of them (mpcd_ensemble_*).  `params` is a list of Params
+    (make_params(..., precision=FP32C)); ens[r] is system r as a Simulation view."""
+
+    def __init__(self, params):
+        self.params = list(params)
+        arr = (Params * len(self.params))(*self.params)
+        h = C.c_void_p()
+        r = lib().mpcd_ensemble_create(arr, len(self.params), C.byref(h))
+        if r:
+            raise MPCDError(r, "mpcd_ensemble_create rejected the parameters or could not allocate")
+        self.h = h
+        self.systems = [Simulation._view(lib().mpcd_ensemble_system(self.h, i), p) for i, p in enumerate(self.params)]
+
+    def _ck(self, r):
+        if r:
+            raise MPCDError(r, lib().mpcd_ensemble_last_error(self.h).decode())
+
+    def __len__(self):
+        return len(self.systems)
+
+    def __getitem__(self, i):
+        return self.systems[i]
+
+    def step(self, nsteps=1):
+        self._ck(lib().mpcd_ensemble_step(self.h, nsteps))
+
+    def set_launch(self, which, per_system=1, block=32):
+        self._ck(lib().mpcd_ensemble_set_launch(self.h, which, per_system, block))
+
+    @property
+    def launch_count(self):
+        return lib().mpcd_ensemble_launch_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for s in self.systems:
+                s.h = None
+            lib().mpcd_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def active_brownian(sim, nsteps, style=INIT_REFERENCE, diag_every=1):

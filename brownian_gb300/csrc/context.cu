@@ -906,3 +906,5 @@ extern "C" int64_t mpcd_launch_count(const mpcd_ctx *c) { return c ? c->launches
 
 // initialisation lives in init.cu; it needs the context internals
 #include "init_host.inc"
+
+#include "ensemble.inc"

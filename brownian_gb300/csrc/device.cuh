@@ -61,6 +61,33 @@ static __device__ __forceinline__ int block_base(int *counter, unsigned m, int l
   return s_base + __shfl_sync(FULL, off, 0);
 }
 
+// Batched launches: block b of a launch over nrep systems belongs to the system r
+// with boff[r] <= b < boff[r+1] (boff ascending, boff[nrep] = the grid) and is
+// that system's virtual block b - boff[r] of boff[r+1] - boff[r]; its SysF64 is
+// copied into shared memory once per block.
+static __device__ __forceinline__ void batch_locate(const SysF64 *Ss, const int *boff, int nrep, SysF64 &sS, int &vb,
+                                                    int &nvb) {
+  __shared__ int s_r;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nrep;
+    const int b = blockIdx.x;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (boff[mid] <= b) lo = mid;
+      else hi = mid;
+    }
+    s_r = lo;
+  }
+  __syncthreads();
+  const int r = s_r;
+  const int *src = reinterpret_cast<const int *>(Ss + r);
+  int *dst = reinterpret_cast<int *>(&sS);
+  for (int k = threadIdx.x; k < (int)(sizeof(SysF64) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  vb = (int)blockIdx.x - boff[r];
+  nvb = boff[r + 1] - boff[r];
+}
+
 // A cell-table entry is (tag << 32) | count with tag = substep + 1: substeps
 // start at -1 (the set-up table), tags at 0, and tags only grow between two
 // invalidations (which zero the tables), so an older entry always has a smaller

@@ -12,28 +12,43 @@ using StreamKernel = void (*)(const SysF64, int, int);
 StreamKernel stream_kernel(int flags);
 using EventKernel = void (*)(const SysF64, int, int);
 EventKernel event_kernel(int flags);
+// batched forms over an array of systems (block offsets per system in boff)
+using StreamKernelB = void (*)(const SysF64 *, const int *, int, int, int);
+using EventKernelB = void (*)(const SysF64 *, const int *, int, int, int);
+StreamKernelB stream_kernel32_b(int flags);
+EventKernelB event_kernel32_b(int flags);
+__global__ void k_cell_prep32_b(const SysF64 *Ss, const int *boff, int nrep);
+__global__ void k_rotate32_b(const SysF64 *Ss, const int *boff, int nrep, int fb);
+__global__ void k_rotate_sort32_b(const SysF64 *Ss, const int *boff, int nrep, int src, int dst);
+__global__ void k_run_shell32_b(const SysF64 *Ss, const int *boff, int nrep, int fb);
+__global__ void k_run_kick32_b(const SysF64 *Ss, const int *boff, int nrep, int fb);
+__global__ void k_aux_b(const SysF64 *Ss, const int *boff, int nrep, int l, int act);
+__global__ void k_fin_b(const SysF64 *Ss, const int *boff, int nrep, int mode, int l);
+__global__ void k_end_step_b(const SysF64 *Ss, const int *boff, int nrep);
+__global__ void k_scan_blocks_b(const SysF64 *Ss, const int *boff, int nrep, int nblk);
+__global__ void k_gather_err(const SysF64 *Ss, int nrep, int *out);
 // FP32-compensated form (kernels_fp32c.cu)
 StreamKernel stream_kernel32(int flags);
 int stream32_per_thread();  // particles per thread of the FP32 streaming pass
 EventKernel event_kernel32(int flags);
-__global__ void k_cell_prep32(const SysF64 S);
-__global__ void k_rotate32(const SysF64 S, int fb);
-__global__ void k_rotate_sort32(const SysF64 S, int src, int dst);
-__global__ void k_run_shell32(const SysF64 S, int fb);
-__global__ void k_run_kick32(const SysF64 S, int fb);
+__global__ void k_cell_prep32(__grid_constant__ const SysF64 S);
+__global__ void k_rotate32(__grid_constant__ const SysF64 S, int fb);
+__global__ void k_rotate_sort32(__grid_constant__ const SysF64 S, int src, int dst);
+__global__ void k_run_shell32(__grid_constant__ const SysF64 S, int fb);
+__global__ void k_run_kick32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_aos_to_q(const SysF64 S, const double *pos, const double *vel, int fb);
 __global__ void k_q_to_aos(const SysF64 S, double *pos, double *vel, int fb);
 __global__ void k_cell_prep(const SysF64 S);
-__global__ void k_scan_blocks(const SysF64 S, int nblk);
+__global__ void k_scan_blocks(__grid_constant__ const SysF64 S, int nblk);
 __global__ void k_rotate_sort(const SysF64 S, int src, int dst);
 __global__ void k_rotate(const SysF64 S, int fb);
 __global__ void k_run_shell(const SysF64 S, int fb);
 __global__ void k_run_kick(const SysF64 S, int fb);
-__global__ void k_fin(const SysF64 S, int mode, int l);
-__global__ void k_aux(const SysF64 S, int l, int act);
+__global__ void k_fin(__grid_constant__ const SysF64 S, int mode, int l);
+__global__ void k_aux(__grid_constant__ const SysF64 S, int l, int act);
 __global__ void k_colloid_setup(const SysF64 S);
 __global__ void k_colloid_pot(const SysF64 S);
-__global__ void k_end_step(const SysF64 S);
+__global__ void k_end_step(__grid_constant__ const SysF64 S);
 __global__ void k_diag_fluid(const SysF64 S, double *part);
 
 // initialisation

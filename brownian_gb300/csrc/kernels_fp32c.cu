@@ -104,13 +104,13 @@ __device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, in
 #define STREAM32_U 2
 #endif
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream32(const SysF64 S, int l, int fb) {
+static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
   constexpr int flags = FLAGS;
   constexpr int U = STREAM32_U;
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const Fluid32 F = fluid32_at(S, fb);
-  const int p0 = blockIdx.x * (256 * U) + threadIdx.x;
+  const int p0 = VB * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
   int cx[U], cy[U], cz[U];
   float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
@@ -208,6 +208,20 @@ __global__ void __launch_bounds__(256) k_stream32(const SysF64 S, int l, int fb)
   }
 }
 
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32(__grid_constant__ const SysF64 S, int l, int fb) {
+  k_stream32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_stream32_body<FLAGS>(sS, VB, NVB, l, fb);
+}
+
 int stream32_per_thread() { return STREAM32_U; }
 
 struct f3 { float x, y, z; };
@@ -251,7 +265,7 @@ __device__ f3 reflect32(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, f3 
 // wall collisions of the listed particles in colloid order, then (last substep)
 // their run() record and binning; one particle per lane
 template <int FLAGS>
-__global__ void __launch_bounds__(128) k_events32(const SysF64 S, int l, int fb) {
+static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
   constexpr int flags = FLAGS;
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
@@ -260,9 +274,9 @@ __global__ void __launch_bounds__(128) k_events32(const SysF64 S, int l, int fb)
   const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
   const int n = min(S.ss->nevents, S.events_cap);
   const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
-  // event i goes to block i % gridDim.x: the few hundred to few thousand events of
+  // event i goes to block i % NVB: the few hundred to few thousand events of
   // a substep spread over all SMs instead of filling the first few
-  for (int i = blockIdx.x + gridDim.x * threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = VB + NVB * threadIdx.x; i < n; i += NVB * blockDim.x) {
     const int p = S.events[i];
     int cx, cy, cz;
     float ox, oy, oz;
@@ -335,6 +349,20 @@ __global__ void __launch_bounds__(128) k_events32(const SysF64 S, int l, int fb)
   }
 }
 
+template <int FLAGS>
+__global__ void __launch_bounds__(128) k_events32(__grid_constant__ const SysF64 S, int l, int fb) {
+  k_events32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+template <int FLAGS>
+__global__ void __launch_bounds__(128) k_events32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_events32_body<FLAGS>(sS, VB, NVB, l, fb);
+}
+
 StreamKernel stream_kernel32(int flags) {
   switch (flags) {
     case F_STREAM | F_COLLIDE: return k_stream32<F_STREAM | F_COLLIDE>;
@@ -353,11 +381,29 @@ EventKernel event_kernel32(int flags) {
   return nullptr;
 }
 
+StreamKernelB stream_kernel32_b(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_stream32_b<F_STREAM | F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream32_b<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_SHELL | F_BINROT: return k_stream32_b<F_SHELL | F_BINROT>;
+  }
+  return nullptr;
+}
+
+EventKernelB event_kernel32_b(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_events32_b<F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_events32_b<F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_SHELL | F_BINROT: return k_events32_b<F_SHELL | F_BINROT>;
+  }
+  return nullptr;
+}
+
 // SRD collision per cell (cpp/rotation_mpcd.cpp:14-49): cell mean from the exact
 // sums, thermostat factor in FP64, rotation about the random axis in FP32, stored
 // as the FP32 affine map v' = A v + b; plus the occupancy prefix of the counting sort.
-__global__ void __launch_bounds__(256) k_cell_prep32(const SysF64 S) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const int VB, const int NVB) {
+  const int c = VB * blockDim.x + threadIdx.x;
   if (c < S.Nc) S.shell_cnt[c] = 0;
   CellAcc a = CellAcc{0, 0, 0, 0, 0, 0};
   if (c < S.Cpad) {
@@ -381,7 +427,7 @@ __global__ void __launch_bounds__(256) k_cell_prep32(const SysF64 S) {
       total += wsum[q];
     }
     if (c < S.Cpad) S.cell_off[c] = before + incl - v;
-    if (threadIdx.x == 0) S.blk_off[blockIdx.x] = total;
+    if (threadIdx.x == 0) S.blk_off[VB] = total;
   }
   if (c >= S.C) return;
   float *ab = S.cell_ab32 + (size_t)c * 12;
@@ -418,6 +464,18 @@ __global__ void __launch_bounds__(256) k_cell_prep32(const SysF64 S) {
   ab[11] = fz - (ab[6] * fx + ab[7] * fy + ab[8] * fz);
 }
 
+__global__ void __launch_bounds__(256) k_cell_prep32(__grid_constant__ const SysF64 S) {
+  k_cell_prep32_body(S, blockIdx.x, gridDim.x);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(256) k_cell_prep32_b(const SysF64 *Ss, const int *boff, int nrep) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_cell_prep32_body(sS, VB, NVB);
+}
+
 __device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &vy, float &vz) {
   const float4 *m = reinterpret_cast<const float4 *>(ab);
   float4 a = m[0], b = m[1], c = m[2];
@@ -427,8 +485,8 @@ __device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &v
   vx = nx; vy = ny; vz = nz;
 }
 
-__global__ void __launch_bounds__(256) k_rotate32(const SysF64 S, int fb) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+static __device__ __forceinline__ void k_rotate32_body(const SysF64 &S, const int VB, const int NVB, int fb) {
+  const int p = VB * blockDim.x + threadIdx.x;
   if (p >= S.N) return;
   const int c = S.rotcell[p];
   if (c >= S.C) return;
@@ -438,8 +496,20 @@ __global__ void __launch_bounds__(256) k_rotate32(const SysF64 S, int fb) {
   F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
 }
 
-__global__ void __launch_bounds__(256) k_rotate_sort32(const SysF64 S, int src, int dst) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_rotate32(__grid_constant__ const SysF64 S, int fb) {
+  k_rotate32_body(S, blockIdx.x, gridDim.x, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(256) k_rotate32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_rotate32_body(sS, VB, NVB, fb);
+}
+
+static __device__ __forceinline__ void k_rotate_sort32_body(const SysF64 &S, const int VB, const int NVB, int src, int dst) {
+  const int p = VB * blockDim.x + threadIdx.x;
   if (p >= S.N) return;
   const Fluid32 F = fluid32_at(S, src), G = fluid32_at(S, dst);
   const int c = S.rotcell[p];
@@ -463,13 +533,25 @@ __global__ void __launch_bounds__(256) k_rotate_sort32(const SysF64 S, int src, 
   S.newpos[id] = slot;
 }
 
+__global__ void __launch_bounds__(256) k_rotate_sort32(__grid_constant__ const SysF64 S, int src, int dst) {
+  k_rotate_sort32_body(S, blockIdx.x, gridDim.x, src, dst);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(256) k_rotate_sort32_b(const SysF64 *Ss, const int *boff, int nrep, int src, int dst) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_rotate_sort32_body(sS, VB, NVB, src, dst);
+}
+
 // run() (cpp/run.cpp:17-24) on the FP32 fluid: rear-shell test against V + v0 ra
-__global__ void k_run_shell32(const SysF64 S, int fb) {
+static __device__ __forceinline__ void k_run_shell32_body(const SysF64 &S, const int VB, const int NVB, int fb) {
   const int n = min(S.ss->nshell, S.shell_cap);
   const int b = (int)((S.ss->step * S.n_sub - 1) & 1);
   const float4 *Xq = S.Xcq[b], *Xo = S.Xco[b];
   const Fluid32 F = fluid32_at(S, fb);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = VB * blockDim.x + threadIdx.x; i < n; i += NVB * blockDim.x) {
     ShellRec rec = S.shell[i];
     int p = S.newpos[rec.p];
     int cx, cy, cz;
@@ -491,10 +573,22 @@ __global__ void k_run_shell32(const SysF64 S, int fb) {
   }
 }
 
-__global__ void k_run_kick32(const SysF64 S, int fb) {
+__global__ void k_run_shell32(__grid_constant__ const SysF64 S, int fb) {
+  k_run_shell32_body(S, blockIdx.x, gridDim.x, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void k_run_shell32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_run_shell32_body(sS, VB, NVB, fb);
+}
+
+static __device__ __forceinline__ void k_run_kick32_body(const SysF64 &S, const int VB, const int NVB, int fb) {
   const int n = min(S.ss->nshell, S.shell_cap);
   const Fluid32 F = fluid32_at(S, fb);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = VB * blockDim.x + threadIdx.x; i < n; i += NVB * blockDim.x) {
     ShellRec rec = S.shell[i];
     if (!rec.pass) continue;
     int p = S.newpos[rec.p];
@@ -507,6 +601,18 @@ __global__ void k_run_kick32(const SysF64 S, int fb) {
     }
     F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
   }
+}
+
+__global__ void k_run_kick32(__grid_constant__ const SysF64 S, int fb) {
+  k_run_kick32_body(S, blockIdx.x, gridDim.x, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void k_run_kick32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_run_kick32_body(sS, VB, NVB, fb);
 }
 
 // AoS doubles (particle order) -> FP32 records; download scatters back by id

@@ -189,9 +189,21 @@ StreamKernel stream_kernel(int flags) {
 // colloid_aux of substep l (1..n_sub) as a kernel of its own (blocks of
 // S.aux_nw warps, one colloid each); `act`: with the pending orientation update
 // of substep l-1
-__global__ void __launch_bounds__(256) k_aux(const SysF64 S, int l, int act) {
+static __device__ __forceinline__ void k_aux_body(const SysF64 &S, const int VB, const int NVB, int l, int act) {
   const long long gs = S.ss->step * S.n_sub + (l - 1);
-  if ((int)blockIdx.x < S.Nc) colloid_aux(S, gs, blockIdx.x, act != 0, threadIdx.x >> 5, S.aux_nw);
+  if ((int)VB < S.Nc) colloid_aux(S, gs, VB, act != 0, threadIdx.x >> 5, S.aux_nw);
+}
+
+__global__ void __launch_bounds__(256) k_aux(__grid_constant__ const SysF64 S, int l, int act) {
+  k_aux_body(S, blockIdx.x, gridDim.x, l, act);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(256) k_aux_b(const SysF64 *Ss, const int *boff, int nrep, int l, int act) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_aux_body(sS, VB, NVB, l, act);
 }
 
 EventKernel event_kernel(int flags) {
@@ -274,7 +286,7 @@ __global__ void __launch_bounds__(256) k_cell_prep(const SysF64 S) {
 }
 
 // counting sort, second half: exclusive prefix of the block totals (one block)
-__global__ void __launch_bounds__(1024) k_scan_blocks(const SysF64 S, int nblk) {
+static __device__ __forceinline__ void k_scan_blocks_body(const SysF64 &S, const int VB, const int NVB, int nblk) {
   __shared__ int wsum[32];
   __shared__ int carry;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -299,6 +311,18 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const SysF64 S, int nblk) 
     if (threadIdx.x == 0) carry += total;
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(__grid_constant__ const SysF64 S, int nblk) {
+  k_scan_blocks_body(S, blockIdx.x, gridDim.x, nblk);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(1024) k_scan_blocks_b(const SysF64 *Ss, const int *boff, int nrep, int nblk) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_scan_blocks_body(sS, VB, NVB, (sS.Cpad + 255) / 256);  // each system's own block count
 }
 
 // The SRD collision applied to each particle, w' = A w + b of its cell, and the
@@ -447,9 +471,9 @@ __device__ __forceinline__ void set_shift(const SysF64 &S, long long nn) {
 // the following substep (update_pos_md, cpp/update.cpp:48-54).  In the fused step
 // the orientation update of substeps 1..n-1 runs in the next streaming pass
 // instead (colloid_aux), off the critical path.
-__global__ void __launch_bounds__(128) k_fin(const SysF64 S, int mode, int l) {
+static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB, const int NVB, int mode, int l) {
   const int lane = threadIdx.x & 31;
-  const int j = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+  const int j = VB + NVB * (threadIdx.x >> 5);
   const long long step = S.ss->step;
   const long long g = step * S.n_sub + (l - 1);  // substep finished (l >= 1)
   const long long gn = g + 1;                    // substep advanced to
@@ -525,6 +549,18 @@ __global__ void __launch_bounds__(128) k_fin(const SysF64 S, int mode, int l) {
   S.ra[3 * j + k] = ra;
 }
 
+__global__ void __launch_bounds__(128) k_fin(__grid_constant__ const SysF64 S, int mode, int l) {
+  k_fin_body(S, blockIdx.x, gridDim.x, mode, l);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void __launch_bounds__(128) k_fin_b(const SysF64 *Ss, const int *boff, int nrep, int mode, int l) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_fin_body(sS, VB, NVB, mode, l);
+}
+
 // Set-up (the prologue of main, cpp/active_brownian.cpp:93-96): forces at the
 // current positions (compute_force_md), the cell table for the run() candidates
 // of the first step (substep g0-1) and the table of the first substep g0.
@@ -567,8 +603,20 @@ __global__ void __launch_bounds__(128) k_colloid_pot(const SysF64 S) {
 }
 
 // completes a step: bumps the step counter
-__global__ void k_end_step(const SysF64 S) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) S.ss->step += 1;
+static __device__ __forceinline__ void k_end_step_body(const SysF64 &S, const int VB, const int NVB) {
+  if (threadIdx.x == 0 && VB == 0) S.ss->step += 1;
+}
+
+__global__ void k_end_step(__grid_constant__ const SysF64 S) {
+  k_end_step_body(S, blockIdx.x, gridDim.x);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+__global__ void k_end_step_b(const SysF64 *Ss, const int *boff, int nrep) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_end_step_body(sS, VB, NVB);
 }
 
 // fluid diagnostics from the exact cell sums of the last binning: per block the
@@ -590,6 +638,12 @@ __global__ void __launch_bounds__(256) k_diag_fluid(const SysF64 S, double *part
   }
   if (threadIdx.x == 0)
     for (int k = 0; k < 5; ++k) part[blockIdx.x * 5 + k] = sh[k][0];
+}
+
+// error bits of every system of a batch, for one read-back
+__global__ void k_gather_err(const SysF64 *Ss, int nrep, int *out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrep) out[r] = Ss[r].ss->err;
 }
 
 }  // namespace bgb

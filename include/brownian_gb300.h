@@ -149,6 +149,29 @@ enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, mu
  * exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
+/* ---- batched ensemble (no counterpart in the reference) ------------------------------- */
+/* nrep independent systems with their own parameters p[0..nrep-1] (box, fluid, colloids,
+ * activity, seed; all MPCD_FP32C with equal n_sub and sort_every) stepped together: every
+ * stage of an MPCD step is one launch over all systems, the step one CUDA graph.  Each
+ * system is an ordinary context (mpcd_ensemble_system): initialise or set its state, call
+ * mpcd_setup and read it back through the single-system calls; step it only through
+ * mpcd_ensemble_step.  The ensemble owns the contexts. */
+typedef struct mpcd_ensemble mpcd_ensemble;
+int mpcd_ensemble_create(const mpcd_params *p, int nrep, mpcd_ensemble **out);
+int mpcd_ensemble_destroy(mpcd_ensemble *e);
+const char *mpcd_ensemble_last_error(const mpcd_ensemble *e);
+mpcd_ctx *mpcd_ensemble_system(mpcd_ensemble *e, int r);
+/* nsteps MPCD steps of every system (all set up, at the same step); synchronises */
+int mpcd_ensemble_step(mpcd_ensemble *e, int nsteps);
+enum { MPCD_ENS_EVENTS = 0,  /* blocks per system of the event pass (1..64) */
+       MPCD_ENS_RUN = 1,     /* blocks per system of run() (1..64) */
+       MPCD_ENS_FIN = 2,     /* threads per block of the colloid finish (32, 64, 128) */
+       MPCD_ENS_AUX = 3 };   /* threads per colloid of the colloid side work (64, 128, 256) */
+/* launch shapes of the batched step (the autotuner's knobs); results do not depend on them */
+int mpcd_ensemble_set_launch(mpcd_ensemble *e, int which, int per_system, int block);
+/* kernels the ensemble launched since creation */
+int64_t mpcd_ensemble_launch_count(const mpcd_ensemble *e);
+
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their
  * own pool (for example a framework's caching allocator that already holds the GPU), or
