@@ -304,6 +304,72 @@ def form_statistics(steps, lag):
             "momentum_drift_rel_fp32c": b["momentum_drift_rel"]}
 
 
+def ensemble_params(nrep, seed=0):
+    """The batched-ensemble workload: box sizes uniform over {16, 24, 32, 40, 48}^3, fluid
+    density 10, colloid count uniform in [5, 200] capped at 10 % volume fraction, radius 2,
+    v0 uniform in [0, 0.1], Dr = 0.001, distinct seeds, FP32-compensated form."""
+    import numpy as np
+
+    import brownian_gb300 as bg
+    rng = np.random.default_rng(seed)
+    out = []
+    M = bg.displaced_mass(RADIUS, DENSITY)
+    for i in range(nrep):
+        Lr = int(rng.choice([16, 24, 32, 40, 48]))
+        cap = int(0.1 * Lr ** 3 / (4.0 / 3.0 * np.pi * RADIUS ** 3))
+        nc = int(min(rng.integers(5, 201), cap))
+        out.append(bg.make_params(Lr, Lr ** 3 * DENSITY, nc, n_sub=10, mass_colloid=M, sig_colloid=2 * RADIUS,
+                                  sigma=2 * RADIUS, I_colloid=0.4 * M * RADIUS ** 2, v0=float(rng.uniform(0, 0.1)),
+                                  theta_deg=90.0, Dr=0.001, seed=1000 * (seed + 1) + i, precision=bg.FP32C))
+    return out
+
+
+def run_ensemble(nrep, steps, rank):
+    """Replica-steps/s of the batched ensemble (autotuned launch shapes) against looping
+    the single-system step over the same replicas."""
+    import torch
+
+    import brownian_gb300 as bg
+    from brownian_gb300.tune import autotune
+    P = ensemble_params(nrep, seed=rank)
+    ens = bg.Ensemble(P)
+    for s in ens:
+        s.initialize(bg.INIT_PHYSICAL)
+        s.setup()
+    tuned = autotune(ens, steps=2)
+    ens.step(2)
+    t0 = time.perf_counter()
+    ens.step(steps)
+    batched_s = time.perf_counter() - t0
+    launches_per_step = None
+    l0 = ens.launch_count
+    ens.step(1)
+    launches_per_step = ens.launch_count - l0 - 1  # minus the error read-back
+    # the same replicas, each stepped by its own single-system call, one after the other
+    st = torch.cuda.Stream()
+    for s in ens:
+        s.set_stream(st.cuda_stream)
+        s.step(1)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in ens:
+            s.step(1)
+    looped_s = time.perf_counter() - t0
+    n_particles = sum(p.n_fluid for p in P)
+    ens.close()
+    return {"workload": "256 replicas" if nrep == 256 else f"{nrep} replicas",
+            "replicas": nrep, "fluid_particles": n_particles, "steps": steps,
+            "value": nrep * steps / batched_s, "unit": "replica-steps/s",
+            "particle_steps_per_s": n_particles * steps / batched_s,
+            "looped": {"value": nrep * steps / looped_s, "unit": "replica-steps/s",
+                       "how": "mpcd_step(1) of each replica in turn on one stream (each call synchronises)"},
+            "speedup_vs_looped": looped_s / batched_s,
+            "launches_per_step": launches_per_step,
+            "autotune": {"choice": tuned["choice"], "ms_per_step": tuned["ms_per_step"],
+                         "trials": len(tuned["log"])},
+            "timing": "wall clock around mpcd_ensemble_step(K) (it ends with a device synchronisation)"}
+
+
 def run_ours(args, rank, world, dist):
     import torch
 
@@ -348,6 +414,7 @@ def run_ours(args, rank, world, dist):
     d = sim.diag()
     sim.close()
     stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
+    ens = run_ensemble(args.ensemble, args.ensemble_steps, rank) if args.ensemble > 0 else None
 
     if rank != 0:
         return None
@@ -374,6 +441,8 @@ def run_ours(args, rank, world, dist):
                                 "kernel_share": o["shares"], "gpu_launches": o["gpu_launches"]}
     if stats:
         line["fp32c_vs_fp64"] = stats
+    if ens:
+        line["ensemble"] = ens
     return line
 
 
@@ -387,6 +456,8 @@ def main():
     ap.add_argument("--both", type=int, default=1, help="also time the other precision form (sub-object)")
     ap.add_argument("--stat-steps", type=int, default=200,
                     help="steps of the FP32c-vs-FP64 statistics run (MSD at lag 100; <=100: skip)")
+    ap.add_argument("--ensemble", type=int, default=256, help="replicas of the batched-ensemble sub-object (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
     args = ap.parse_args()
