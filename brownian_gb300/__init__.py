@@ -26,7 +26,10 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
-           "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count"]
+           "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
+           "mpcd_exchange_read", "mpcd_mlp_create", "mpcd_mlp_destroy", "mpcd_mlp_last_error", "mpcd_mlp_param_count",
+           "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
+           "mpcd_mlp_grad", "mpcd_mlp_train_step"]
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
@@ -97,6 +100,7 @@ def lib():
         L.mpcd_launch_count.restype = C.c_int64
         L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.mpcd_fluid_sums_noalloc.argtypes = [vp, C.c_int64, C.c_double, vp, vp]
+        L.mpcd_exchange_read.argtypes = [vp, dp, C.c_int]
         L.mpcd_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
         L.mpcd_ensemble_destroy.argtypes = [vp]
         L.mpcd_ensemble_last_error.argtypes = [vp]
@@ -205,6 +209,12 @@ class Simulation:
         out.update({k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra", "f")})
         self._ck(lib().mpcd_get_state(self.h, *[_dp(out[k]) for k in ("pos_fl", "vel_fl", "pos_colloid",
                                                                       "vel_colloid", "ang_vel_colloid", "ra", "f")]))
+        return out
+
+    def exchange(self, reset=True):
+        """(Nc, 6): momentum and angular momentum the fluid gave each colloid since the last reset."""
+        out = np.empty((self.Nc, 6))
+        self._ck(lib().mpcd_exchange_read(self.h, _dp(out), 1 if reset else 0))
         return out
 
     def get_colloids(self):

@@ -408,6 +408,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.fnew = m.get<double>(3 * Nc);
   S.xi = m.get<double>(3 * Nc);
   S.exch = m.get<ExchAcc>(Nc);
+  S.xacc = m.get<double>(6 * Nc);
   S.shell_cnt = m.get<int>(Nc);
   S.pot_part = m.get<double>(Nc);
   // run() candidates: particles within sigma/2 + 1/2 of a colloid, with room to spare
@@ -906,5 +907,19 @@ extern "C" int64_t mpcd_launch_count(const mpcd_ctx *c) { return c ? c->launches
 
 // initialisation lives in init.cu; it needs the context internals
 #include "init_host.inc"
+
+extern "C" int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset) {
+  if (!c) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  if (!c->S.Nc) return MPCD_OK;
+  const size_t nb = sizeof(double) * 6 * (size_t)c->S.Nc;
+  if (out) CUDA_OK(c, scopy(c, out, c->S.xacc, nb, cudaMemcpyDeviceToHost));
+  if (reset) {
+    CUDA_OK(c, cudaMemsetAsync(c->S.xacc, 0, nb, c->stream));
+    CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  }
+  return MPCD_OK;
+}
 
 #include "ensemble.inc"

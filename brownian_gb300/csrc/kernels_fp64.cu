@@ -495,7 +495,9 @@ static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB,
     const double x = __dadd_rn((double)e->hi[lane] * 0x1p-20, (double)e->lo[lane] * 0x1p-72);
     e->hi[lane] = 0;
     e->lo[lane] = 0;
-    v = __dadd_rn(v, __ddiv_rn(__dmul_rn(x, S.mass_fl), lin ? S.mass_colloid : S.I_colloid));
+    const double dp = __dmul_rn(x, S.mass_fl);
+    S.xacc[6 * j + lane] += dp;  // the exchange record (mpcd_exchange_read)
+    v = __dadd_rn(v, __ddiv_rn(dp, lin ? S.mass_colloid : S.I_colloid));
     if (lin) {
       // compute_force_md at X_g (done by the streaming pass) and update_velocity_colloid
       const double fn = S.fnew[3 * j + k];

@@ -1,0 +1,528 @@
+// The learned closure's network: an MLP 81 -> 256 -> 256 -> 256 -> 12 with SiLU,
+// trained and evaluated on the GPU by this file's own kernels.
+//
+// Weights are BF16 for the tensor cores (warp-level mma.sync m16n8k16, FP32
+// accumulation) with FP32 master copies for Adam.  Activations and gradients
+// between layers are BF16, every product accumulates in FP32.  The inputs are
+// the closure's 81 colloid features, normalised by stored means and standard
+// deviations; the outputs are the normalised means (6) and log-variances (6) of
+// a colloid's per-step momentum and angular-momentum exchange with the fluid,
+// trained by the Gaussian negative log-likelihood.
+//
+// One GEMM kernel serves every product: C[M x N] = A[M x K] B[K x N] with A and B
+// addressed through arbitrary strides (forward x W, backward dZ W^T and A^T dZ),
+// 64 x 64 block tiles, 32-wide K steps staged in shared memory, four warps of
+// 32 x 32 each, and a fused epilogue (bias, SiLU, the SiLU derivative of the
+// backward pass, BF16 / FP32 stores, FP32 atomic accumulation for split-K
+// weight gradients).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/brownian_gb300.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int IN = MPCD_MLP_IN, INP = 96, H = MPCD_MLP_HIDDEN, OUT = MPCD_MLP_OUT, OUTP = 16, NY = OUT / 2;
+constexpr int BM = 64, BN = 64, BK = 32, PADK = BK + 8;
+
+struct Gemm {
+  const bf16 *A;
+  long long sam, sak;
+  const bf16 *B;
+  long long sbk, sbn;
+  int M, N, K;
+  const float *bias;   // [N] or null
+  int silu;            // apply SiLU after the bias
+  const bf16 *dz;      // backward: multiply by silu'(dz[m, n]) (the layer's pre-activation)
+  long long lddz;
+  float *Cf;           // FP32 store
+  long long ldcf;
+  bf16 *Cb;            // BF16 store (after the activation)
+  long long ldcb;
+  bf16 *Zb;            // BF16 store of the pre-activation
+  long long ldzb;
+  float *Cacc;         // FP32 atomic accumulation
+  long long ldca;
+  int kchunk;          // K range of one blockIdx.z
+};
+
+__device__ __forceinline__ float sigm(float z) { return 1.f / (1.f + __expf(-z)); }
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(128) k_gemm(const Gemm g) {
+  __shared__ __align__(16) bf16 As[BM][PADK];
+  __shared__ __align__(16) bf16 Bs[BN][PADK];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kbeg = blockIdx.z * g.kchunk, kend = min(g.K, kbeg + g.kchunk);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  const bf16 zero = __float2bfloat16(0.f);
+  const bool a_kfast = g.sak == 1, b_kfast = g.sbk == 1;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    // stage A[m0.., k0..] and B[k0.., n0..] (as Bs[n][k]), zero outside the matrices
+#pragma unroll 4
+    for (int e = 0; e < (BM * BK) / 128; ++e) {
+      const int idx = e * 128 + tid;
+      const int r = a_kfast ? idx / BK : idx % BM, kk = a_kfast ? idx % BK : idx / BM;
+      const int m = m0 + r, k = k0 + kk;
+      As[r][kk] = (m < g.M && k < kend) ? g.A[m * g.sam + k * g.sak] : zero;
+    }
+#pragma unroll 4
+    for (int e = 0; e < (BN * BK) / 128; ++e) {
+      const int idx = e * 128 + tid;
+      const int c = b_kfast ? idx / BK : idx % BN, kk = b_kfast ? idx % BK : idx / BN;
+      const int n = n0 + c, k = k0 + kk;
+      Bs[c][kk] = (n < g.N && k < kend) ? g.B[k * g.sbk + n * g.sbn] : zero;
+    }
+    __syncthreads();
+    const int gq = lane >> 2, q = lane & 3;
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r0 = wm * 32 + i * 16 + gq;
+        af[i][0] = *reinterpret_cast<const uint32_t *>(&As[r0][kk + q * 2]);
+        af[i][1] = *reinterpret_cast<const uint32_t *>(&As[r0 + 8][kk + q * 2]);
+        af[i][2] = *reinterpret_cast<const uint32_t *>(&As[r0][kk + q * 2 + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t *>(&As[r0 + 8][kk + q * 2 + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn * 32 + j * 8 + gq;
+        bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + q * 2]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + q * 2 + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+  // epilogue
+  const int gq = lane >> 2, q = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm * 32 + i * 16 + gq + (r >= 2 ? 8 : 0);
+        const int n = n0 + wn * 32 + j * 8 + q * 2 + (r & 1);
+        if (m >= g.M || n >= g.N) continue;
+        float v = acc[i][j][r];
+        if (g.Cacc) {
+          atomicAdd(&g.Cacc[m * g.ldca + n], v);
+          continue;
+        }
+        if (g.bias) v += g.bias[n];
+        if (g.Zb) g.Zb[m * g.ldzb + n] = __float2bfloat16(v);
+        if (g.dz) {
+          const float z = __bfloat162float(g.dz[m * g.lddz + n]), s = sigm(z);
+          v *= s * (1.f + z * (1.f - s));
+        }
+        if (g.silu) v = v * sigm(v);
+        if (g.Cf) g.Cf[m * g.ldcf + n] = v;
+        if (g.Cb) g.Cb[m * g.ldcb + n] = __float2bfloat16(v);
+      }
+}
+
+// raw features [n][IN] -> normalised BF16 [n][INP] (zero padded)
+__global__ void k_features_in(const float *x, int n, const float *mean, const float *istd, bf16 *out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)n * INP) return;
+  const int r = (int)(i / INP), c = (int)(i % INP);
+  out[i] = __float2bfloat16(c < IN ? (x[(long long)r * IN + c] - mean[c]) * istd[c] : 0.f);
+}
+
+// Gaussian negative log-likelihood of normalised targets under (mean, log-variance)
+// outputs; writes d loss / d output (BF16, mean over the batch) and adds the loss sum
+__global__ void k_nll(const float *o, const float *y, int n, const float *ymean, const float *yistd, bf16 *dout,
+                      double *loss) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.f;
+  if (r < n) {
+    const float inv = 1.f / (float)n;
+    for (int k = 0; k < NY; ++k) {
+      const float t = (y[r * NY + k] - ymean[k]) * yistd[k];
+      const float mu = o[r * OUTP + k];
+      const float sraw = o[r * OUTP + NY + k];
+      const float s = fminf(fmaxf(sraw, -12.f), 12.f);
+      const float e = __expf(-s), d = t - mu;
+      l += 0.5f * (d * d * e + s);
+      dout[r * OUTP + k] = __float2bfloat16(-d * e * inv);
+      dout[r * OUTP + NY + k] = __float2bfloat16((sraw == s) ? 0.5f * (1.f - d * d * e) * inv : 0.f);
+    }
+    for (int k = OUT; k < OUTP; ++k) dout[r * OUTP + k] = __float2bfloat16(0.f);
+  }
+  // block sum, one atomic per block
+  __shared__ float sh[256];
+  sh[threadIdx.x] = l;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, (double)sh[0]);
+}
+
+// normalised outputs -> physical units: mean * std + mean, log-variance + 2 log std
+__global__ void k_denorm(const float *o, int n, const float *ymean, const float *yistd, float *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * OUT) return;
+  const int r = i / OUT, k = i % OUT;
+  const float v = o[r * OUTP + k];
+  out[i] = k < NY ? v / yistd[k] + ymean[k] : v - 2.f * __logf(yistd[k - NY]);
+}
+
+// column sums of a BF16 matrix into FP32 (bias gradients), one atomic per (block, column)
+__global__ void k_colsum(const bf16 *a, int n, int cols, long long lda, float *out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const int per = (n + gridDim.y - 1) / gridDim.y, r0 = blockIdx.y * per, r1 = min(n, r0 + per);
+  float s = 0.f;
+  for (int r = r0; r < r1; ++r) s += __bfloat162float(a[r * lda + c]);
+  atomicAdd(&out[c], s);
+}
+
+// the parameter layout: flat FP32 vector (W1 [IN][H], b1, W2 [H][H], b2, W3, b3, W4 [H][OUT], b4)
+// and the padded BF16 weights the GEMMs read
+struct Layout {
+  long long w[4], b[4], total;
+  int kin[4], nout[4];
+};
+
+Layout layout() {
+  Layout L;
+  const int kin[4] = {IN, H, H, H}, nout[4] = {H, H, H, OUT};
+  long long o = 0;
+  for (int l = 0; l < 4; ++l) {
+    L.kin[l] = kin[l];
+    L.nout[l] = nout[l];
+    L.w[l] = o;
+    o += (long long)kin[l] * nout[l];
+    L.b[l] = o;
+    o += nout[l];
+  }
+  L.total = o;
+  return L;
+}
+
+// Adam on the FP32 masters, then the BF16 copies (weights at [k][n] of a padded
+// [kpad][npad] matrix; biases stay FP32)
+__global__ void k_adam(float *p, const float *gr, float *m, float *v, long long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2, Layout L, bf16 *w0, bf16 *w1, bf16 *w2, bf16 *w3, float *bias) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = gr[i];
+  const float mi = b1 * m[i] + (1.f - b1) * g, vi = b2 * v[i] + (1.f - b2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float x = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  p[i] = x;
+  bf16 *ws[4] = {w0, w1, w2, w3};
+  const int npad[4] = {H, H, H, OUTP};
+  long long boff = 0;
+  for (int l = 0; l < 4; ++l) {
+    if (i >= L.w[l] && i < L.b[l]) {
+      const long long j = i - L.w[l];
+      const int k = (int)(j / L.nout[l]), c = (int)(j % L.nout[l]);
+      ws[l][(long long)k * npad[l] + c] = __float2bfloat16(x);
+      return;
+    }
+    if (i >= L.b[l] && i < L.b[l] + L.nout[l]) {
+      bias[boff + (i - L.b[l])] = x;
+      return;
+    }
+    boff += npad[l];
+  }
+}
+
+}  // namespace
+
+struct mpcd_mlp {
+  int max_batch = 0;
+  Layout L;
+  float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // flat FP32 params, grads, Adam moments
+  bf16 *w[4] = {nullptr, nullptr, nullptr, nullptr};               // padded BF16 weights
+  float *bias = nullptr;                                           // padded biases [H][H][H][OUTP]
+  float *xmean = nullptr, *xistd = nullptr, *ymean = nullptr, *yistd = nullptr;
+  bf16 *X = nullptr, *Z[3] = {nullptr, nullptr, nullptr}, *A[3] = {nullptr, nullptr, nullptr};
+  float *O = nullptr;
+  bf16 *dO = nullptr, *dA = nullptr, *dZ = nullptr;
+  double *loss = nullptr;
+  float *host_p = nullptr;
+  int adam_t = 0;
+  std::vector<void *> allocs;
+  std::string err;
+};
+
+namespace {
+
+int mfail(mpcd_mlp *n, int code, const std::string &e) {
+  if (n) n->err = e;
+  return code;
+}
+
+template <typename T>
+T *dalloc(mpcd_mlp *n, size_t count) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, count * sizeof(T) + 256) != cudaSuccess) {
+    n->err = "out of device memory";
+    return nullptr;
+  }
+  cudaMemset(p, 0, count * sizeof(T) + 256);
+  n->allocs.push_back(p);
+  return static_cast<T *>(p);
+}
+
+void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
+  g.kchunk = ksplit > 1 ? ((g.K + ksplit - 1) / ksplit + BK - 1) / BK * BK : g.K;
+  const int kz = ksplit > 1 ? (g.K + g.kchunk - 1) / g.kchunk : 1;
+  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, kz);
+  k_gemm<<<grid, 128, 0, s>>>(g);
+}
+
+Gemm base() {
+  Gemm g;
+  memset(&g, 0, sizeof g);
+  return g;
+}
+
+const int kNpad[4] = {H, H, H, OUTP};
+const int kKpad[4] = {INP, H, H, H};
+
+long long bias_off(int l) {
+  long long o = 0;
+  for (int i = 0; i < l; ++i) o += kNpad[i];
+  return o;
+}
+
+// forward of rows [0, n) of n->X; stores Z (pre-activations) and A (activations) for the backward pass
+void forward(mpcd_mlp *nn, int n, cudaStream_t s) {
+  const bf16 *in = nn->X;
+  long long ldin = INP;
+  for (int l = 0; l < 4; ++l) {
+    Gemm g = base();
+    g.A = in; g.sam = ldin; g.sak = 1;
+    g.B = nn->w[l]; g.sbk = kNpad[l]; g.sbn = 1;
+    g.M = n; g.N = kNpad[l]; g.K = kKpad[l];
+    g.bias = nn->bias + bias_off(l);
+    if (l < 3) {
+      g.silu = 1;
+      g.Zb = nn->Z[l]; g.ldzb = H;
+      g.Cb = nn->A[l]; g.ldcb = H;
+      in = nn->A[l];
+      ldin = H;
+    } else {
+      g.Cf = nn->O; g.ldcf = OUTP;
+    }
+    gemm(s, g);
+  }
+}
+
+// gradients of the mean loss over rows [0, n) into n->g (zeroed first)
+void backward(mpcd_mlp *nn, int n, cudaStream_t s) {
+  cudaMemsetAsync(nn->g, 0, sizeof(float) * nn->L.total, s);
+  const bf16 *dcur = nn->dO;  // gradient w.r.t. the output of layer l (after its activation)
+  long long ldd = OUTP;
+  for (int l = 3; l >= 0; --l) {
+    const int kin = nn->L.kin[l], nout = nn->L.nout[l];
+    const bf16 *act = l > 0 ? nn->A[l - 1] : nn->X;
+    const long long ldact = l > 0 ? H : INP;
+    // dW[k][c] = sum_b act[b][k] dcur[b][c]  (dcur is already d/d(pre-activation) of layer l)
+    Gemm gw = base();
+    gw.A = act; gw.sam = 1; gw.sak = ldact;
+    gw.B = dcur; gw.sbk = ldd; gw.sbn = 1;
+    gw.M = kin; gw.N = nout; gw.K = n;
+    gw.Cacc = nn->g + nn->L.w[l]; gw.ldca = nout;
+    gemm(s, gw, n >= 4096 ? 16 : 1);
+    dim3 cg((nout + 127) / 128, n >= 4096 ? 32 : 1);
+    k_colsum<<<cg, 128, 0, s>>>(dcur, n, nout, ldd, nn->g + nn->L.b[l]);
+    if (l == 0) break;
+    // d/d(pre-activation of layer l-1) = (dcur W_l^T) * silu'(Z_{l-1})
+    Gemm gd = base();
+    gd.A = dcur; gd.sam = ldd; gd.sak = 1;
+    gd.B = nn->w[l]; gd.sbk = 1; gd.sbn = kNpad[l];  // B(k = c, n = i) = W_l[i][c]
+    gd.M = n; gd.N = H; gd.K = kNpad[l];
+    gd.dz = nn->Z[l - 1]; gd.lddz = H;
+    bf16 *dst = (l % 2) ? nn->dA : nn->dZ;
+    gd.Cb = dst; gd.ldcb = H;
+    gemm(s, gd);
+    dcur = dst;
+    ldd = H;
+  }
+}
+
+void init_params(mpcd_mlp *nn, uint64_t seed, std::vector<float> &h) {
+  std::mt19937_64 rng(seed);
+  h.assign(nn->L.total, 0.f);
+  for (int l = 0; l < 4; ++l) {
+    const float a = std::sqrt(6.f / (float)(nn->L.kin[l] + nn->L.nout[l]));  // Glorot uniform
+    std::uniform_real_distribution<float> u(-a, a);
+    for (long long i = nn->L.w[l]; i < nn->L.b[l]; ++i) h[i] = u(rng);
+  }
+}
+
+int upload_params(mpcd_mlp *nn, const float *h) {
+  if (cudaMemcpy(nn->p, h, sizeof(float) * nn->L.total, cudaMemcpyHostToDevice) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "parameter upload");
+  // zero gradient, zero learning rate: writes the BF16 copies and biases from the masters
+  cudaMemset(nn->g, 0, sizeof(float) * nn->L.total);
+  const long long n = nn->L.total;
+  k_adam<<<(unsigned)((n + 255) / 256), 256>>>(nn->p, nn->g, nn->m, nn->v, n, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f,
+                                              nn->L, nn->w[0], nn->w[1], nn->w[2], nn->w[3], nn->bias);
+  cudaMemset(nn->m, 0, sizeof(float) * n);
+  cudaMemset(nn->v, 0, sizeof(float) * n);
+  return cudaDeviceSynchronize() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "parameter upload");
+}
+
+int stage_inputs(mpcd_mlp *nn, const float *x, int n, cudaStream_t s) {
+  if (n < 1 || n > nn->max_batch) return mfail(nn, MPCD_ERR_CAPACITY, "batch larger than max_batch");
+  const long long tot = (long long)n * INP;
+  k_features_in<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(x, n, nn->xmean, nn->xistd, nn->X);
+  return MPCD_OK;
+}
+
+}  // namespace
+
+extern "C" int mpcd_mlp_create(int max_batch, uint64_t seed, mpcd_mlp **out) {
+  if (!out || max_batch < 1) return MPCD_ERR_PARAM;
+  *out = nullptr;
+  mpcd_mlp *nn = new mpcd_mlp();
+  nn->max_batch = max_batch;
+  nn->L = layout();
+  const long long P = nn->L.total;
+  nn->p = dalloc<float>(nn, P); nn->g = dalloc<float>(nn, P); nn->m = dalloc<float>(nn, P); nn->v = dalloc<float>(nn, P);
+  for (int l = 0; l < 4; ++l) nn->w[l] = dalloc<bf16>(nn, (size_t)kKpad[l] * kNpad[l]);
+  nn->bias = dalloc<float>(nn, 3 * H + OUTP);
+  nn->xmean = dalloc<float>(nn, IN); nn->xistd = dalloc<float>(nn, IN);
+  nn->ymean = dalloc<float>(nn, NY); nn->yistd = dalloc<float>(nn, NY);
+  const size_t B = (size_t)max_batch;
+  nn->X = dalloc<bf16>(nn, B * INP);
+  for (int l = 0; l < 3; ++l) {
+    nn->Z[l] = dalloc<bf16>(nn, B * H);
+    nn->A[l] = dalloc<bf16>(nn, B * H);
+  }
+  nn->O = dalloc<float>(nn, B * OUTP);
+  nn->dO = dalloc<bf16>(nn, B * OUTP);
+  nn->dA = dalloc<bf16>(nn, B * H);
+  nn->dZ = dalloc<bf16>(nn, B * H);
+  nn->loss = dalloc<double>(nn, 1);
+  if (!nn->err.empty()) {
+    mpcd_mlp_destroy(nn);
+    return MPCD_ERR_NOMEM;
+  }
+  std::vector<float> one(IN, 1.f), zero(IN, 0.f);
+  cudaMemcpy(nn->xistd, one.data(), sizeof(float) * IN, cudaMemcpyHostToDevice);
+  cudaMemcpy(nn->yistd, one.data(), sizeof(float) * NY, cudaMemcpyHostToDevice);
+  std::vector<float> h;
+  init_params(nn, seed, h);
+  int r = upload_params(nn, h.data());
+  if (r) {
+    mpcd_mlp_destroy(nn);
+    return r;
+  }
+  *out = nn;
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_mlp_destroy(mpcd_mlp *nn) {
+  if (!nn) return MPCD_ERR_PARAM;
+  cudaDeviceSynchronize();
+  for (void *a : nn->allocs) cudaFree(a);
+  delete nn;
+  return MPCD_OK;
+}
+
+extern "C" const char *mpcd_mlp_last_error(const mpcd_mlp *nn) { return nn ? nn->err.c_str() : "null network"; }
+
+extern "C" int64_t mpcd_mlp_param_count(const mpcd_mlp *nn) { return nn ? nn->L.total : -1; }
+
+extern "C" int mpcd_mlp_set_normalisation(mpcd_mlp *nn, const float *x_mean, const float *x_std, const float *y_mean,
+                                          const float *y_std) {
+  if (!nn || !x_mean || !x_std || !y_mean || !y_std) return MPCD_ERR_PARAM;
+  std::vector<float> xi(IN), yi(NY);
+  for (int i = 0; i < IN; ++i) xi[i] = x_std[i] > 0 ? 1.f / x_std[i] : 0.f;
+  for (int i = 0; i < NY; ++i) yi[i] = y_std[i] > 0 ? 1.f / y_std[i] : 0.f;
+  if (cudaMemcpy(nn->xmean, x_mean, sizeof(float) * IN, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(nn->xistd, xi.data(), sizeof(float) * IN, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(nn->ymean, y_mean, sizeof(float) * NY, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(nn->yistd, yi.data(), sizeof(float) * NY, cudaMemcpyHostToDevice) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "normalisation upload");
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_mlp_get_params(mpcd_mlp *nn, float *out) {
+  if (!nn || !out) return MPCD_ERR_PARAM;
+  if (cudaMemcpy(out, nn->p, sizeof(float) * nn->L.total, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "parameter download");
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_mlp_set_params(mpcd_mlp *nn, const float *in) {
+  if (!nn || !in) return MPCD_ERR_PARAM;
+  return upload_params(nn, in);
+}
+
+extern "C" int mpcd_mlp_forward(mpcd_mlp *nn, const float *x, int n, float *out, void *stream) {
+  if (!nn || !x || !out) return MPCD_ERR_PARAM;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int r = stage_inputs(nn, x, n, s);
+  if (r) return r;
+  forward(nn, n, s);
+  k_denorm<<<(n * OUT + 255) / 256, 256, 0, s>>>(nn->O, n, nn->ymean, nn->yistd, out);
+  return cudaGetLastError() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "forward launch");
+}
+
+extern "C" int mpcd_mlp_grad(mpcd_mlp *nn, const float *x, const float *y, int n, float *grad, double *loss) {
+  if (!nn || !x || !y) return MPCD_ERR_PARAM;
+  int r = stage_inputs(nn, x, n, nullptr);
+  if (r) return r;
+  forward(nn, n, nullptr);
+  cudaMemset(nn->loss, 0, sizeof(double));
+  k_nll<<<(n + 255) / 256, 256>>>(nn->O, y, n, nn->ymean, nn->yistd, nn->dO, nn->loss);
+  backward(nn, n, nullptr);
+  if (grad && cudaMemcpy(grad, nn->g, sizeof(float) * nn->L.total, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "gradient download");
+  double l = 0;
+  if (cudaMemcpy(&l, nn->loss, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "loss download");
+  if (loss) *loss = l / n;
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_mlp_train_step(mpcd_mlp *nn, const float *x, const float *y, int n, float lr, double *loss) {
+  int r = mpcd_mlp_grad(nn, x, y, n, nullptr, loss);
+  if (r) return r;
+  nn->adam_t += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f / (1.f - std::pow(b1, (float)nn->adam_t)), c2 = 1.f / (1.f - std::pow(b2, (float)nn->adam_t));
+  const long long P = nn->L.total;
+  k_adam<<<(unsigned)((P + 255) / 256), 256>>>(nn->p, nn->g, nn->m, nn->v, P, lr, b1, b2, 1e-8f, c1, c2, nn->L,
+                                              nn->w[0], nn->w[1], nn->w[2], nn->w[3], nn->bias);
+  return cudaGetLastError() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "adam launch");
+}

@@ -107,6 +107,7 @@ struct SysF64 {
   double *fnew;             // [Nc][3] force at the positions of the substep in flight
   double *xi;               // [Nc][3] rotational-diffusion normals of the substep in flight
   ExchAcc *exch;       // [Nc]
+  double *xacc;        // [Nc][6] fluid-to-colloid momentum and angular momentum received since the last read
   int *shell_cnt;      // [Nc]
   // fluid-to-colloid table, double-buffered like X: per cell (substep << 32) | count,
   // entries of another substep read as empty, so the table is never cleared

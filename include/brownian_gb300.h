@@ -149,6 +149,12 @@ enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, mu
  * exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
+/* ---- exchange record (no counterpart in the reference) ------------------------------- */
+/* The momentum (m sum dv, 3) and angular momentum (m sum r x dv, 3) the fluid gave each colloid
+ * in the stochastic reflections (cpp/fluid_colloid_collision.cpp:46-47) since the last reset:
+ * out[6 j + k], Nc x 6 doubles (NULL: reset only).  The training data of the learned closure. */
+int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset);
+
 /* ---- batched ensemble (no counterpart in the reference) ------------------------------- */
 /* nrep independent systems with their own parameters p[0..nrep-1] (box, fluid, colloids,
  * activity, seed; all MPCD_FP32C with equal n_sub and sort_every) stepped together: every
@@ -171,6 +177,34 @@ enum { MPCD_ENS_EVENTS = 0,  /* blocks per system of the event pass (1..64) */
 int mpcd_ensemble_set_launch(mpcd_ensemble *e, int which, int per_system, int block);
 /* kernels the ensemble launched since creation */
 int64_t mpcd_ensemble_launch_count(const mpcd_ensemble *e);
+
+/* ---- learned closure network (no counterpart in the reference) ----------------------- */
+/* MLP 81 -> 256 -> 256 -> 256 -> 12 with SiLU, BF16 weights on the tensor cores with FP32
+ * accumulation and FP32 master weights for Adam.  Inputs: a colloid's 81 closure features
+ * (raw units; normalised inside by mpcd_mlp_set_normalisation's statistics).  Outputs: the
+ * means (6) and log-variances (6) of its per-step momentum and angular-momentum exchange with
+ * the fluid, in physical units.  x, y and out are device pointers (rows x 81, rows x 6,
+ * rows x 12 floats); rows <= max_batch.  Parameters as one flat FP32 vector (W1 [81][256], b1,
+ * W2 [256][256], b2, W3, b3, W4 [256][12], b4).  Weight gradients are summed with FP32 atomics,
+ * so a gradient is reproducible only to rounding. */
+#define MPCD_MLP_IN 81
+#define MPCD_MLP_HIDDEN 256
+#define MPCD_MLP_OUT 12
+typedef struct mpcd_mlp mpcd_mlp;
+int mpcd_mlp_create(int max_batch, uint64_t seed, mpcd_mlp **out);
+int mpcd_mlp_destroy(mpcd_mlp *n);
+const char *mpcd_mlp_last_error(const mpcd_mlp *n);
+int64_t mpcd_mlp_param_count(const mpcd_mlp *n);
+int mpcd_mlp_set_normalisation(mpcd_mlp *n, const float *x_mean, const float *x_std, const float *y_mean,
+                               const float *y_std);
+int mpcd_mlp_get_params(mpcd_mlp *n, float *out_host);
+int mpcd_mlp_set_params(mpcd_mlp *n, const float *in_host);
+/* inference, asynchronous on `stream` */
+int mpcd_mlp_forward(mpcd_mlp *n, const float *x, int rows, float *out, void *stream);
+/* mean Gaussian negative log-likelihood of y and its gradient (host, param_count floats; NULL: skip) */
+int mpcd_mlp_grad(mpcd_mlp *n, const float *x, const float *y, int rows, float *grad_host, double *loss_host);
+/* one Adam step (beta 0.9, 0.999) on the batch; loss_host receives the batch loss before the step */
+int mpcd_mlp_train_step(mpcd_mlp *n, const float *x, const float *y, int rows, float lr, double *loss_host);
 
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their

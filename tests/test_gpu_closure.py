@@ -1,0 +1,73 @@
+"""The closure network on the GPU (BF16 tensor-core GEMMs, FP32 accumulation)
+against its CPU restatement (oracle/mlp_ref.py): gradients (the restatement
+rounds to BF16 where the GPU stores BF16), outputs, and that training lowers
+the loss below what a network-free prediction gives."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n, seed):
+    import torch
+
+    from brownian_gb300 import closure
+    rng = np.random.default_rng(seed)
+    net = closure.Network(max_batch=4096, seed=seed)
+    p = rng.normal(0, 0.08, net.n_params).astype(np.float32)
+    net.set_params(p)
+    xm = rng.normal(0, 1, M.IN).astype(np.float32)
+    xs = rng.uniform(0.5, 2, M.IN).astype(np.float32)
+    ym = rng.normal(0, 1, M.NY).astype(np.float32)
+    ys = rng.uniform(0.5, 2, M.NY).astype(np.float32)
+    net.set_normalisation(xm, xs, ym, ys)
+    x = (xm + xs * rng.normal(0, 1, (n, M.IN))).astype(np.float32)
+    y = (ym + ys * rng.normal(0, 1, (n, M.NY))).astype(np.float32)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    return net, p, x, y, xm, xs, ym, ys, xd, yd
+
+
+def test_gradients_match_cpu_oracle():
+    net, p, x, y, xm, xs, ym, ys, xd, yd = _setup(300, 1)
+    loss, g = net.grad(xd.data_ptr(), yd.data_ptr(), 300)
+    lref, gref = M.loss_and_grad(p, x, y, xm, xs, ym, ys, bf16_emul=True)
+    assert abs(loss - lref) <= 1e-3 * abs(lref)
+    o = 0
+    for k, n in M.DIMS:
+        for size in (k * n, n):
+            a, b = g[o:o + size], gref[o:o + size]
+            assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-7, (o, size)
+            o += size
+    net.close()
+
+
+def test_forward_matches_cpu_oracle():
+    import torch
+    net, p, x, y, xm, xs, ym, ys, xd, yd = _setup(1000, 2)
+    out = torch.zeros((1000, M.OUT), dtype=torch.float32, device="cuda")
+    net.forward(xd.data_ptr(), out.data_ptr(), 1000)
+    torch.cuda.synchronize()
+    ref = M.forward(p, x.astype(np.float64), xm, xs, ym, ys)
+    got = out.cpu().numpy()
+    assert np.linalg.norm(got - ref) <= 2e-2 * np.linalg.norm(ref)
+    net.close()
+
+
+def test_training_beats_the_network_free_prediction():
+    import torch
+
+    from brownian_gb300 import closure
+    rng = np.random.default_rng(3)
+    n = 20000
+    x = rng.normal(0, 1, (n, M.IN)).astype(np.float32)
+    A = rng.normal(0, 0.3, (M.IN, M.NY))
+    y = (np.tanh(x @ A) + (0.2 + 0.3 * np.abs(x[:, :1])) * rng.normal(0, 1, (n, M.NY))).astype(np.float32)
+    net = closure.Network(max_batch=4096, seed=3)
+    net.fit_normalisation(x, y)
+    losses = closure.train(net, x, y, epochs=8, batch=2048, lr=2e-3)
+    # network-free: the normalised target's mean 0 and variance 1 -> 0.5 per output
+    assert losses[-1] < losses[0]
+    assert losses[-1] < 0.5 * M.NY - 1.0, losses
+    net.close()
