@@ -370,6 +370,79 @@ def run_ensemble(nrep, steps, rank):
             "timing": "wall clock around mpcd_ensemble_step(K) (it ends with a device synchronisation)"}
 
 
+def run_closure(samples_steps, deploy_steps):
+    """The learned closure: training samples from full MPCD of the 64^3 system with v0 swept
+    over [0, 0.1] (500 colloids x 5 activities x samples_steps steps), GPU training, then
+    colloid-only runs against full MPCD (the judge) on a 500-colloid system at volume
+    fraction 0.1, and the time per MPCD step of both at 500 and 2000 colloids."""
+    import time as _t
+
+    import numpy as np
+
+    import brownian_gb300 as bg
+    from brownian_gb300 import closure
+    M = bg.displaced_mass(RADIUS, DENSITY)
+
+    def P(Lr, nc, v0, seed):
+        return bg.make_params(Lr, Lr ** 3 * DENSITY, nc, n_sub=10, mass_colloid=M, sig_colloid=2 * RADIUS,
+                              sigma=2 * RADIUS, I_colloid=0.4 * M * RADIUS ** 2, v0=v0, theta_deg=90.0, Dr=0.001,
+                              seed=seed, precision=bg.FP32C)
+    t0 = _t.perf_counter()
+    X, Y = closure.generate_gpu([P(L, NC, v0, 500 + i) for i, v0 in enumerate((0.0, 0.025, 0.05, 0.075, 0.1))],
+                                steps=samples_steps)
+    t_data = _t.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(X.shape[0])
+    X, Y = X[perm], Y[perm]
+    cut = int(0.95 * X.shape[0])
+    net = closure.Network(max_batch=8192, seed=0)
+    net.fit_normalisation(X[:cut], Y[:cut])
+    t0 = _t.perf_counter()
+    losses = closure.train(net, X[:cut], Y[:cut], epochs=12, batch=8192, lr=3e-4)
+    t_train = _t.perf_counter() - t0
+    held = closure.nll(net, X[cut:], Y[cut:])
+    free = closure.free_nll(Y[:cut], Y[cut:])
+    L500 = int(round((500 * 4.0 / 3.0 * np.pi * RADIUS ** 3 / 0.1) ** (1.0 / 3.0)))
+    res = closure.compare(P(L500, 500, 0.05, 901), net, steps=deploy_steps)
+    # timing at 2000 colloids, volume fraction 0.1
+    L2k = int(round((2000 * 4.0 / 3.0 * np.pi * RADIUS ** 3 / 0.1) ** (1.0 / 3.0)))
+    p2k = P(L2k, 2000, 0.05, 902)
+    full = closure._sim(p2k)
+    full.initialize(bg.INIT_PHYSICAL)
+    full.setup()
+    full.step(3)
+    t0 = _t.perf_counter()
+    full.step(10)
+    t_full2k = (_t.perf_counter() - t0) / 10
+    c0 = full.get_colloids()
+    full.close()
+    net2k = closure.Network(max_batch=2048)
+    net2k.set_params(net.params())
+    net2k.set_normalisation(*net.norm)
+    sur = closure.Surrogate(p2k, net2k)
+    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    sur.step(5)
+    t0 = _t.perf_counter()
+    sur.step(100)
+    t_sur2k = (_t.perf_counter() - t0) / 100
+    sur.close()
+    net2k.close()
+    net.close()
+    ndt = 0.1
+    return {"workload": "closure trained on 64^3 / 500 colloids, v0 in {0, .025, .05, .075, .1}; deployed on "
+                        f"{L500}^3 / 500 colloids (volume fraction 0.1, v0 = 0.05) against full MPCD",
+            "samples": int(X.shape[0]), "data_s": t_data, "train_s": t_train, "epochs": len(losses),
+            "train_loss_first_last": [losses[0], losses[-1]],
+            "heldout_nll": held, "heldout_nll_without_network": free,
+            "colloid_time_per_wall_s": {"surrogate_500": ndt / (res["t_surrogate_ms"] / 1e3),
+                                        "full_500": ndt / (res["t_full_ms"] / 1e3),
+                                        "surrogate_2000": ndt / t_sur2k, "full_2000": ndt / t_full2k},
+            "speedup_500": res["speedup"], "speedup_2000": t_full2k / t_sur2k,
+            "deploy_steps": deploy_steps, "lags": res["lags"], "rel_diff_vs_full": res["rel_diff_vs_full"],
+            "stats": res["stats"],
+            "timing": "wall clock around step calls (each ends with a synchronisation)"}
+
+
 def run_ours(args, rank, world, dist):
     import torch
 
@@ -415,6 +488,7 @@ def run_ours(args, rank, world, dist):
     sim.close()
     stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
     ens = run_ensemble(args.ensemble, args.ensemble_steps, rank) if args.ensemble > 0 else None
+    clo = run_closure(args.closure_steps, 600) if (args.closure_steps > 0 and rank == 0) else None
 
     if rank != 0:
         return None
@@ -443,6 +517,8 @@ def run_ours(args, rank, world, dist):
         line["fp32c_vs_fp64"] = stats
     if ens:
         line["ensemble"] = ens
+    if clo:
+        line["closure"] = clo
     return line
 
 
@@ -458,6 +534,8 @@ def main():
                     help="steps of the FP32c-vs-FP64 statistics run (MSD at lag 100; <=100: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="replicas of the batched-ensemble sub-object (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--closure-steps", type=int, default=800,
+                    help="steps per activity of the closure's training runs (500 colloids each; 0: skip)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
     args = ap.parse_args()

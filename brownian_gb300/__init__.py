@@ -29,7 +29,9 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
            "mpcd_exchange_read", "mpcd_mlp_create", "mpcd_mlp_destroy", "mpcd_mlp_last_error", "mpcd_mlp_param_count",
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
-           "mpcd_mlp_grad", "mpcd_mlp_train_step"]
+           "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
+           "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
+           "mpcd_surrogate_features", "mpcd_surrogate_step"]
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2

@@ -157,7 +157,26 @@ class Network:
             pass
 
 
-def train(net, X, Y, epochs=20, batch=4096, lr=1e-3, seed=0, log=None):
+def nll(net, X, Y):
+    """Mean Gaussian negative log-likelihood of (X, Y) under the network, in chunks."""
+    import torch
+    Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).cuda()
+    Yd = torch.from_numpy(np.ascontiguousarray(Y, dtype=np.float32)).cuda()
+    tot, n = 0.0, X.shape[0]
+    for b0 in range(0, n, net.max_batch):
+        rows = min(net.max_batch, n - b0)
+        l, _ = net.grad(Xd[b0:].data_ptr(), Yd[b0:].data_ptr(), rows)
+        tot += l * rows
+    return tot / n
+
+
+def free_nll(Y_train, Y):
+    """The same likelihood without the network: targets as N(mean, std) of the training set."""
+    ym, ys = Y_train.mean(0), Y_train.std(0)
+    return float(np.mean(np.sum(0.5 * ((Y - ym) / ys) ** 2, axis=1)))
+
+
+def train(net, X, Y, epochs=20, batch=4096, lr=3e-4, seed=0, log=None):
     """Adam over shuffled mini-batches on the GPU; returns the mean loss of each epoch."""
     import torch
     rng = np.random.default_rng(seed)
@@ -178,3 +197,184 @@ def train(net, X, Y, epochs=20, batch=4096, lr=1e-3, seed=0, log=None):
         if log:
             log(ep, losses[-1])
     return losses
+
+
+class Surrogate:
+    """Colloid-only dynamics with the closure network (mpcd_surrogate_*)."""
+
+    def __init__(self, params, net):
+        L = lib()
+        vp, dp = C.c_void_p, C.POINTER(C.c_double)
+        from . import Params
+        L.mpcd_surrogate_create.argtypes = [C.POINTER(Params), vp, C.POINTER(vp)]
+        L.mpcd_surrogate_destroy.argtypes = [vp]
+        L.mpcd_surrogate_last_error.argtypes = [vp]
+        L.mpcd_surrogate_last_error.restype = C.c_char_p
+        L.mpcd_surrogate_set_state.argtypes = [vp, dp, dp, dp, dp]
+        L.mpcd_surrogate_get_state.argtypes = [vp, dp, dp, dp, dp]
+        L.mpcd_surrogate_features.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
+        L.mpcd_surrogate_step.argtypes = [vp, C.c_int]
+        self.params, self.net = params, net
+        self.Nc = params.n_colloid
+        h = vp()
+        r = L.mpcd_surrogate_create(C.byref(params), net.h, C.byref(h))
+        if r:
+            raise MPCDError(r, "mpcd_surrogate_create rejected the parameters")
+        self.h = h
+
+    def _ck(self, r):
+        if r:
+            raise MPCDError(r, lib().mpcd_surrogate_last_error(self.h).decode())
+
+    @staticmethod
+    def _dp(a):
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def set_state(self, pos, vel, ang_vel, ra):
+        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.Nc, 3) for x in (pos, vel, ang_vel, ra)]
+        self._ck(lib().mpcd_surrogate_set_state(self.h, *[self._dp(x) for x in a]))
+
+    def get_state(self):
+        out = {k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra")}
+        self._ck(lib().mpcd_surrogate_get_state(self.h, *[self._dp(out[k]) for k in
+                                                           ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra")]))
+        return out
+
+    def features(self, recompute=True):
+        out = np.empty((self.Nc, IN), dtype=np.float32)
+        self._ck(lib().mpcd_surrogate_features(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), 1 if recompute else 0))
+        return out
+
+    def step(self, nsteps=1):
+        self._ck(lib().mpcd_surrogate_step(self.h, nsteps))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpcd_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ statistics
+
+def unwrap(traj, L):
+    """(T, Nc, 3) wrapped positions -> unwrapped (minimum-image increments)."""
+    d = np.diff(traj, axis=0)
+    d -= L * np.round(d / L)
+    return np.concatenate([traj[:1], traj[:1] + np.cumsum(d, axis=0)])
+
+
+def msd(U, lags):
+    return np.array([np.mean(np.sum((U[lag:] - U[:-lag]) ** 2, axis=2)) for lag in lags])
+
+
+def autocorr(A, lags):
+    """<a(t) . a(t + lag)> over time origins and colloids."""
+    return np.array([np.mean(np.sum(A[lag:] * A[:len(A) - lag], axis=2)) if lag else np.mean(np.sum(A * A, axis=2))
+                     for lag in lags])
+
+
+def trajectory(stepper, getter, steps):
+    """Runs `steps` MPCD steps, recording colloid positions, velocities and orientations."""
+    X, V, R = [], [], []
+    for _ in range(steps):
+        stepper()
+        s = getter()
+        X.append(s["pos_colloid"].copy())
+        V.append(s["vel_colloid"].copy())
+        R.append(s["ra"].copy())
+    return np.array(X), np.array(V), np.array(R)
+
+
+# ------------------------------------------------------------------ end to end
+
+def _sim(p):
+    from . import Params
+    kw = {k: getattr(p, k) for k, _ in Params._fields_ if k not in ("Lx", "Ly", "Lz", "n_fluid", "n_colloid")}
+    return Simulation(p.Lx, p.n_fluid, p.n_colloid, **kw)
+
+
+def generate_gpu(params_list, steps, warmup=20, net=None):
+    """Samples from full MPCD runs, one per Params: the features (computed on the GPU by
+    the surrogate's feature kernel) at the start of every step and the exchange over it."""
+    Xs, Ys = [], []
+    feat_net = net if net is not None else Network(max_batch=max(p.n_colloid for p in params_list))
+    for p in params_list:
+        sim = _sim(p)
+        sim.initialize(INIT_PHYSICAL)
+        sim.setup()
+        sim.step(warmup)
+        sim.exchange(reset=True)
+        feat = Surrogate(p, feat_net)
+        for _ in range(steps):
+            c = sim.get_colloids()
+            feat.set_state(c["pos_colloid"], c["vel_colloid"], c["ang_vel_colloid"], c["ra"])
+            Xs.append(feat.features())
+            sim.step(1)
+            Ys.append(sim.exchange(reset=True).astype(np.float32))
+        feat.close()
+        sim.close()
+    if net is None:
+        feat_net.close()
+    return np.concatenate(Xs), np.concatenate(Ys)
+
+
+def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0, 1, 2, 5, 10, 20),
+            olags=(0, 10, 50, 100)):
+    """Full MPCD (the judge), the closure surrogate and colloid-only dynamics without any
+    fluid exchange, from the same colloid state: MSD, velocity and orientation
+    autocorrelations, and the time per MPCD step of the full run and of the surrogate."""
+    import time
+    full = _sim(p)
+    full.initialize(INIT_PHYSICAL)
+    full.setup()
+    full.step(warmup)
+    c0 = full.get_colloids()
+    t0 = time.perf_counter()
+    full.step(20)
+    full.get_colloids()
+    t_full = (time.perf_counter() - t0) / 20
+    runs = {"full": closure_traj(full, steps)}
+    full.close()
+    sur = Surrogate(p, net)
+    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    sur.step(5)
+    t0 = time.perf_counter()
+    sur.step(100)
+    t_sur = (time.perf_counter() - t0) / 100
+    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    runs["closure"] = closure_traj(sur, steps)
+    sur.close()
+    none_net = Network(max_batch=p.n_colloid)
+    none_net.set_normalisation(np.zeros(IN), np.ones(IN), np.zeros(NY), np.full(NY, 1e-20))
+    none_net.set_params(np.zeros(none_net.n_params))
+    bare = Surrogate(p, none_net)
+    bare.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    runs["no_closure"] = closure_traj(bare, steps)
+    bare.close()
+    none_net.close()
+    L = float(p.Lx)
+    out = {"t_full_ms": t_full * 1e3, "t_surrogate_ms": t_sur * 1e3, "speedup": t_full / t_sur}
+    stats = {}
+    for name, (X, V, R) in runs.items():
+        U = unwrap(X, L)
+        stats[name] = {"msd": msd(U, lags).tolist(), "vacf": autocorr(V, vlags).tolist(),
+                       "oacf": autocorr(R, olags).tolist()}
+    out["stats"] = stats
+    out["lags"] = {"msd": list(lags), "vacf": list(vlags), "oacf": list(olags)}
+    rel = {}
+    for name in ("closure", "no_closure"):
+        rel[name] = {k: (np.array(stats[name][k]) / np.array(stats["full"][k]) - 1.0).tolist()
+                     for k in ("msd", "vacf", "oacf")}
+    out["rel_diff_vs_full"] = rel
+    return out
+
+
+def closure_traj(obj, steps):
+    getter = obj.get_colloids if hasattr(obj, "get_colloids") else obj.get_state
+    return trajectory(lambda: obj.step(1), getter, steps)

@@ -349,10 +349,17 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.m_beta = p.mass_fl / p.kbt;
   S.inv_m_beta = p.kbt / p.mass_fl;
   S.cs = 3.0 * p.kbt * dt2 / p.mass_fl;
+  // run() gives each particle of a colloid's rear shell M v0 / (m cnt): with a shell of
+  // one particle (a colloid whose rear is blocked by another) that is M v0 / m.  The
+  // default speed bound of the exact cell sums covers it, and the cell-table reach
+  // covers a wall collision's displacement dt/2 (|v| + |v'|) at such speeds.
+  const double kick = p.n_colloid > 0 ? fabs(p.v0) * p.mass_colloid / p.mass_fl : 0.0;
+  const double vth = sqrt(p.kbt / p.mass_fl);
+  const double vmax = p.vmax > 0 ? p.vmax : 24.0 * vth + 2.0 * kick;
   // cell-table reach: sphere (or run() shell) + a wall collision's displacement
-  // (dt/2 (|v| + |v'|), 0.1 needs speeds near 20 kT units) + a colloid's move in one
-  // substep + FP32 slack; both displacements are checked on the device
-  const double pmargin = 0.1, cmargin = 0.05;
+  // (0.1 covers speeds near 20 kT units) + a colloid's move in one substep + FP32
+  // slack; both displacements are checked on the device
+  const double pmargin = fmax(0.1, 0.5 * dt * (2.0 * kick + 6.0 * vth)), cmargin = 0.05;
   S.r_coll = (float)(p.sigma * 0.5);
   S.r_shell = (float)(p.sigma * 0.5 + 0.5);
   S.rT_coll = (float)(p.sigma * 0.5 + pmargin + cmargin + 0.01);
@@ -361,7 +368,6 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.cmargin2 = cmargin * cmargin;
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
-  const double vmax = p.vmax > 0 ? p.vmax : 24.0 * sqrt(p.kbt / p.mass_fl);
   S.precision = p.precision;
   S.aux_nw = 4;
   S.dtf = (float)dt;

@@ -288,6 +288,8 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
     const uint16_t *lst = S.Tlist[buf] + (size_t)lin * TCAP;
     const int id = F.id[p];
     const f3 vdump = fm(vx, vy, vz);
+    const int cx0 = cx, cy0 = cy, cz0 = cz;
+    const float ox0 = ox, oy0 = oy, oz0 = oz;
     if (flags & F_COLLIDE) {
       for (int last = -1;;) {
         int j = 0x7FFFFFFF;
@@ -319,6 +321,12 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
         ox += 0.5f * vx * S.dtf; oy += 0.5f * vy * S.dtf; oz += 0.5f * vz * S.dtf;
         carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
       }
+    }
+    {
+      // the cell table is built with a margin; a move beyond it could hide a colloid
+      const float ex = rel(cx, ox, (float)cx0, ox0, S.Lx), ey = rel(cy, oy, (float)cy0, oy0, S.Ly),
+                  ez = rel(cz, oz, (float)cz0, oz0, S.Lz);
+      if (ex * ex + ey * ey + ez * ez > (float)S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
     }
     if (flags & F_SHELL) {
       ShellRec rec;

@@ -11,8 +11,9 @@
 //
 // One GEMM kernel serves every product: C[M x N] = A[M x K] B[K x N] with A and B
 // addressed through arbitrary strides (forward x W, backward dZ W^T and A^T dZ),
-// 64 x 64 block tiles, 32-wide K steps staged in shared memory, four warps of
-// 32 x 32 each, and a fused epilogue (bias, SiLU, the SiLU derivative of the
+// 32 x 64 block tiles, 32-wide K steps staged in shared memory through 16-byte
+// loads (the next tile prefetched into registers), four warps of 32 x 16 each,
+// and a fused epilogue (bias, SiLU, the SiLU derivative of the
 // backward pass, BF16 / FP32 stores, FP32 atomic accumulation for split-K
 // weight gradients).
 #include <cuda_bf16.h>
@@ -31,7 +32,11 @@ namespace {
 typedef __nv_bfloat16 bf16;
 
 constexpr int IN = MPCD_MLP_IN, INP = 96, H = MPCD_MLP_HIDDEN, OUT = MPCD_MLP_OUT, OUTP = 16, NY = OUT / 2;
-constexpr int BM = 64, BN = 64, BK = 32, PADK = BK + 8;
+constexpr int BM = 32, BN = 64, BK = 32;
+// normalised log-variances are used within [-6, 6] (variances between 0.0025 and 400 times
+// the target's): beyond that the likelihood's gradient is zero and inference clamps
+constexpr float kLogVarClamp = 6.f;
+constexpr float kInputClip = 6.f;
 
 struct Gemm {
   const bf16 *A;
@@ -64,74 +69,127 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Staging of one operand tile into shared memory as T[row][k] (rows: m for A, n for
+// B), 8 elements per 16-byte load along whichever dimension is contiguous in
+// memory (scalar loads where a vector would leave the matrix, is misaligned or
+// neither stride is 1).  ROWS x KT elements, 128 threads.
+template <int ROWS, int KT>
+struct Stage {
+  static constexpr int NV = ROWS * KT / 8 / 128;  // vectors per thread
+  uint4 v[NV];
+  __device__ __forceinline__ static void slot(int t, bool kfast, int &r, int &k) {
+    if (kfast) { r = t / (KT / 8); k = (t % (KT / 8)) * 8; }
+    else { k = t / (ROWS / 8); r = (t % (ROWS / 8)) * 8; }
+  }
+  __device__ __forceinline__ void load(const bf16 *base, long long rs, long long ks, int r0, int k0, int rmax, int kmax,
+                                       bool kfast) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      int r, k;
+      slot(threadIdx.x + 128 * i, kfast, r, k);
+      r += r0; k += k0;
+      const bf16 *p = base + r * rs + k * ks;
+      const bool full = kfast ? (r < rmax && k + 8 <= kmax) : (k < kmax && r + 8 <= rmax);
+      if (full && (kfast ? ks == 1 : rs == 1) && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+        v[i] = *reinterpret_cast<const uint4 *>(p);
+      } else {
+        bf16 e[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int rr = kfast ? r : r + q, kk = kfast ? k + q : k;
+          e[q] = (rr < rmax && kk < kmax) ? base[rr * rs + kk * ks] : __float2bfloat16(0.f);
+        }
+        v[i] = *reinterpret_cast<const uint4 *>(e);
+      }
+    }
+  }
+  template <int LD>
+  __device__ __forceinline__ void store(bf16 (*T)[LD], bool kfast) const {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      int r, k;
+      slot(threadIdx.x + 128 * i, kfast, r, k);
+      const bf16 *e = reinterpret_cast<const bf16 *>(&v[i]);
+      if (kfast) {
+        *reinterpret_cast<uint4 *>(&T[r][k]) = v[i];
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) T[r + q][k] = e[q];
+      }
+    }
+  }
+};
+
+// C tile TM x TN per block of 4 warps side by side along N (each TM x TN/4: TM/16
+// m16 by TN/32 n8 mma tiles), K in steps of TK; the next K tile is loaded into
+// registers while the current one is multiplied.  Two shapes: TK = 256 takes a
+// whole layer's K in one staging (inference-sized GEMMs: every load in flight at
+// once), TK = 32 streams long reductions (weight gradients over the batch).
+template <int TM, int TN, int TK>
 __global__ void __launch_bounds__(128) k_gemm(const Gemm g) {
-  __shared__ __align__(16) bf16 As[BM][PADK];
-  __shared__ __align__(16) bf16 Bs[BN][PADK];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  constexpr int LD = TK + 8, MT = TM / 16, NT = TN / 32;
+  __shared__ __align__(16) bf16 As[TM][LD];
+  __shared__ __align__(16) bf16 Bs[TN][LD];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
   const int kbeg = blockIdx.z * g.kchunk, kend = min(g.K, kbeg + g.kchunk);
-  float acc[2][4][4];
+  float acc[MT][NT][4];
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < MT; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-  const bf16 zero = __float2bfloat16(0.f);
   const bool a_kfast = g.sak == 1, b_kfast = g.sbk == 1;
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    // stage A[m0.., k0..] and B[k0.., n0..] (as Bs[n][k]), zero outside the matrices
-#pragma unroll 4
-    for (int e = 0; e < (BM * BK) / 128; ++e) {
-      const int idx = e * 128 + tid;
-      const int r = a_kfast ? idx / BK : idx % BM, kk = a_kfast ? idx % BK : idx / BM;
-      const int m = m0 + r, k = k0 + kk;
-      As[r][kk] = (m < g.M && k < kend) ? g.A[m * g.sam + k * g.sak] : zero;
-    }
-#pragma unroll 4
-    for (int e = 0; e < (BN * BK) / 128; ++e) {
-      const int idx = e * 128 + tid;
-      const int c = b_kfast ? idx / BK : idx % BN, kk = b_kfast ? idx % BK : idx / BN;
-      const int n = n0 + c, k = k0 + kk;
-      Bs[c][kk] = (n < g.N && k < kend) ? g.B[k * g.sbk + n * g.sbn] : zero;
-    }
+  Stage<TM, TK> sa;
+  Stage<TN, TK> sb;
+  if (kbeg < kend) {
+    sa.load(g.A, g.sam, g.sak, m0, kbeg, g.M, kend, a_kfast);
+    sb.load(g.B, g.sbn, g.sbk, n0, kbeg, g.N, kend, b_kfast);
+  }
+  const int gq = lane >> 2, q = lane & 3;
+  for (int k0 = kbeg; k0 < kend; k0 += TK) {
+    sa.store(As, a_kfast);
+    sb.store(Bs, b_kfast);
     __syncthreads();
-    const int gq = lane >> 2, q = lane & 3;
+    if (k0 + TK < kend) {
+      sa.load(g.A, g.sam, g.sak, m0, k0 + TK, g.M, kend, a_kfast);
+      sb.load(g.B, g.sbn, g.sbk, n0, k0 + TK, g.N, kend, b_kfast);
+    }
+    const int kspan = min(TK, kend - k0);
+#pragma unroll 4
+    for (int kk = 0; kk < kspan; kk += 16) {
+      uint32_t af[MT][4], bfr[NT][2];
 #pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r0 = wm * 32 + i * 16 + gq;
+      for (int i = 0; i < MT; ++i) {
+        const int r0 = i * 16 + gq;
         af[i][0] = *reinterpret_cast<const uint32_t *>(&As[r0][kk + q * 2]);
         af[i][1] = *reinterpret_cast<const uint32_t *>(&As[r0 + 8][kk + q * 2]);
         af[i][2] = *reinterpret_cast<const uint32_t *>(&As[r0][kk + q * 2 + 8]);
         af[i][3] = *reinterpret_cast<const uint32_t *>(&As[r0 + 8][kk + q * 2 + 8]);
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = wn * 32 + j * 8 + gq;
-        bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + q * 2]);
-        bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + q * 2 + 8]);
+      for (int j = 0; j < NT; ++j) {
+        const int cc = warp * (TN / 4) + j * 8 + gq;
+        bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[cc][kk + q * 2]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[cc][kk + q * 2 + 8]);
       }
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+      for (int i = 0; i < MT; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+        for (int j = 0; j < NT; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
     }
     __syncthreads();
   }
   // epilogue
-  const int gq = lane >> 2, q = lane & 3;
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < MT; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const int m = m0 + wm * 32 + i * 16 + gq + (r >= 2 ? 8 : 0);
-        const int n = n0 + wn * 32 + j * 8 + q * 2 + (r & 1);
+        const int m = m0 + i * 16 + gq + (r >= 2 ? 8 : 0);
+        const int n = n0 + warp * (TN / 4) + j * 8 + q * 2 + (r & 1);
         if (m >= g.M || n >= g.N) continue;
         float v = acc[i][j][r];
         if (g.Cacc) {
@@ -150,12 +208,15 @@ __global__ void __launch_bounds__(128) k_gemm(const Gemm g) {
       }
 }
 
-// raw features [n][IN] -> normalised BF16 [n][INP] (zero padded)
+// raw features [n][IN] -> normalised BF16 [n][INP] (zero padded), clipped to six
+// standard deviations so that inputs far outside the training data (a colloid the
+// dynamics has thrown) meet the network's behaviour at the edge of that data
 __global__ void k_features_in(const float *x, int n, const float *mean, const float *istd, bf16 *out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)n * INP) return;
   const int r = (int)(i / INP), c = (int)(i % INP);
-  out[i] = __float2bfloat16(c < IN ? (x[(long long)r * IN + c] - mean[c]) * istd[c] : 0.f);
+  const float z = c < IN ? (x[(long long)r * IN + c] - mean[c]) * istd[c] : 0.f;
+  out[i] = __float2bfloat16(fminf(fmaxf(z, -kInputClip), kInputClip));
 }
 
 // Gaussian negative log-likelihood of normalised targets under (mean, log-variance)
@@ -170,7 +231,7 @@ __global__ void k_nll(const float *o, const float *y, int n, const float *ymean,
       const float t = (y[r * NY + k] - ymean[k]) * yistd[k];
       const float mu = o[r * OUTP + k];
       const float sraw = o[r * OUTP + NY + k];
-      const float s = fminf(fmaxf(sraw, -12.f), 12.f);
+      const float s = fminf(fmaxf(sraw, -kLogVarClamp), kLogVarClamp);
       const float e = __expf(-s), d = t - mu;
       l += 0.5f * (d * d * e + s);
       dout[r * OUTP + k] = __float2bfloat16(-d * e * inv);
@@ -195,7 +256,8 @@ __global__ void k_denorm(const float *o, int n, const float *ymean, const float 
   if (i >= n * OUT) return;
   const int r = i / OUT, k = i % OUT;
   const float v = o[r * OUTP + k];
-  out[i] = k < NY ? v / yistd[k] + ymean[k] : v - 2.f * __logf(yistd[k - NY]);
+  out[i] = k < NY ? v / yistd[k] + ymean[k]
+                  : fminf(fmaxf(v, -kLogVarClamp), kLogVarClamp) - 2.f * __logf(yistd[k - NY]);
 }
 
 // column sums of a BF16 matrix into FP32 (bias gradients), one atomic per (block, column)
@@ -300,10 +362,17 @@ T *dalloc(mpcd_mlp *n, size_t count) {
 }
 
 void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
+  if (g.K <= 256 && ksplit == 1) {
+    // whole K in one staging, 32 x 32 tiles: many blocks for inference-sized M
+    g.kchunk = g.K;
+    dim3 grid((g.N + 31) / 32, (g.M + 31) / 32, 1);
+    k_gemm<32, 32, 256><<<grid, 128, 0, s>>>(g);
+    return;
+  }
   g.kchunk = ksplit > 1 ? ((g.K + ksplit - 1) / ksplit + BK - 1) / BK * BK : g.K;
   const int kz = ksplit > 1 ? (g.K + g.kchunk - 1) / g.kchunk : 1;
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, kz);
-  k_gemm<<<grid, 128, 0, s>>>(g);
+  k_gemm<BM, BN, BK><<<grid, 128, 0, s>>>(g);
 }
 
 Gemm base() {

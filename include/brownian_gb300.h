@@ -206,6 +206,28 @@ int mpcd_mlp_grad(mpcd_mlp *n, const float *x, const float *y, int rows, float *
 /* one Adam step (beta 0.9, 0.999) on the batch; loss_host receives the batch loss before the step */
 int mpcd_mlp_train_step(mpcd_mlp *n, const float *x, const float *y, int rows, float lr, double *loss_host);
 
+/* ---- colloid-only dynamics with the learned closure (no counterpart in the reference) -- */
+/* The colloids of p (box, n_colloid <= MPCD_SURROGATE_MAX_COLLOIDS, n_sub, ndt, masses, WCA
+ * sig_colloid/eps, sphere diameter sigma, v0, Dr, seed; n_fluid ignored) without the fluid:
+ * each MPCD step the network `net` (max_batch >= n_colloid; borrowed, not owned) predicts
+ * every colloid's fluid exchange, a Gaussian draw of it is applied as an impulse together with
+ * run()'s active kick, then n_sub velocity-Verlet substeps with WCA forces and the orientation
+ * update, in FP32 (one CUDA graph per step). */
+#define MPCD_SURROGATE_MAX_COLLOIDS 2048
+typedef struct mpcd_surrogate mpcd_surrogate;
+int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_surrogate **out);
+int mpcd_surrogate_destroy(mpcd_surrogate *s);
+const char *mpcd_surrogate_last_error(const mpcd_surrogate *s);
+/* state as n_colloid x 3 doubles (host); set_state also computes the forces */
+int mpcd_surrogate_set_state(mpcd_surrogate *s, const double *pos, const double *vel, const double *ang_vel,
+                             const double *ra);
+int mpcd_surrogate_get_state(mpcd_surrogate *s, double *pos, double *vel, double *ang_vel, double *ra);
+/* the network inputs of the current state (n_colloid x 81 floats, host): computed afresh
+ * (recompute != 0) or as the last step left them for the next one */
+int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recompute);
+/* nsteps MPCD steps; synchronises */
+int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps);
+
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their
  * own pool (for example a framework's caching allocator that already holds the GPU), or

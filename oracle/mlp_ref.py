@@ -50,7 +50,7 @@ def loss_and_grad(p, x, y, xmean, xstd, ymean, ystd, bf16_emul=True, dtype=np.fl
     n = x.shape[0]
     xs = np.where(xstd > 0, 1.0 / np.where(xstd > 0, xstd, 1.0), 0.0).astype(dtype)
     ys = np.where(ystd > 0, 1.0 / np.where(ystd > 0, ystd, 1.0), 0.0).astype(dtype)
-    a = r((x - xmean) * xs)
+    a = r(np.clip((x - xmean) * xs, -6, 6))
     acts, zs = [a], []
     for l, (W, b) in enumerate(layers):
         z = a @ W + b
@@ -62,7 +62,7 @@ def loss_and_grad(p, x, y, xmean, xstd, ymean, ystd, bf16_emul=True, dtype=np.fl
             o = z
     t = (y - ymean) * ys
     mu, sraw = o[:, :NY], o[:, NY:]
-    s = np.clip(sraw, -12, 12)
+    s = np.clip(sraw, -6, 6)
     e = np.exp(-s)
     d = t - mu
     loss = float(np.sum(0.5 * (d * d * e + s)) / n)
@@ -85,8 +85,8 @@ def loss_and_grad(p, x, y, xmean, xstd, ymean, ystd, bf16_emul=True, dtype=np.fl
 def forward(p, x, xmean, xstd, ymean, ystd, dtype=np.float64):
     """Outputs in physical units: means (6) and log-variances (6)."""
     layers = [(np.asarray(W, dtype), np.asarray(b, dtype)) for W, b in unflatten(np.asarray(p, dtype))]
-    a = (x - xmean) / np.where(xstd > 0, xstd, np.inf)
+    a = np.clip((x - xmean) / np.where(xstd > 0, xstd, np.inf), -6, 6)
     for l, (W, b) in enumerate(layers):
         z = a @ W + b
         a = z * sig(z) if l < 3 else z
-    return np.concatenate([a[:, :NY] * ystd + ymean, a[:, NY:] + 2 * np.log(ystd)], axis=1)
+    return np.concatenate([a[:, :NY] * ystd + ymean, np.clip(a[:, NY:], -6, 6) + 2 * np.log(ystd)], axis=1)

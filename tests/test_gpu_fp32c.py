@@ -101,3 +101,20 @@ def test_routine_calls_equal_fused_step_fp32c():
     sa, sb = a.get_state(), b.get_state()
     for k in sa:
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_strongly_active_colloids_stay_in_range():
+    """v0 = 0.1: run() can give a rear-shell particle the colloid's whole kick M v0 / m
+    (a shell of one particle when another colloid blocks the rear); the default speed
+    bound and cell-table reach follow from that (this system once overran them at step 80)."""
+    import brownian_gb300 as bg
+    M = bg.displaced_mass(2.0, 10)
+    sim = bg.Simulation(64, 64 ** 3 * 10, 500, n_sub=10, mass_colloid=M, sig_colloid=4.0, sigma=4.0,
+                        I_colloid=0.4 * M * 4.0, v0=0.1, theta_deg=90.0, Dr=0.001, seed=14, precision=bg.FP32C)
+    sim.initialize(bg.INIT_PHYSICAL)
+    sim.setup()
+    sim.step(150)
+    d = sim.diag()
+    # the active kicks feed energy that the cell thermostat removes only at the next rotation
+    assert 0.9 < d["temperature_fluid"] < 1.2
+    sim.close()
