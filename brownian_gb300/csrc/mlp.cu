@@ -26,17 +26,19 @@
 #include <vector>
 
 #include "../../include/brownian_gb300.h"
+#include "mlp_internal.h"
 
 namespace {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int IN = MPCD_MLP_IN, INP = 96, H = MPCD_MLP_HIDDEN, OUT = MPCD_MLP_OUT, OUTP = 16, NY = OUT / 2;
+constexpr int IN = MPCD_MLP_IN, INP = MLP_IN_PADDED, H = MPCD_MLP_HIDDEN, OUT = MPCD_MLP_OUT, OUTP = MLP_OUT_PADDED,
+              NY = OUT / 2;
 constexpr int BM = 32, BN = 64, BK = 32;
 // normalised log-variances are used within [-6, 6] (variances between 0.0025 and 400 times
 // the target's): beyond that the likelihood's gradient is zero and inference clamps
-constexpr float kLogVarClamp = 6.f;
-constexpr float kInputClip = 6.f;
+constexpr float kLogVarClamp = MLP_LOGVAR_CLAMP;
+constexpr float kInputClip = MLP_INPUT_CLIP;
 
 struct Gemm {
   const bf16 *A;
@@ -595,3 +597,17 @@ extern "C" int mpcd_mlp_train_step(mpcd_mlp *nn, const float *x, const float *y,
                                               nn->w[0], nn->w[1], nn->w[2], nn->w[3], nn->bias);
   return cudaGetLastError() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "adam launch");
 }
+
+MlpIO mlp_io(mpcd_mlp *nn) {
+  MlpIO io;
+  io.X = nn->X;
+  io.xmean = nn->xmean; io.xistd = nn->xistd;
+  io.O = nn->O;
+  io.ymean = nn->ymean; io.yistd = nn->yistd;
+  io.max_batch = nn->max_batch;
+  return io;
+}
+
+int mlp_stage(mpcd_mlp *nn, const float *x, int rows, cudaStream_t s) { return stage_inputs(nn, x, rows, s); }
+
+void mlp_layers(mpcd_mlp *nn, int rows, cudaStream_t s) { forward(nn, rows, s); }

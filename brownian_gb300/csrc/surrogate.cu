@@ -19,6 +19,7 @@
 
 #include "../../include/brownian_gb300.h"
 #include "common.cuh"
+#include "mlp_internal.h"
 
 namespace {
 
@@ -40,6 +41,7 @@ struct Sur {
   float4 *xref;     // positions at the last neighbour-list build
   int *built;       // a list exists
   int *err;
+  const float *On, *ymean, *yistd;  // the network's normalised outputs and their normalisation
 };
 
 __device__ __forceinline__ float wrapd(float d, float L, float iL) { return d - L * rintf(d * iL); }
@@ -125,19 +127,19 @@ __device__ __forceinline__ float3 wca_pair(const Sur &S, float dx, float dy, flo
   return make_float3(mag * dx * ir, mag * dy * ir, mag * dz * ir);
 }
 
-// One MPCD step of every colloid in one block (MAXC / 1024 colloids per thread,
+// One MPCD step of every colloid in one block (one or two colloids per thread,
 // their velocity, angular velocity, orientation and force in registers, all
 // positions and velocities in shared memory):
-//   the fluid's exchange drawn from the network's Gaussian (S.out), applied in equal
+//   the fluid's exchange drawn from the network's Gaussian (its outputs S.On), applied in equal
 //   parts after each substep's position update, and run()'s kick at the start;
 //   the neighbour list (pairs within three radii plus a skin), rebuilt only when a
 //   colloid has moved more than half the skin since the last build;
 //   n_sub substeps of update_pos_md, update_activity_direction, compute_force_md,
 //   update_velocity_colloid;
 //   the network inputs of the next step (S.feat).
-constexpr int PER = MAXC / 1024;
 constexpr int MAXF = 24;  // force partners per colloid (within the WCA cutoff plus the skin)
 
+template <int PER>  // colloids per thread: 1 up to 1024 colloids, 2 up to MAXC
 __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
   extern __shared__ float4 smem[];
   float4 *sX = smem, *sV = smem + MAXC;
@@ -157,14 +159,19 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
     sX[j] = x;
     v[u] = S.V[j]; w[u] = S.W[j]; a[u] = S.ra[j]; fo[u] = S.f[j];
     // the exchange and the active kick
-    const float *o = S.out + (size_t)j * NO;
+    // the network's normalised outputs -> mean and standard deviation in physical units
+    const float *o = S.On + (size_t)j * MLP_OUT_PADDED;
     const uint4 r0 = draw4(S.key, DOM_SUR_KICK, 0, (uint32_t)(j + 1), 0, step);
     const uint4 r1 = draw4(S.key, DOM_SUR_KICK, 1, (uint32_t)(j + 1), 0, step);
     const float2 g0 = normal2(r0.x, r0.y), g1 = normal2(r0.z, r0.w), g2 = normal2(r1.x, r1.y);
     const float xi[6] = {g0.x, g0.y, g1.x, g1.y, g2.x, g2.y};
     float dp[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) dp[k] = o[k] + __expf(0.5f * o[6 + k]) * xi[k];
+    for (int k = 0; k < 6; ++k) {
+      const float is = S.yistd[k];
+      const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
+      dp[k] = (o[k] + __expf(0.5f * lv) * xi[k]) / is + S.ymean[k];
+    }
     // the exchange arrives over the step's substeps (the fluid collides every substep),
     // the active kick at its start (run())
     const float fm = 1.f / (S.M * S.n_sub), fi = 1.f / (S.I * S.n_sub);
@@ -284,33 +291,39 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
+    // the nearest KNEAR as (d2, k) in registers: every candidate is passed down a
+    // fully unrolled chain of compare-and-swap, nearest (then lowest index) first
     float bd[KNEAR];
     int bk[KNEAR];
-    int cnt = 0;
+#pragma unroll
+    for (int m = 0; m < KNEAR; ++m) { bd[m] = 3.0e38f; bk[m] = 0x7FFFFFFF; }
     const float4 xj = sX[j];
     const int n = S.nnb[j];
     for (int e = 0; e < n; ++e) {
-      const int k = S.nbr[j * MAXNB + e];
+      int k = S.nbr[j * MAXNB + e];
       const float4 xk = sX[k];
       const float dx = wrapd(xk.x - xj.x, S.L[0], S.iL[0]), dy = wrapd(xk.y - xj.y, S.L[1], S.iL[1]),
                   dz = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
-      const float d2 = dx * dx + dy * dy + dz * dz;
+      float d2 = dx * dx + dy * dy + dz * dz;
       if (!(d2 < S.ct_feat2)) continue;
-      // insert (d2, k) into the sorted list of the nearest KNEAR
-      int pos = cnt;
-      while (pos > 0 && (bd[pos - 1] > d2 || (bd[pos - 1] == d2 && bk[pos - 1] > k))) {
-        if (pos < KNEAR) { bd[pos] = bd[pos - 1]; bk[pos] = bk[pos - 1]; }
-        --pos;
+#pragma unroll
+      for (int m = 0; m < KNEAR; ++m) {
+        const bool less = d2 < bd[m] || (d2 == bd[m] && k < bk[m]);
+        const float td = less ? bd[m] : d2;
+        const int tk = less ? bk[m] : k;
+        bd[m] = less ? d2 : bd[m];
+        bk[m] = less ? k : bk[m];
+        d2 = td;
+        k = tk;
       }
-      if (pos < KNEAR) { bd[pos] = d2; bk[pos] = k; }
-      if (cnt < KNEAR) ++cnt;
     }
     float *o = S.feat + (size_t)j * NF;
     o[0] = v[u].x; o[1] = v[u].y; o[2] = v[u].z; o[3] = w[u].x; o[4] = w[u].y; o[5] = w[u].z;
     o[6] = a[u].x; o[7] = a[u].y; o[8] = a[u].z;
+#pragma unroll
     for (int m = 0; m < KNEAR; ++m) {
       float *q = o + 9 + 6 * m;
-      if (m < cnt) {
+      if (bk[m] != 0x7FFFFFFF) {
         const float4 xk = sX[bk[m]], vk = sV[bk[m]];
         q[0] = wrapd(xk.x - xj.x, S.L[0], S.iL[0]); q[1] = wrapd(xk.y - xj.y, S.L[1], S.iL[1]);
         q[2] = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
@@ -379,9 +392,11 @@ constexpr size_t kSmem = 2 * MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16
 int enqueue_step(mpcd_surrogate *s) {
   const Sur &S = s->S;
   // S.feat holds the current state's network inputs (set_state, or the previous step)
-  int r = mpcd_mlp_forward(s->net, S.feat, S.Nc, S.out, s->stream);
+  int r = mlp_stage(s->net, S.feat, S.Nc, s->stream);
   if (r) return sfail(s, r, std::string("closure network: ") + mpcd_mlp_last_error(s->net));
-  k_sur_md<<<1, 1024, kSmem, s->stream>>>(S);
+  mlp_layers(s->net, S.Nc, s->stream);
+  if (S.Nc <= 1024) k_sur_md<1><<<1, 1024, kSmem, s->stream>>>(S);
+  else k_sur_md<2><<<1, 1024, kSmem, s->stream>>>(S);
   return MPCD_OK;
 }
 
@@ -393,10 +408,15 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   if (p->n_colloid < 1 || p->n_colloid > MAXC || p->n_sub < 1 || !(p->ndt > 0) || !(p->mass_colloid > 0) ||
       !(p->I_colloid > 0) || p->Lx < 1 || p->Ly < 1 || p->Lz < 1)
     return MPCD_ERR_PARAM;
+  if (mlp_io(net).max_batch < p->n_colloid) return MPCD_ERR_CAPACITY;
   mpcd_surrogate *s = new mpcd_surrogate();
   s->net = net;
   Sur &S = s->S;
   memset(&S, 0, sizeof S);
+  const MlpIO io = mlp_io(net);
+  S.On = io.O;
+  S.ymean = io.ymean;
+  S.yistd = io.yistd;
   S.Nc = p->n_colloid;
   S.n_sub = p->n_sub;
   const int Ls[3] = {p->Lx, p->Ly, p->Lz};
@@ -434,7 +454,8 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   S.xref = salloc<float4>(s, Nc); S.built = salloc<int>(s, 1);
   S.err = salloc<int>(s, 1);
   if (!s->err.empty() || cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaFuncSetAttribute(k_sur_md, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess) {
+      cudaFuncSetAttribute(k_sur_md<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess) {
     mpcd_surrogate_destroy(s);
     return MPCD_ERR_NOMEM;
   }
