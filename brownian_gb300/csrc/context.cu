@@ -172,7 +172,7 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
     cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
   }
   launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags),
-         blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread() : 1)), 256, c->S, l, fb);
+         blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread() : stream64_per_thread(flags))), 256, c->S, l, fb);
   if (fork) {
     launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act);
     cudaEventRecord(c->ev_join, c->aux);

@@ -53,97 +53,131 @@ __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double 
 // shell, or sits in an aliased cell) goes to the event list, which k_events then
 // processes with the reference's exact FP64 arithmetic, one event per lane; all
 // other particles finish here (shell record, SRD binning on the last substep).
+// U particles per thread (thread t of block b: particles b * 256 U + t + 256 u),
+// their loads issued together so more memory requests are in flight.  The pass
+// that also lists run() shell members keeps more state per particle and one
+// particle per thread, for its register count.
+#ifndef STREAM64_U
+#define STREAM64_U 2
+#endif
+#ifndef STREAM64_U_SHELL
+#define STREAM64_U_SHELL 1
+#endif
+static constexpr __host__ __device__ int stream64_u(int flags) { return (flags & F_SHELL) ? STREAM64_U_SHELL : STREAM64_U; }
 template <int FLAGS>
 __global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int fb) {
   constexpr int flags = FLAGS;
+  constexpr int U = stream64_u(FLAGS);
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const Fluid F = fluid_at(S, fb);
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = p < S.N;
+  const int p0 = blockIdx.x * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
-  bool ev = false;
-  unsigned members = 0;  // run() shell members among the cell-table slots
-  const uint16_t *lst = nullptr;
-  int cnt = 0;
-  if (valid) {
-    double x = F.x[p], y = F.y[p], z = F.z[p];
-    double wx = 0, wy = 0, wz = 0;
-    if (flags & (F_STREAM | F_BINROT)) { wx = F.wx[p]; wy = F.wy[p]; wz = F.wz[p]; }
+  double x[U], y[U], z[U], wx[U], wy[U], wz[U];
+  bool valid[U], ev[U];
+  unsigned members[U];  // run() shell members among the cell-table slots
+  int cnt[U], lin[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    valid[u] = p < S.N;
+    ev[u] = false;
+    members[u] = 0;
+    cnt[u] = 0;
+    lin[u] = 0;
+    wx[u] = wy[u] = wz[u] = 0;
+    if (valid[u]) {
+      x[u] = F.x[p]; y[u] = F.y[p]; z[u] = F.z[p];
+      if (flags & (F_STREAM | F_BINROT)) { wx[u] = F.wx[p]; wy[u] = F.wy[p]; wz[u] = F.wz[p]; }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
     if (flags & F_STREAM) {
       // update_pos_mpcd: pos = mod(pos + vel*dt, len)   cpp/update.cpp:56-60
-      x = ref_mod(__dadd_rn(x, wx), S.dx);
-      y = ref_mod(__dadd_rn(y, wy), S.dy);
-      z = ref_mod(__dadd_rn(z, wz), S.dz);
+      x[u] = ref_mod(__dadd_rn(x[u], wx[u]), S.dx);
+      y[u] = ref_mod(__dadd_rn(y[u], wy[u]), S.dy);
+      z[u] = ref_mod(__dadd_rn(z[u], wz[u]), S.dz);
     }
     if (flags & (F_COLLIDE | F_SHELL)) {
       bool alias;
-      int lin = cell_of_pos(S, x, y, z, alias);
-      ev = alias;
-      if (!alias) {
-        cnt = tcount(S.Tcnt[buf][lin], gs);
-        if (cnt > 0) {
-          cnt = cnt < TCAP ? cnt : TCAP;
-          lst = S.Tlist[buf] + (size_t)lin * TCAP;
-          const float4 *Xf = S.Xf[buf];
-          const float px = d2f_trunc(x), py = d2f_trunc(y), pz = d2f_trunc(z);
-          const float ch = S.r_coll + 1e-3f, sl = S.r_shell - 1e-3f, sh = S.r_shell + 1e-3f;
-          for (int k = 0; k < cnt; ++k) {
-            float4 c = Xf[lst[k]];
-            float dx = wrap_half(c.x - px, S.Lxf), dy = wrap_half(c.y - py, S.Lyf), dz = wrap_half(c.z - pz, S.Lzf);
-            float d2 = dx * dx + dy * dy + dz * dz;
-            if (flags & F_COLLIDE) ev |= d2 <= ch * ch;
-            if (flags & F_SHELL) {
-              if (d2 < sl * sl) members |= 1u << k;
-              else ev |= d2 <= sh * sh;
-            }
-          }
+      lin[u] = cell_of_pos(S, x[u], y[u], z[u], alias);
+      ev[u] = alias;
+      if (!alias) cnt[u] = tcount(S.Tcnt[buf][lin[u]], gs);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
+    if ((flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
+      cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
+      const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+      const float4 *Xf = S.Xf[buf];
+      const float px = d2f_trunc(x[u]), py = d2f_trunc(y[u]), pz = d2f_trunc(z[u]);
+      const float ch = S.r_coll + 1e-3f, sl = S.r_shell - 1e-3f, sh = S.r_shell + 1e-3f;
+      for (int k = 0; k < cnt[u]; ++k) {
+        const float4 c = Xf[lst[k]];
+        const float dx = wrap_half(c.x - px, S.Lxf), dy = wrap_half(c.y - py, S.Lyf), dz = wrap_half(c.z - pz, S.Lzf);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (flags & F_COLLIDE) ev[u] |= d2 <= ch * ch;
+        if (flags & F_SHELL) {
+          if (d2 < sl * sl) members[u] |= 1u << k;
+          else ev[u] |= d2 <= sh * sh;
         }
       }
     }
-    if (!ev && (flags & F_BINROT)) bin_for_rotation(S, p, x, y, z, wx, wy, wz);
-    if (flags & F_STREAM) { F.x[p] = x; F.y[p] = y; F.z[p] = z; }
+    const int p = p0 + 256 * u;
+    if (!ev[u] && (flags & F_BINROT)) bin_for_rotation(S, p, x[u], y[u], z[u], wx[u], wy[u], wz[u]);
+    if (flags & F_STREAM) { F.x[p] = x[u]; F.y[p] = y[u]; F.z[p] = z[u]; }
   }
   // appends: events one atomic per warp (no block barrier), run() candidate
   // records (last substep) one atomic per block
   const int lane = threadIdx.x & 31;
-  const bool has_rec = (flags & F_SHELL) && !ev && members != 0;
-  const unsigned mev = __ballot_sync(FULL, ev), mrec = __ballot_sync(FULL, has_rec);
-  int bev = 0, brec = 0;
-  if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
-  bev = __shfl_sync(FULL, bev, 0);
-  if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
   const unsigned lt = (1u << lane) - 1u;
-  if (ev) {
-    int i = bev + __popc(mev & lt);
-    if (i < S.events_cap) S.events[i] = p;
-    else atomicOr(&S.ss->err, ERRB_SHELL);
-  }
-  if (has_rec) {
-    int i = brec + __popc(mrec & lt);
-    if (i < S.shell_cap) {
-      // colloids in ascending index, the order run() visits them
-      ShellRec *r = S.shell + i;
-      r->p = F.id[p];
-      r->pass = 0;
-      int n = 0, last = -1;
-      for (int it = 0; it < cnt && n < SHELL_J; ++it) {
-        int best = 0x7FFFFFFF;
-        for (int k = 0; k < cnt; ++k) {
-          int j = lst[k];
-          if (((members >> k) & 1u) && j > last && j < best) best = j;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    const bool has_rec = (flags & F_SHELL) && valid[u] && !ev[u] && members[u] != 0;
+    const unsigned mev = __ballot_sync(FULL, ev[u]), mrec = __ballot_sync(FULL, has_rec);
+    int bev = 0, brec = 0;
+    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
+    bev = __shfl_sync(FULL, bev, 0);
+    if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
+    if (ev[u]) {
+      const int i = bev + __popc(mev & lt);
+      if (i < S.events_cap) S.events[i] = p;
+      else atomicOr(&S.ss->err, ERRB_SHELL);
+    }
+    if (has_rec) {
+      const int i = brec + __popc(mrec & lt);
+      if (i < S.shell_cap) {
+        // colloids in ascending index, the order run() visits them
+        const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+        ShellRec *r = S.shell + i;
+        r->p = F.id[p];
+        r->pass = 0;
+        int n = 0, last = -1;
+        for (int it = 0; it < cnt[u] && n < SHELL_J; ++it) {
+          int best = 0x7FFFFFFF;
+          for (int k = 0; k < cnt[u]; ++k) {
+            const int j = lst[k];
+            if (((members[u] >> k) & 1u) && j > last && j < best) best = j;
+          }
+          if (best == 0x7FFFFFFF) break;
+          r->j[n++] = (uint16_t)best;
+          last = best;
         }
-        if (best == 0x7FFFFFFF) break;
-        r->j[n++] = (uint16_t)best;
-        last = best;
+        if (__popc(members[u]) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
+        r->n = (uint8_t)n;
+      } else {
+        atomicOr(&S.ss->err, ERRB_SHELL);
       }
-      if (__popc(members) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
-      r->n = (uint8_t)n;
-    } else {
-      atomicOr(&S.ss->err, ERRB_SHELL);
     }
   }
 }
+
+int stream64_per_thread(int flags) { return stream64_u(flags); }
 
 // The particles the streaming pass listed: wall collisions in colloid order with
 // the reference's exact arithmetic (and, on the last substep, their run() record
