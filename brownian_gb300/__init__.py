@@ -286,7 +286,8 @@ class Simulation:
 
     def set_launch(self, which, grid=0, block=32):
         """Launch shape of the event (LAUNCH_EVENTS) or colloid-finish (LAUNCH_FIN)
-        kernel; grid 0 is the default, one block per SM."""
+        kernel; grid 0 is the default, one block per SM (128 threads for the events,
+        32 for the finish)."""
         self._ck(lib().mpcd_set_launch(self.h, which, grid, block))
 
     @property

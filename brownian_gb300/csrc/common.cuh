@@ -42,8 +42,32 @@ __device__ __host__ __forceinline__ uint4 draw4(uint2 key, uint32_t dom, uint32_
   return philox(make_uint4(a, b, t, (dom << 24) | (blk & 0xFFFFFFu)), key);
 }
 
-// uniform in (0,1): (w + 1/2) 2^-32, exact in double
-__device__ __host__ __forceinline__ double u01(uint32_t w) { return ((double)w + 0.5) * 2.3283064365386963e-10; }
+// The double v 2^-k for an odd v < 2^53 (negated if neg), assembled on the
+// integer pipe: the leading-bit position b of v gives the exponent, v shifted up
+// to bit 52 the mantissa.  Exact (v has at most 53 significant bits).
+__device__ __forceinline__ double odd_scaled(unsigned long long v, int k, bool neg) {
+  const int b = 63 - __clzll((long long)v);
+  const unsigned long long bits =
+      ((unsigned long long)(1023 + b - k) << 52) | ((v << (52 - b)) & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)(bits | (neg ? 0x8000000000000000ull : 0ull)));
+}
+
+// uniform in (0,1): (w + 1/2) 2^-32 = (2w + 1) 2^-33, exact in double.  The device
+// assembles it from bits: a GB300 SM runs one FP64 instruction of a warp per ~64
+// cycles, the integer form costs a few cycles; both give the same double.
+__device__ __host__ __forceinline__ double u01(uint32_t w) {
+#ifdef __CUDA_ARCH__
+  return odd_scaled(2ull * w + 1ull, 33, false);
+#else
+  return ((double)w + 0.5) * 2.3283064365386963e-10;
+#endif
+}
+
+// 2 u01(w) - 1 = (2w + 1 - 2^32) 2^-32, exact (the reference's 2 ran - 1)
+__device__ __forceinline__ double pm1(uint32_t w) {
+  const long long n = 2ll * (long long)w + 1ll - 4294967296ll;  // odd, |n| < 2^32
+  return odd_scaled((unsigned long long)(n < 0 ? -n : n), 32, n < 0);
+}
 
 // ------------------------------------------------------------- exact FP64 helpers
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }

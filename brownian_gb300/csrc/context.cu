@@ -74,7 +74,7 @@ struct mpcd_ctx {
   int next_sub = 1;              // routine-level: the substep mpcd_substep expects
   int nblk = 0;                  // 256-cell blocks of the counting sort
   int n_sm = 152;                // multiprocessors of the device
-  int ev_grid = 0, ev_block = 32;    // k_events launch shape (grid 0: one block per SM)
+  int ev_grid = 0, ev_block = 128;   // k_events launch shape (grid 0: one block per SM)
   int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
 };
 
@@ -424,6 +424,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.shell = m.get<ShellRec>(S.shell_cap);
   S.events_cap = S.N / 16 + 65536;
   S.events = m.get<int>(S.events_cap);
+  S.evrec = S.precision == MPCD_FP64 ? m.get<EventRec>(S.events_cap) : nullptr;
   S.ss = m.get<StepState>(1);
   c->inv_n = m.get<double>(S.max_per_cell + 1);
   S.inv_n = c->inv_n;
@@ -677,7 +678,7 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
     return fail(c, MPCD_ERR_PARAM, "launch shape: block a multiple of 32 in [32, 128], grid <= 65535");
   if (which == MPCD_LAUNCH_EVENTS) {
     c->ev_grid = grid > 0 ? grid : 0;
-    c->ev_block = grid > 0 ? block : 32;
+    c->ev_block = grid > 0 ? block : 128;
   } else if (which == MPCD_LAUNCH_FIN) {
     c->fin_grid = grid > 0 ? grid : 0;
     c->fin_block = grid > 0 ? block : 32;

@@ -129,13 +129,56 @@ static __device__ __forceinline__ float wrap_half(float d, float L) {
 
 // ----------------------------------------------------------- exact exchange sums
 
-static __device__ __forceinline__ void exch_add(ExchAcc *e, int comp, double v, int *err) {
-  if ((dbits(v) & 0x7FFFFFFFFFFFFFFFll) >= 0x4130000000000000ll) atomicOr(err, ERRB_DELTA);  // |v| >= 2^20
-  long long hi = to_fix(v, 20);
-  double res = __dsub_rn(v, (double)hi * 0x1p-20);
-  long long lo = to_fix(res, 72);
-  atomicAdd((unsigned long long *)&e->hi[comp], (unsigned long long)hi);
-  atomicAdd((unsigned long long *)&e->lo[comp], (unsigned long long)lo);
+// One exchange component split as hi = to_fix(v, 20), lo = to_fix(res, 72) with
+// res = v - hi 2^-20 (exact in FP64), computed on the integer pipe only.  With
+// v = +-M 2^E (M the 53-bit significand) and T = E + 72: for T >= 0, v 2^72 is an
+// integer and lo = v 2^72 - hi 2^52 exactly, a difference that fits 64 bits, so
+// wrap-around arithmetic gives it; for T < 0, |v| < 2^-19, hi is 0 (or +-1 when
+// T = -1) and lo = round_half_even((+-M - hi 2^(52-T)) 2^T).  Denormals give 0, as
+// to_fix does.  |v| < 2^20 (checked by the caller) keeps T <= 40.
+static __device__ __forceinline__ void exch_split(double v, long long &hi, long long &lo) {
+  const long long b = dbits(v);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  hi = to_fix(v, 20);
+  const unsigned long long M = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int T = ex - 1075 + 72;
+  const bool neg = b < 0;
+  if (ex == 0) {
+    lo = 0;
+  } else if (T >= 0) {
+    const unsigned long long X = T < 64 ? M << T : 0ull;
+    lo = (long long)((neg ? 0ull - X : X) - ((unsigned long long)hi << 52));
+  } else {
+    const long long N = (neg ? -(long long)M : (long long)M) - (hi != 0 ? hi * (1ll << 53) : 0ll);
+    const unsigned long long A = (unsigned long long)(N < 0 ? -N : N);
+    const int s = -T;
+    unsigned long long r = 0;
+    if (s < 63) {
+      r = A >> s;
+      const unsigned long long rem = A & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+      if (rem > half || (rem == half && (r & 1ull))) r += 1ull;
+    }
+    lo = N < 0 ? -(long long)r : (long long)r;
+  }
+}
+
+// The six components of one collision's exchange (dv, dl) at once: range test,
+// split, then the twelve atomics.
+static __device__ __forceinline__ void exch_add6(ExchAcc *e, d3 dv, d3 dl, int *err) {
+  const double v[6] = {dv.x, dv.y, dv.z, dl.x, dl.y, dl.z};
+  long long hi[6], lo[6];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    bad |= (dbits(v[k]) & 0x7FFFFFFFFFFFFFFFll) >= 0x4130000000000000ll;  // |v| >= 2^20 (or NaN)
+    exch_split(v[k], hi[k], lo[k]);
+  }
+  if (bad) atomicOr(err, ERRB_DELTA);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    atomicAdd((unsigned long long *)&e->hi[k], (unsigned long long)hi[k]);
+    atomicAdd((unsigned long long *)&e->lo[k], (unsigned long long)lo[k]);
+  }
 }
 
 static __device__ __forceinline__ double exch_val(const ExchAcc &e, int comp) {
@@ -161,30 +204,45 @@ static __device__ __forceinline__ double cd_next(CollDraw &d) {
 
 // stochastic_reflection (cpp/fluid_colloid_collision.cpp:7-24): Rayleigh normal
 // speed along rs plus one Gaussian tangential component along unit(un x t)
+//
+// Draws in the reference's order: u, the three components of t, then pairs of
+// Box-Muller tries.  The first eight come from two Philox blocks taken up front,
+// so the three independent chains (the unit normal, the Rayleigh speed, the
+// Gaussian) are straight-line code that overlaps; a third block onwards serves
+// the rare case of two rejected tries.
 static __device__ d3 stochastic_reflection(const SysF64 &S, CollDraw &d, d3 rf, d3 rs) {
-  double u = cd_next(d);
-  double om = __dsub_rn(1.0, u);
+  const uint4 r0 = draw4(d.key, DOM_COLL, 0, d.a, d.b, d.t), r1 = draw4(d.key, DOM_COLL, 1, d.a, d.b, d.t);
+  d.idx = 8;
+  double om = __dsub_rn(1.0, u01(r0.x));
   double random_e = __dmul_rn(om, om);
+  // polar Box-Muller rejection; each try is a fixed function of the key, and a
+  // try is rejected with probability 1 - pi/4, so 256 tries never run out
+  // (2 ran - 1 is exact: pm1 builds it from the draw's bits)
+  double x1 = pm1(r1.x), x2 = pm1(r1.y);
+  double z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+  if (z > 1.0) {
+    x1 = pm1(r1.z);
+    x2 = pm1(r1.w);
+    z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+    for (int it = 2; z > 1.0 && it < 256; ++it) {
+      x1 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
+      x2 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
+      z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+    }
+  }
+  const double lre = log(random_e), lz = log(z);
   // vector / |vector| as one reciprocal and three products (within an ulp of the
   // reference's three divisions); likewise /m_beta as * kT/m
   d3 n = mul3s(rs, __drcp_rn(__dsqrt_rn(norm2_ref(rs.x, rs.y, rs.z))));
-  double val = __dsqrt_rn(__dmul_rn(-log(random_e), S.inv_m_beta));
+  double val = __dsqrt_rn(__dmul_rn(-lre, S.inv_m_beta));
+  double g = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lz), z));
   d3 un = mul3s(n, val);
-  double t0 = cd_next(d), t1 = cd_next(d), t2 = cd_next(d);
-  d3 t = mk(ref_img(__dsub_rn(__dmul_rn(t0, S.dx.L), rf.x), S.dx), ref_img(__dsub_rn(__dmul_rn(t1, S.dy.L), rf.y), S.dy),
-            ref_img(__dsub_rn(__dmul_rn(t2, S.dz.L), rf.z), S.dz));
+  d3 t = mk(ref_img(__dsub_rn(__dmul_rn(u01(r0.y), S.dx.L), rf.x), S.dx),
+            ref_img(__dsub_rn(__dmul_rn(u01(r0.z), S.dy.L), rf.y), S.dy),
+            ref_img(__dsub_rn(__dmul_rn(u01(r0.w), S.dz.L), rf.z), S.dz));
   d3 ut = cross_ref(un, t);
   ut = mul3s(ut, __drcp_rn(__dsqrt_rn(norm2_ref(ut.x, ut.y, ut.z))));
-  double x1 = 0, x2 = 0, z = 2.0;
-  // polar Box-Muller rejection; each try is a fixed function of the key, and a
-  // try is rejected with probability 1 - pi/4, so 256 tries never run out
-  for (int it = 0; z > 1.0 && it < 256; ++it) {
-    x1 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
-    x2 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
-    z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
-  }
-  z = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(z)), z));
-  double v1 = __dmul_rn(__dmul_rn(x1, z), S.sqrt_kt_m);
+  double v1 = __dmul_rn(__dmul_rn(x1, g), S.sqrt_kt_m);
   return add3(mul3s(ut, v1), un);
 }
 
@@ -257,9 +315,18 @@ static __device__ __noinline__ void near_colloids(const SysF64 &S, int flags, in
   d3 vdump = mk(0, 0, 0);
   bool have_dump = false;
   if (flags & F_COLLIDE) {
-    for (int j = cand_next(S, it, cbox); j >= 0; j = cand_next(S, it, cbox)) {
-      if (!within(S, Xc, Xf[j], j, x, y, z, S.r_coll, S.sig2q)) continue;
+    for (;;) {
+      // the next colloid, in ascending order, whose sphere holds the particle; the
+      // search ends before the collision, so lanes of a warp whose hits are
+      // different candidates of their lists run the collision together
+      int j;
+      do {
+        j = cand_next(S, it, cbox);
+      } while (j >= 0 && !within(S, Xc, Xf[j], j, x, y, z, S.r_coll, S.sig2q));
+      if (j < 0) break;
       d3 Xj = mk(Xc[3 * j], Xc[3 * j + 1], Xc[3 * j + 2]);
+      // issued with Xj, used after the reflection
+      const d3 Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]), Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
       if (!have_dump) {  // dump_vel_fl: the velocity when the collision routine began
         vdump = mk(__dmul_rn(wx, S.inv_dt), __dmul_rn(wy, S.inv_dt), __dmul_rn(wz, S.inv_dt));
         have_dump = true;
@@ -272,14 +339,10 @@ static __device__ __noinline__ void near_colloids(const SysF64 &S, int flags, in
       CollDraw d;
       d.key = S.key; d.a = (uint32_t)(pid + 1); d.b = (uint32_t)(j + 1); d.t = (uint32_t)gs; d.idx = 0;
       d3 u = stochastic_reflection(S, d, mk(x, y, z), rs);
-      d3 Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]);
-      d3 Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
       d3 vn = add3(add3(u, Vj), cross_ref(Wj, rs));
       d3 dv = sub3(vdump, vn);
       d3 dl = cross_ref(rs, dv);
-      ExchAcc *e = S.exch + j;
-      exch_add(e, 0, dv.x, &S.ss->err); exch_add(e, 1, dv.y, &S.ss->err); exch_add(e, 2, dv.z, &S.ss->err);
-      exch_add(e, 3, dl.x, &S.ss->err); exch_add(e, 4, dl.y, &S.ss->err); exch_add(e, 5, dl.z, &S.ss->err);
+      exch_add6(S.exch + j, dv, dl, &S.ss->err);
       wx = __dmul_rn(vn.x, S.dt); wy = __dmul_rn(vn.y, S.dt); wz = __dmul_rn(vn.z, S.dt);
       wchanged = true;
       // step forward half a substep with the new velocity

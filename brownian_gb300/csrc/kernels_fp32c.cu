@@ -274,9 +274,11 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
   const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
   const int n = min(S.ss->nevents, S.events_cap);
   const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
-  // event i goes to block i % NVB: the few hundred to few thousand events of
-  // a substep spread over all SMs instead of filling the first few
-  for (int i = VB + NVB * threadIdx.x; i < n; i += NVB * blockDim.x) {
+  // event i goes to block i % NVB and, within it, to warp (i / NVB) % warps: the
+  // few hundred to few thousand events of a substep spread over all SMs and over
+  // each SM's four schedulers instead of filling the first few
+  const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int i = VB + NVB * k0; i < n; i += NVB * blockDim.x) {
     const int p = S.events[i];
     int cx, cy, cz;
     float ox, oy, oz;
@@ -292,16 +294,24 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
     const float ox0 = ox, oy0 = oy, oz0 = oz;
     if (flags & F_COLLIDE) {
       for (int last = -1;;) {
-        int j = 0x7FFFFFFF;
-        for (int k = 0; k < cnt; ++k) {
-          int c = lst[k];
-          if (c > last && c < j) j = c;
+        // the next colloid, in ascending order, whose sphere holds the particle; the
+        // search ends before the collision, so lanes of a warp whose hits are
+        // different candidates of their lists run the collision together
+        int j;
+        float4 cq, co;
+        for (;;) {
+          j = 0x7FFFFFFF;
+          for (int k = 0; k < cnt; ++k) {
+            int c = lst[k];
+            if (c > last && c < j) j = c;
+          }
+          if (j == 0x7FFFFFFF) break;
+          last = j;
+          cq = Xq[j]; co = Xo[j];
+          f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+          if (r.x * r.x + r.y * r.y + r.z * r.z <= rc2) break;
         }
         if (j == 0x7FFFFFFF) break;
-        last = j;
-        float4 cq = Xq[j], co = Xo[j];
-        f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
-        if (!(r.x * r.x + r.y * r.y + r.z * r.z <= rc2)) continue;
         // back half a substep, reflect, forward half a substep
         ox -= 0.5f * vx * S.dtf; oy -= 0.5f * vy * S.dtf; oz -= 0.5f * vz * S.dtf;
         carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
@@ -314,10 +324,7 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
         vx = u.x + V.x + wr.x; vy = u.y + V.y + wr.y; vz = u.z + V.z + wr.z;
         f3 dv = fm(vdump.x - vx, vdump.y - vy, vdump.z - vz);
         f3 dl = fcross(rs, dv);
-        ExchAcc *e = S.exch + j;
-        exch_add(e, 0, (double)dv.x, &S.ss->err); exch_add(e, 1, (double)dv.y, &S.ss->err);
-        exch_add(e, 2, (double)dv.z, &S.ss->err); exch_add(e, 3, (double)dl.x, &S.ss->err);
-        exch_add(e, 4, (double)dl.y, &S.ss->err); exch_add(e, 5, (double)dl.z, &S.ss->err);
+        exch_add6(S.exch + j, mk(dv.x, dv.y, dv.z), mk(dl.x, dl.y, dl.z), &S.ss->err);
         ox += 0.5f * vx * S.dtf; oy += 0.5f * vy * S.dtf; oz += 0.5f * vz * S.dtf;
         carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
       }

@@ -64,8 +64,10 @@ __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double 
 #define STREAM64_U_SHELL 1
 #endif
 static constexpr __host__ __device__ int stream64_u(int flags) { return (flags & F_SHELL) ? STREAM64_U_SHELL : STREAM64_U; }
+// Five blocks per SM (48 registers, a few spilled to L1) measured faster than four
+// without spills.
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int fb) {
+__global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb) {
   constexpr int flags = FLAGS;
   constexpr int U = stream64_u(FLAGS);
   const long long step = S.ss->step;
@@ -107,10 +109,11 @@ __global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int fb) {
       if (!alias) cnt[u] = tcount(S.Tcnt[buf][lin[u]], gs);
     }
   }
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    if (!valid[u]) continue;
-    if ((flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
+    if (valid[u] && (flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
       cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
       const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
       const float4 *Xf = S.Xf[buf];
@@ -128,27 +131,36 @@ __global__ void __launch_bounds__(256) k_stream(const SysF64 S, int l, int fb) {
       }
     }
     const int p = p0 + 256 * u;
-    if (!ev[u] && (flags & F_BINROT)) bin_for_rotation(S, p, x[u], y[u], z[u], wx[u], wy[u], wz[u]);
-    if (flags & F_STREAM) { F.x[p] = x[u]; F.y[p] = y[u]; F.z[p] = z[u]; }
-  }
-  // appends: events one atomic per warp (no block barrier), run() candidate
-  // records (last substep) one atomic per block
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
-    const bool has_rec = (flags & F_SHELL) && valid[u] && !ev[u] && members[u] != 0;
-    const unsigned mev = __ballot_sync(FULL, ev[u]), mrec = __ballot_sync(FULL, has_rec);
-    int bev = 0, brec = 0;
+    if (valid[u]) {
+      if (!ev[u] && (flags & F_BINROT)) bin_for_rotation(S, p, x[u], y[u], z[u], wx[u], wy[u], wz[u]);
+      if (flags & F_STREAM) { F.x[p] = x[u]; F.y[p] = y[u]; F.z[p] = z[u]; }
+    }
+    // the event record, one atomic per warp (no block barrier), written while the
+    // particle's state is still in registers
+    const unsigned mev = __ballot_sync(FULL, ev[u]);
+    int bev = 0;
     if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
     bev = __shfl_sync(FULL, bev, 0);
-    if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
     if (ev[u]) {
       const int i = bev + __popc(mev & lt);
-      if (i < S.events_cap) S.events[i] = p;
-      else atomicOr(&S.ss->err, ERRB_SHELL);
+      if (i < S.events_cap) {
+        EventRec r;
+        r.xy = make_double2(x[u], y[u]); r.zwx = make_double2(z[u], wx[u]); r.wywz = make_double2(wy[u], wz[u]);
+        r.p = p; r.pad = 0;
+        S.evrec[i] = r;
+      } else {
+        atomicOr(&S.ss->err, ERRB_SHELL);
+      }
     }
+  }
+  // run() candidate records (last substep), one atomic per block
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!(flags & F_SHELL)) break;
+    const int p = p0 + 256 * u;
+    const bool has_rec = valid[u] && !ev[u] && members[u] != 0;
+    const unsigned mrec = __ballot_sync(FULL, has_rec);
+    const int brec = block_base(&S.ss->nshell, mrec, lane);
     if (has_rec) {
       const int i = brec + __popc(mrec & lt);
       if (i < S.shell_cap) {
@@ -190,11 +202,14 @@ __global__ void __launch_bounds__(128, 4) k_events(const SysF64 S, int l, int fb
   const int buf = (int)(gs & 1);
   const Fluid F = fluid_at(S, fb);
   const int n = min(S.ss->nevents, S.events_cap);
-  // event i goes to block i % gridDim.x: the few hundred to few thousand events of
-  // a substep spread over all SMs instead of filling the first few
-  for (int i = blockIdx.x + gridDim.x * threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int p = S.events[i];
-    double x = F.x[p], y = F.y[p], z = F.z[p], wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
+  // event i goes to block i % gridDim.x and, within it, to warp (i / gridDim.x) %
+  // warps: the few hundred to few thousand events of a substep spread over all SMs
+  // and over each SM's four schedulers instead of filling the first few
+  const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int i = blockIdx.x + gridDim.x * k0; i < n; i += gridDim.x * blockDim.x) {
+    const EventRec r = S.evrec[i];
+    const int p = r.p;
+    double x = r.xy.x, y = r.xy.y, z = r.zwx.x, wx = r.zwx.y, wy = r.wywz.x, wz = r.wywz.y;
     bool alias, wchanged = false;
     int lin = cell_of_pos(S, x, y, z, alias);
     ShellRec rec;
@@ -302,7 +317,7 @@ __global__ void __launch_bounds__(256) k_cell_prep(const SysF64 S) {
   double s = var > 0 ? sqrt(S.cs * (double)(n - 1) / var) : 1.0;
   // rotation axis: rho = 2 ran - 1, phi = 4 asin(1) ran (cpp/rotation_mpcd.cpp:19-20)
   uint4 r = draw4(S.key, DOM_AXIS, 0, (uint32_t)(c + 1), 0, (uint32_t)(S.ss->step + 1));
-  double rho = 2.0 * u01(r.x) - 1.0, phi = S.two_pi * u01(r.y);
+  double rho = pm1(r.x), phi = S.two_pi * u01(r.y);
   double sp, cp;
   sincos(phi, &sp, &cp);
   double sq = sqrt(1.0 - rho * rho);

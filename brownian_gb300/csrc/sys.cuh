@@ -41,6 +41,13 @@ struct ExchAcc {
   long long hi[6], lo[6];
 };
 
+// an FP64 event: the particle and its streamed position and displacement, so the
+// event pass starts from one record instead of an index and a gather
+struct __align__(16) EventRec {
+  double2 xy, zwx, wywz;
+  int p, pad;
+};
+
 // quantities that change every step, kept on the device so one captured CUDA
 // graph serves every step
 struct StepState {
@@ -119,6 +126,7 @@ struct SysF64 {
   // particles near a sphere surface in the substep in flight
   int *events;
   int events_cap;
+  EventRec *evrec;  // FP64 form: the listed particles' state as the streaming pass left it
   // FP32-compensated fluid (precision MPCD_FP32C): per particle one 16-byte record
   // {cell x | y << 10 | z << 20, offset x, offset y, offset z} with offsets in
   // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32

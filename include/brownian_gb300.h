@@ -144,8 +144,8 @@ enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, mu
        MPCD_LAUNCH_AUX = 2 };  /* colloid side work (forces, cell table, orientation; a kernel on a
                                   second stream beside the streaming and event passes): grid > 0
                                   sets, block = threads per colloid (64, 128 or 256) */
-/* grid <= 0 restores the default (events and finish: one block per SM; side work:
- * 128 threads per colloid); results do not depend on the shape (every sum is
+/* grid <= 0 restores the default (events: one block of 128 threads per SM; finish:
+ * one block of 32 per SM; side work: 128 threads per colloid); results do not depend on the shape (every sum is
  * exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
