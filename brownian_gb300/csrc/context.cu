@@ -52,6 +52,8 @@ struct mpcd_ctx {
   bool own_stream = false;
   cudaStream_t aux = nullptr;    // second stream: colloid work beside the fluid passes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
+  cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_fin = nullptr;
   cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sorts][fluid buffer]
   int step_launches[2][2] = {{0, 0}, {0, 0}};
   int fbuf = 0;                  // fluid buffer holding the current state
@@ -156,12 +158,20 @@ static int colloid_grid(const mpcd_ctx *c) {
   return g > 0 ? g : 1;
 }
 
+static const char *stream_name(int flags) {
+  flags &= ~F_PIPE;
+  return flags == (F_STREAM | F_COLLIDE) ? "k_stream"
+         : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
+         : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
+}
+
+// One substep's fluid passes in stream order (the FP64 form's substep kernels are
+// the overlapped ones, F_PIPE, whose results do not depend on the schedule).
 static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
   const int fb = c->fbuf;
-  const char *name = flags == (F_STREAM | F_COLLIDE) ? "k_stream"
-                     : flags == (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) ? "k_stream_last"
-                     : flags == (F_SHELL | F_BINROT) ? "k_stream_setup" : "k_stream_other";
   const bool f32 = c->S.precision == MPCD_FP32C;
+  if (!f32 && (flags & F_STREAM)) flags |= F_PIPE;
+  const char *name = stream_name(flags);
   // The colloid forces, the next cell table and the orientation work of a substep
   // need nothing the fluid passes write: they run as a kernel of their own (which
   // keeps the streaming pass at its own, low register count) on the second,
@@ -183,7 +193,7 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
   if (fork) cudaStreamWaitEvent(c->stream, c->ev_join, 0);  // k_fin reads the forces and the orientation
 }
 
-static void enq_fin(mpcd_ctx *c, int mode, int l) {
+static void enq_fin_on(mpcd_ctx *c, cudaStream_t s, int mode, int l) {
   // one warp per colloid (warp j / grid of block j % grid): each SM's FP64 unit
   // serves the chains of a few colloids only
   int g = c->fin_grid > 0 ? c->fin_grid : c->n_sm;
@@ -195,8 +205,10 @@ static void enq_fin(mpcd_ctx *c, int mode, int l) {
     w = 4;
     g = (int)blocks_for(nc, 4);
   }
-  launch(c, "k_fin", k_fin, g, 32 * w, c->S, mode, l);
+  launch_on(c, s, "k_fin", k_fin, g, 32 * w, c->S, mode, l);
 }
+
+static void enq_fin(mpcd_ctx *c, int mode, int l) { enq_fin_on(c, c->stream, mode, l); }
 
 static unsigned prep_blocks(const SysF64 &S) { return blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256); }
 
@@ -226,16 +238,56 @@ static void enq_run_fluid(mpcd_ctx *c) {
   launch(c, "k_run_kick", f32 ? k_run_kick32 : k_run_kick, 152 * 4, 256, S, c->fbuf);
 }
 
+// The substeps of the FP64 form, overlapped on three streams.  Per substep l:
+//   main   k_stream(l)            needs k_stream(l-1) and k_aux(l-1) (cell table of l)
+//   events k_events(l), k_fin(l)  need k_stream(l); k_fin also k_aux(l)
+//   aux    k_aux(l)               needs k_fin(l-1) (the positions of substep l)
+// so the streaming pass of l+1, bandwidth-bound, runs beside the event pass and the
+// colloid finish of l, latency-bound.  k_stream(l+1) tests against the positions
+// of l with the displacement bound as margin and leaves the particles k_events(l)
+// may be changing (pending) to the event passes; no data of the concurrent passes
+// overlap (see the F_PIPE kernels).
+static void enq_substeps_overlapped(mpcd_ctx *c) {
+  const int n = c->S.n_sub;
+  const bool nc = c->S.Nc > 0;
+  cudaEventRecord(c->ev_start, c->stream);
+  cudaStreamWaitEvent(c->evs, c->ev_start, 0);
+  if (nc) cudaStreamWaitEvent(c->aux, c->ev_start, 0);
+  for (int l = 1; l <= n; ++l) {
+    const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
+    if (l >= 2 && nc) cudaStreamWaitEvent(c->stream, c->ev_aux, 0);
+    launch(c, stream_name(flags), stream_kernel(flags), blocks_for(c->S.N, 256 * stream64_per_thread(flags)), 256,
+           c->S, l, c->fbuf);
+    cudaEventRecord(c->ev_str, c->stream);
+    if (nc) {
+      if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_fin, 0);
+      launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, l >= 2 ? 1 : 0);
+      cudaEventRecord(c->ev_aux, c->aux);
+    }
+    cudaStreamWaitEvent(c->evs, c->ev_str, 0);
+    launch_on(c, c->evs, "k_events", event_kernel(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, c->S,
+              l, c->fbuf);
+    if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
+    enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+    cudaEventRecord(c->ev_fin, c->evs);
+  }
+  cudaStreamWaitEvent(c->stream, c->ev_fin, 0);
+}
+
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
 static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
   enq_rotation(c, sort);
   enq_run_fluid(c);
   enq_fin(c, M_KICK | M_ADVANCE, 0);
-  for (int l = 1; l <= n; ++l) {
-    // the orientation update of substep l-1 rides on the streaming pass of substep l
-    enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l, l >= 2);
-    enq_fin(c, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+  if (c->S.precision == MPCD_FP64) {
+    enq_substeps_overlapped(c);
+  } else {
+    for (int l = 1; l <= n; ++l) {
+      // the orientation update of substep l-1 rides on the streaming pass of substep l
+      enq_stream(c, l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE), l, l >= 2);
+      enq_fin(c, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+    }
   }
   launch(c, "k_end_step", k_end_step, 1, 32, c->S);
 }
@@ -264,6 +316,7 @@ static const char *err_text(int bits) {
   if (bits & ERRB_DISPLACE) return "a wall collision displaced a particle beyond the cell-table margin";
   if (bits & ERRB_SHELLSLOTS) return "a particle lies in more rear shells than a record holds";
   if (bits & ERRB_DELTA) return "a colloid momentum exchange left the range of the exact sums";
+  if (bits & ERRB_EVENTS) return "the wall-collision event lists overflowed";
   return "device error";
 }
 
@@ -358,14 +411,22 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   const double vmax = p.vmax > 0 ? p.vmax : 24.0 * vth + 2.0 * kick;
   // cell-table reach: sphere (or run() shell) + a wall collision's displacement
   // (0.1 covers speeds near 20 kT units) + a colloid's move in one substep + FP32
-  // slack; both displacements are checked on the device
-  const double pmargin = fmax(0.1, 0.5 * dt * (2.0 * kick + 6.0 * vth)), cmargin = 0.05;
+  // slack; both displacements are checked on the device.  The colloid bound is
+  // dt (20 sigma_V + 20 |v0|), sigma_V = sqrt(3 kT / M) the colloid's thermal speed,
+  // within [0.005, 0.05]: the FP64 form's streaming pass tests against the previous
+  // substep's colloid positions with it as margin, and every particle within it of
+  // a sphere goes to the (latency-bound) event passes, so it is kept tight.
+  const double kt_c = fmax(p.kbt, p.kbt1);
+  const double vcol = p.n_colloid > 0 ? 20.0 * sqrt(3.0 * kt_c / p.mass_colloid) + 20.0 * fabs(p.v0) : 0.0;
+  const double pmargin = fmax(0.1, 0.5 * dt * (2.0 * kick + 6.0 * vth));
+  const double cmargin = fmin(0.05, fmax(0.005, dt * vcol));
   S.r_coll = (float)(p.sigma * 0.5);
   S.r_shell = (float)(p.sigma * 0.5 + 0.5);
   S.rT_coll = (float)(p.sigma * 0.5 + pmargin + cmargin + 0.01);
   S.rT_shell = (float)(p.sigma * 0.5 + 0.5 + pmargin + cmargin + 0.01);
   S.disp_margin2 = pmargin * pmargin;
   S.cmargin2 = cmargin * cmargin;
+  S.cmarginf = (float)cmargin;
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   S.precision = p.precision;
@@ -424,7 +485,13 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.shell = m.get<ShellRec>(S.shell_cap);
   S.events_cap = S.N / 16 + 65536;
   S.events = m.get<int>(S.events_cap);
-  S.evrec = S.precision == MPCD_FP64 ? m.get<EventRec>(S.events_cap) : nullptr;
+  if (S.precision == MPCD_FP64) {
+    S.newrec[0] = m.get<EventRec>(S.events_cap);
+    S.newrec[1] = m.get<EventRec>(S.events_cap);
+    S.pend_cap = S.events_cap;
+    S.prec = m.get<EventRec>(S.pend_cap);
+    S.pend = m.get<uint8_t>(S.N);
+  }
   S.ss = m.get<StepState>(1);
   c->inv_n = m.get<double>(S.max_per_cell + 1);
   S.inv_n = c->inv_n;
@@ -455,8 +522,13 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   int prio_lo = 0, prio_hi = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->evs, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_str, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_aux, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fin, cudaEventDisableTiming) != cudaSuccess) {
     mpcd_destroy(c);
     return MPCD_ERR_CUDA;
   }
@@ -483,8 +555,9 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->ss_host) cudaFreeHost(c->ss_host);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->evs) cudaStreamDestroy(c->evs);
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_fin})
+    if (e) cudaEventDestroy(e);
   delete c;
   return MPCD_OK;
 }
@@ -707,6 +780,8 @@ extern "C" int mpcd_setup(mpcd_ctx *c) {
   CUDA_OK(c, cudaMemcpyAsync(&c->S.ss->err, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   // create_box + neighbour_list_md + compute_force_md: forces at the current positions,
   // cell table around each colloid (cpp/active_brownian.cpp:93-96)
+  // no particle is pending between steps (a step cut short by an error may have left marks)
+  if (c->S.pend) CUDA_OK(c, cudaMemsetAsync(c->S.pend, 0, (size_t)c->S.N, c->stream));
   launch(c, "k_colloid_setup", k_colloid_setup, colloid_grid(c), 128, c->S);
   // neighbour_list_mpcd seen from the fluid: run() candidates of the first step, and the
   // SRD binning of its rotation_mpcd

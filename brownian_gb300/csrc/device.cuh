@@ -220,10 +220,15 @@ static __device__ d3 stochastic_reflection(const SysF64 &S, CollDraw &d, d3 rf, 
   // (2 ran - 1 is exact: pm1 builds it from the draw's bits)
   double x1 = pm1(r1.x), x2 = pm1(r1.y);
   double z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+  // the second try is computed by every lane and selected, so the lanes of a warp
+  // stay together; only two rejections in a row (1 in 22) branch
+  const double x1b = pm1(r1.z), x2b = pm1(r1.w);
+  const double zb = __dadd_rn(__dmul_rn(x1b, x1b), __dmul_rn(x2b, x2b));
+  const bool second = z > 1.0;
+  x1 = second ? x1b : x1;
+  x2 = second ? x2b : x2;
+  z = second ? zb : z;
   if (z > 1.0) {
-    x1 = pm1(r1.z);
-    x2 = pm1(r1.w);
-    z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
     for (int it = 2; z > 1.0 && it < 256; ++it) {
       x1 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
       x2 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
@@ -290,81 +295,97 @@ static __device__ __forceinline__ bool within(const SysF64 &S, const double *Xc,
   return norm2_ref(rx, ry, rz) <= r2;
 }
 
-// Everything a particle does near colloids: wall collisions in colloid order
-// (fluid_colloid_collision.cpp:30-45) and, on the last substep, the run()
-// candidate record.  Kept out of line so the common streaming path stays lean.
-static __device__ __noinline__ void near_colloids(const SysF64 &S, int flags, int pid, int lin, bool alias, long long gs,
-                                           int buf, double &x, double &y, double &z, double &wx, double &wy,
-                                           double &wz, bool &wchanged, ShellRec &rec) {
+// The state of one listed particle while the event pass works on it.  It lives in
+// shared memory so that any thread of the block can carry the particle's
+// collisions: the collisions of a block are gathered onto its first threads (one
+// warp, as a rule) because a GB300 SM takes ~64 cycles per FP64 warp instruction
+// however few lanes are active; spread over every warp the FP64 bodies would queue
+// on the SM's FP64 pipe.
+struct EvState {
+  double x, y, z, wx, wy, wz;
+  double x0, y0, z0;     // position before the first collision (displacement check)
+  double vdx, vdy, vdz;  // velocity when the collision routine began (dump_vel_fl)
+  int p, id, lin, last;  // fluid slot, particle id, cell, last colloid the search visited
+  int cnt, j;            // cell-table candidates; colloid of the next collision (-1: none)
+  bool alias, dumped, changed;
+};
+
+static __device__ __forceinline__ CandIter ev_iter(const SysF64 &S, const EvState &st, int buf) {
+  CandIter it;
+  it.brute = st.alias;
+  it.lin = st.lin;
+  it.last = st.last;
+  it.cnt = st.cnt;
+  it.lst = S.Tlist[buf] + (size_t)st.lin * TCAP;
+  return it;
+}
+
+// the next colloid, in ascending order after the last one visited, whose sphere
+// holds the particle (fluid_colloid_collision.cpp:30-33), or -1
+static __device__ __forceinline__ int ev_next_hit(const SysF64 &S, EvState &st, int buf) {
   const double *Xc = S.X[buf];
   const float4 *Xf = S.Xf[buf];
-  const int *cbox = S.cbox[buf];
-  CandIter it;
-  it.brute = alias;
-  it.lin = lin;
+  CandIter it = ev_iter(S, st, buf);
+  int j;
+  do {
+    j = cand_next(S, it, S.cbox[buf]);
+  } while (j >= 0 && !within(S, Xc, Xf[j], j, st.x, st.y, st.z, S.r_coll, S.sig2q));
+  st.last = it.last;
+  return j;
+}
+
+// One wall collision of the particle with colloid j (fluid_colloid_collision.cpp:34-45):
+// half a substep back, stochastic reflection in the colloid's frame, the exchange
+// into the colloid's exact sums, half a substep forward.
+static __device__ __noinline__ void ev_collide(const SysF64 &S, EvState &st, int j, long long gs, int buf) {
+  const double *Xc = S.X[buf];
+  const d3 Xj = mk(Xc[3 * j], Xc[3 * j + 1], Xc[3 * j + 2]);
+  // issued with Xj, used after the reflection
+  const d3 Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]), Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
+  double x = st.x, y = st.y, z = st.z, wx = st.wx, wy = st.wy, wz = st.wz;
+  if (!st.dumped) {  // dump_vel_fl: the velocity when the collision routine began
+    st.vdx = __dmul_rn(wx, S.inv_dt); st.vdy = __dmul_rn(wy, S.inv_dt); st.vdz = __dmul_rn(wz, S.inv_dt);
+    st.dumped = true;
+  }
+  // step back half a substep with the current velocity
+  x = ref_mod(__dsub_rn(x, __dmul_rn(wx, 0.5)), S.dx);
+  y = ref_mod(__dsub_rn(y, __dmul_rn(wy, 0.5)), S.dy);
+  z = ref_mod(__dsub_rn(z, __dmul_rn(wz, 0.5)), S.dz);
+  d3 rs = mk(ref_img(__dsub_rn(x, Xj.x), S.dx), ref_img(__dsub_rn(y, Xj.y), S.dy), ref_img(__dsub_rn(z, Xj.z), S.dz));
+  CollDraw d;
+  d.key = S.key; d.a = (uint32_t)(st.id + 1); d.b = (uint32_t)(j + 1); d.t = (uint32_t)gs; d.idx = 0;
+  d3 u = stochastic_reflection(S, d, mk(x, y, z), rs);
+  d3 vn = add3(add3(u, Vj), cross_ref(Wj, rs));
+  d3 dv = sub3(mk(st.vdx, st.vdy, st.vdz), vn);
+  d3 dl = cross_ref(rs, dv);
+  exch_add6(S.exch + j, dv, dl, &S.ss->err);
+  wx = __dmul_rn(vn.x, S.dt); wy = __dmul_rn(vn.y, S.dt); wz = __dmul_rn(vn.z, S.dt);
+  // step forward half a substep with the new velocity
+  x = ref_mod(__dadd_rn(x, __dmul_rn(wx, 0.5)), S.dx);
+  y = ref_mod(__dadd_rn(y, __dmul_rn(wy, 0.5)), S.dy);
+  z = ref_mod(__dadd_rn(z, __dmul_rn(wz, 0.5)), S.dz);
+  // the cell table is built with a margin; a move beyond it could hide a colloid
+  double ex = ref_img(__dsub_rn(x, st.x0), S.dx), ey = ref_img(__dsub_rn(y, st.y0), S.dy),
+         ez = ref_img(__dsub_rn(z, st.z0), S.dz);
+  if (norm2_ref(ex, ey, ez) > S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
+  st.x = x; st.y = y; st.z = z; st.wx = wx; st.wy = wy; st.wz = wz;
+  st.changed = true;
+}
+
+// run() candidate record of the particle at its final position: the colloids, in
+// ascending order, whose rear-shell sphere holds it
+static __device__ __forceinline__ void ev_shell(const SysF64 &S, const EvState &st, int buf, ShellRec &rec) {
+  const double *Xc = S.X[buf];
+  const float4 *Xf = S.Xf[buf];
+  CandIter it = ev_iter(S, st, buf);
   it.last = -1;
-  if (!alias) {
-    int c = tcount(S.Tcnt[buf][lin], gs);
-    it.cnt = c < TCAP ? c : TCAP;
-    it.lst = S.Tlist[buf] + (size_t)lin * TCAP;
-  } else {
-    it.cnt = 0;
-    it.lst = nullptr;
-  }
-  const double x0 = x, y0 = y, z0 = z;
-  d3 vdump = mk(0, 0, 0);
-  bool have_dump = false;
-  if (flags & F_COLLIDE) {
-    for (;;) {
-      // the next colloid, in ascending order, whose sphere holds the particle; the
-      // search ends before the collision, so lanes of a warp whose hits are
-      // different candidates of their lists run the collision together
-      int j;
-      do {
-        j = cand_next(S, it, cbox);
-      } while (j >= 0 && !within(S, Xc, Xf[j], j, x, y, z, S.r_coll, S.sig2q));
-      if (j < 0) break;
-      d3 Xj = mk(Xc[3 * j], Xc[3 * j + 1], Xc[3 * j + 2]);
-      // issued with Xj, used after the reflection
-      const d3 Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]), Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
-      if (!have_dump) {  // dump_vel_fl: the velocity when the collision routine began
-        vdump = mk(__dmul_rn(wx, S.inv_dt), __dmul_rn(wy, S.inv_dt), __dmul_rn(wz, S.inv_dt));
-        have_dump = true;
-      }
-      // step back half a substep with the current velocity
-      x = ref_mod(__dsub_rn(x, __dmul_rn(wx, 0.5)), S.dx);
-      y = ref_mod(__dsub_rn(y, __dmul_rn(wy, 0.5)), S.dy);
-      z = ref_mod(__dsub_rn(z, __dmul_rn(wz, 0.5)), S.dz);
-      d3 rs = mk(ref_img(__dsub_rn(x, Xj.x), S.dx), ref_img(__dsub_rn(y, Xj.y), S.dy), ref_img(__dsub_rn(z, Xj.z), S.dz));
-      CollDraw d;
-      d.key = S.key; d.a = (uint32_t)(pid + 1); d.b = (uint32_t)(j + 1); d.t = (uint32_t)gs; d.idx = 0;
-      d3 u = stochastic_reflection(S, d, mk(x, y, z), rs);
-      d3 vn = add3(add3(u, Vj), cross_ref(Wj, rs));
-      d3 dv = sub3(vdump, vn);
-      d3 dl = cross_ref(rs, dv);
-      exch_add6(S.exch + j, dv, dl, &S.ss->err);
-      wx = __dmul_rn(vn.x, S.dt); wy = __dmul_rn(vn.y, S.dt); wz = __dmul_rn(vn.z, S.dt);
-      wchanged = true;
-      // step forward half a substep with the new velocity
-      x = ref_mod(__dadd_rn(x, __dmul_rn(wx, 0.5)), S.dx);
-      y = ref_mod(__dadd_rn(y, __dmul_rn(wy, 0.5)), S.dy);
-      z = ref_mod(__dadd_rn(z, __dmul_rn(wz, 0.5)), S.dz);
-      // the cell table is built with a margin; a move beyond it could hide a colloid
-      double ex = ref_img(__dsub_rn(x, x0), S.dx), ey = ref_img(__dsub_rn(y, y0), S.dy),
-             ez = ref_img(__dsub_rn(z, z0), S.dz);
-      if (norm2_ref(ex, ey, ez) > S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
-    }
-  }
-  if (flags & F_SHELL) {
-    rec.p = pid;
-    rec.n = 0;
-    rec.pass = 0;
-    it.last = -1;
-    for (int j = cand_next(S, it, cbox); j >= 0; j = cand_next(S, it, cbox)) {
-      if (!within(S, Xc, Xf[j], j, x, y, z, S.r_shell, S.rsh2)) continue;
-      if (rec.n < SHELL_J) rec.j[rec.n++] = (uint16_t)j;
-      else atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
-    }
+  rec.p = st.id;
+  rec.n = 0;
+  rec.pass = 0;
+  for (int j = cand_next(S, it, S.cbox[buf]); j >= 0; j = cand_next(S, it, S.cbox[buf])) {
+    if (!within(S, Xc, Xf[j], j, st.x, st.y, st.z, S.r_shell, S.rsh2)) continue;
+    if (rec.n < SHELL_J) rec.j[rec.n++] = (uint16_t)j;
+    else atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
   }
 }
 

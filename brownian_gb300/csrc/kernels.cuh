@@ -4,7 +4,7 @@
 
 namespace bgb {
 
-enum : int { F_STREAM = 1, F_COLLIDE = 2, F_SHELL = 4, F_BINROT = 8 };
+enum : int { F_STREAM = 1, F_COLLIDE = 2, F_SHELL = 4, F_BINROT = 8, F_PIPE = 16 };
 enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8 };
 
 // k_stream<FLAGS> instantiations, by flag set (nullptr for a set not built)

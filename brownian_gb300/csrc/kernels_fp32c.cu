@@ -277,41 +277,56 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
   // event i goes to block i % NVB and, within it, to warp (i / NVB) % warps: the
   // few hundred to few thousand events of a substep spread over all SMs and over
   // each SM's four schedulers instead of filling the first few
+  // (a warp-uniform trip count and collision loop, as the FP64 form: the body of a
+  // collision runs once for all lanes of a warp that hit a colloid at that rank)
   const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  for (int i = VB + NVB * k0; i < n; i += NVB * blockDim.x) {
-    const int p = S.events[i];
-    int cx, cy, cz;
-    float ox, oy, oz;
-    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
-    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+  for (int base = 0;; base += blockDim.x) {
+    const int i = VB + NVB * (k0 + base);
+    const bool valid = i < n;
+    if (!__any_sync(FULL, valid)) break;
+    const int p = valid ? S.events[i] : 0;
+    int cx = 0, cy = 0, cz = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+    int cnt = 0, id = 0;
+    if (valid) {
+      unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+      vx = F.vx[p]; vy = F.vy[p]; vz = F.vz[p];
+      id = F.id[p];
+    }
     const int lin = cx + S.Lx * (cy + S.Ly * cz);
-    int cnt = tcount(S.Tcnt[buf][lin], gs);
-    cnt = cnt < TCAP ? cnt : TCAP;
+    if (valid) {
+      cnt = tcount(S.Tcnt[buf][lin], gs);
+      cnt = cnt < TCAP ? cnt : TCAP;
+    }
     const uint16_t *lst = S.Tlist[buf] + (size_t)lin * TCAP;
-    const int id = F.id[p];
     const f3 vdump = fm(vx, vy, vz);
     const int cx0 = cx, cy0 = cy, cz0 = cz;
     const float ox0 = ox, oy0 = oy, oz0 = oz;
     if (flags & F_COLLIDE) {
-      for (int last = -1;;) {
-        // the next colloid, in ascending order, whose sphere holds the particle; the
-        // search ends before the collision, so lanes of a warp whose hits are
-        // different candidates of their lists run the collision together
-        int j;
-        float4 cq, co;
-        for (;;) {
-          j = 0x7FFFFFFF;
-          for (int k = 0; k < cnt; ++k) {
-            int c = lst[k];
-            if (c > last && c < j) j = c;
+      bool more = valid;
+      int last = -1;
+      while (__any_sync(FULL, more)) {
+        // each lane's next colloid, in ascending order, whose sphere holds the
+        // particle; then all lanes meet before the collision body
+        int j = 0x7FFFFFFF;
+        float4 cq = make_float4(0.f, 0.f, 0.f, 0.f), co = cq;
+        if (more) {
+          for (;;) {
+            j = 0x7FFFFFFF;
+            for (int k = 0; k < cnt; ++k) {
+              int c = lst[k];
+              if (c > last && c < j) j = c;
+            }
+            if (j == 0x7FFFFFFF) break;
+            last = j;
+            cq = Xq[j]; co = Xo[j];
+            f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+            if (r.x * r.x + r.y * r.y + r.z * r.z <= rc2) break;
           }
-          if (j == 0x7FFFFFFF) break;
-          last = j;
-          cq = Xq[j]; co = Xo[j];
-          f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
-          if (r.x * r.x + r.y * r.y + r.z * r.z <= rc2) break;
+          more = j != 0x7FFFFFFF;
         }
-        if (j == 0x7FFFFFFF) break;
+        __syncwarp();
+        if (j == 0x7FFFFFFF) continue;
         // back half a substep, reflect, forward half a substep
         ox -= 0.5f * vx * S.dtf; oy -= 0.5f * vy * S.dtf; oz -= 0.5f * vz * S.dtf;
         carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
@@ -329,6 +344,7 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
         carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
       }
     }
+    if (!valid) continue;
     {
       // the cell table is built with a margin; a move beyond it could hide a colloid
       const float ex = rel(cx, ox, (float)cx0, ox0, S.Lx), ey = rel(cy, oy, (float)cy0, oy0, S.Ly),

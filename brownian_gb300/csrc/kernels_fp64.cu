@@ -19,6 +19,7 @@
 //                 colloid positions and the cell table of the next substep
 //   k_fin         per colloid: end of fluid_colloid_collision, update_activity_direction,
 //                 update_velocity_colloid, then update_pos_md of the next substep
+#include "../../include/brownian_gb300.h"
 #include "device.cuh"
 
 namespace bgb {
@@ -75,10 +76,16 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
   const Fluid F = fluid_at(S, fb);
   const int p0 = blockIdx.x * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
+  // F_PIPE: the colloid positions of the previous substep (this substep's are being
+  // computed meanwhile) and the displacement bound as margin; pending particles
+  // belong to the event passes and are skipped
+  const int xb = (flags & F_PIPE) ? (int)((gs - 1) & 1) : buf;
+  const float mg = (flags & F_PIPE) ? S.cmarginf : 0.f;
   double x[U], y[U], z[U], wx[U], wy[U], wz[U];
   bool valid[U], ev[U];
   unsigned members[U];  // run() shell members among the cell-table slots
   int cnt[U], lin[U];
+  uint8_t pd[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int p = p0 + 256 * u;
@@ -87,12 +94,16 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
     members[u] = 0;
     cnt[u] = 0;
     lin[u] = 0;
+    pd[u] = 0;
     wx[u] = wy[u] = wz[u] = 0;
     if (valid[u]) {
       x[u] = F.x[p]; y[u] = F.y[p]; z[u] = F.z[p];
       if (flags & (F_STREAM | F_BINROT)) { wx[u] = F.wx[p]; wy[u] = F.wy[p]; wz[u] = F.wz[p]; }
+      if (flags & F_PIPE) pd[u] = S.pend[p];
     }
   }
+#pragma unroll
+  for (int u = 0; u < U; ++u) valid[u] = valid[u] && pd[u] == 0;
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     if (!valid[u]) continue;
@@ -116,9 +127,9 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
     if (valid[u] && (flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
       cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
       const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
-      const float4 *Xf = S.Xf[buf];
+      const float4 *Xf = S.Xf[xb];
       const float px = d2f_trunc(x[u]), py = d2f_trunc(y[u]), pz = d2f_trunc(z[u]);
-      const float ch = S.r_coll + 1e-3f, sl = S.r_shell - 1e-3f, sh = S.r_shell + 1e-3f;
+      const float ch = S.r_coll + 1e-3f + mg, sl = S.r_shell - 1e-3f - mg, sh = S.r_shell + 1e-3f + mg;
       for (int k = 0; k < cnt[u]; ++k) {
         const float4 c = Xf[lst[k]];
         const float dx = wrap_half(c.x - px, S.Lxf), dy = wrap_half(c.y - py, S.Lyf), dz = wrap_half(c.z - pz, S.Lzf);
@@ -139,17 +150,18 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
     // particle's state is still in registers
     const unsigned mev = __ballot_sync(FULL, ev[u]);
     int bev = 0;
-    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
+    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nnew[buf], __popc(mev));
     bev = __shfl_sync(FULL, bev, 0);
     if (ev[u]) {
       const int i = bev + __popc(mev & lt);
       if (i < S.events_cap) {
         EventRec r;
         r.xy = make_double2(x[u], y[u]); r.zwx = make_double2(z[u], wx[u]); r.wywz = make_double2(wy[u], wz[u]);
-        r.p = p; r.pad = 0;
-        S.evrec[i] = r;
+        r.p = p; r.id = F.id[p];
+        S.newrec[buf][i] = r;
+        if (flags & F_PIPE) S.pend[p] = 1;
       } else {
-        atomicOr(&S.ss->err, ERRB_SHELL);
+        atomicOr(&S.ss->err, ERRB_EVENTS);
       }
     }
   }
@@ -193,43 +205,114 @@ int stream64_per_thread(int flags) { return stream64_u(flags); }
 
 // The particles the streaming pass listed: wall collisions in colloid order with
 // the reference's exact arithmetic (and, on the last substep, their run() record
-// and SRD binning), one particle per lane so the FP64 work fills whole warps.
+// and SRD binning).  Per round of up to blockDim.x particles (one per thread):
+// each thread loads its particle and finds its first collision; then the block's
+// collisions are gathered onto its first threads, rank by rank (a particle's
+// second collision follows its first), and each particle is finished by its own
+// thread.  blockDim.x <= 128.
 template <int FLAGS>
-__global__ void __launch_bounds__(128, 4) k_events(const SysF64 S, int l, int fb) {
+__global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
   constexpr int flags = FLAGS;
+  __shared__ EvState sst[128];
+  __shared__ int stask[128];
+  __shared__ int sntask;
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const int buf = (int)(gs & 1);
   const Fluid F = fluid_at(S, fb);
-  const int n = min(S.ss->nevents, S.events_cap);
-  // event i goes to block i % gridDim.x and, within it, to warp (i / gridDim.x) %
-  // warps: the few hundred to few thousand events of a substep spread over all SMs
-  // and over each SM's four schedulers instead of filling the first few
-  const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  for (int i = blockIdx.x + gridDim.x * k0; i < n; i += gridDim.x * blockDim.x) {
-    const EventRec r = S.evrec[i];
-    const int p = r.p;
-    double x = r.xy.x, y = r.xy.y, z = r.zwx.x, wx = r.zwx.y, wy = r.wywz.x, wz = r.wywz.y;
-    bool alias, wchanged = false;
-    int lin = cell_of_pos(S, x, y, z, alias);
-    ShellRec rec;
-    rec.n = 0;
-    near_colloids(S, flags, F.id[p], lin, alias, gs, buf, x, y, z, wx, wy, wz, wchanged, rec);
-    if ((flags & F_SHELL) && rec.n) {
-      int idx = atomicAdd(&S.ss->nshell, 1);
-      if (idx < S.shell_cap) S.shell[idx] = rec;
-      else atomicOr(&S.ss->err, ERRB_SHELL);
+  // F_PIPE: items 0..np-1 are the particles pending from earlier substeps of this
+  // step (their streaming of this substep is done here), items np.. the ones this
+  // substep's streaming pass listed; every item's state goes back to prec[i]
+  const int nn = min(S.ss->nnew[buf], S.events_cap);
+  const int np = (flags & F_PIPE) ? S.ss->npend : 0;
+  int n = np + nn;
+  if ((flags & F_PIPE) && n > S.pend_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&S.ss->err, ERRB_EVENTS);
+    n = S.pend_cap;
+  }
+  // item i goes to block i % gridDim.x: the items of a substep spread over all SMs
+  EvState &st = sst[threadIdx.x];
+  for (int base = 0;; base += blockDim.x) {
+    const int i = blockIdx.x + gridDim.x * (threadIdx.x + base);
+    const bool valid = i < n;
+    if (!__syncthreads_or(valid)) break;  // block-uniform trip count
+    const bool old = i < np;
+    st.j = -1;
+    if (valid) {
+      const EventRec r = old ? S.prec[i] : S.newrec[buf][i - np];
+      double x = r.xy.x, y = r.xy.y, z = r.zwx.x;
+      const double wx = r.zwx.y, wy = r.wywz.x, wz = r.wywz.y;
+      if ((flags & F_PIPE) && old) {
+        // update_pos_mpcd of a pending particle (as the streaming pass does it)
+        x = ref_mod(__dadd_rn(x, wx), S.dx);
+        y = ref_mod(__dadd_rn(y, wy), S.dy);
+        z = ref_mod(__dadd_rn(z, wz), S.dz);
+      }
+      bool alias;
+      const int lin = cell_of_pos(S, x, y, z, alias);
+      int cnt = 0;
+      if (!alias) {
+        cnt = tcount(S.Tcnt[buf][lin], gs);
+        cnt = cnt < TCAP ? cnt : TCAP;
+      }
+      st.x = x; st.y = y; st.z = z; st.wx = wx; st.wy = wy; st.wz = wz;
+      st.x0 = x; st.y0 = y; st.z0 = z;
+      st.vdx = st.vdy = st.vdz = 0.0;
+      st.p = r.p; st.id = r.id; st.lin = lin; st.last = -1; st.cnt = cnt;
+      st.alias = alias; st.dumped = false; st.changed = false;
+      if (flags & F_COLLIDE) st.j = ev_next_hit(S, st, buf);
     }
-    if (flags & F_BINROT) bin_for_rotation(S, p, x, y, z, wx, wy, wz);
-    if (flags & F_COLLIDE) { F.x[p] = x; F.y[p] = y; F.z[p] = z; }
-    if (wchanged) { F.wx[p] = wx; F.wy[p] = wy; F.wz[p] = wz; }
+    if (flags & F_COLLIDE) {
+      for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) sntask = 0;
+        __syncthreads();
+        if (st.j >= 0) stask[atomicAdd(&sntask, 1)] = threadIdx.x;
+        __syncthreads();
+        const int nt = sntask;
+        if (nt == 0) break;
+        if ((int)threadIdx.x < nt) {
+          EvState &t = sst[stask[threadIdx.x]];
+          ev_collide(S, t, t.j, gs, buf);
+          t.j = ev_next_hit(S, t, buf);
+        }
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const int p = st.p;
+      if (flags & F_SHELL) {
+        ShellRec rec;
+        ev_shell(S, st, buf, rec);
+        if (rec.n) {
+          int idx = atomicAdd(&S.ss->nshell, 1);
+          if (idx < S.shell_cap) S.shell[idx] = rec;
+          else atomicOr(&S.ss->err, ERRB_SHELL);
+        }
+      }
+      if (flags & F_BINROT) bin_for_rotation(S, p, st.x, st.y, st.z, st.wx, st.wy, st.wz);
+      if ((flags & F_PIPE) || st.changed) {
+        F.x[p] = st.x; F.y[p] = st.y; F.z[p] = st.z;
+        F.wx[p] = st.wx; F.wy[p] = st.wy; F.wz[p] = st.wz;
+      }
+      if (flags & F_PIPE) {
+        EventRec o;
+        o.xy = make_double2(st.x, st.y); o.zwx = make_double2(st.z, st.wx); o.wywz = make_double2(st.wy, st.wz);
+        o.p = p; o.id = st.id;
+        S.prec[i] = o;
+        if (flags & F_SHELL) S.pend[p] = 0;  // the last substep: back to the streaming pass next step
+      }
+    }
+    __syncthreads();  // the next round reuses the shared state
   }
 }
 
 StreamKernel stream_kernel(int flags) {
+  // substeps run overlapped (F_PIPE); the set-up pass stands alone
   switch (flags) {
-    case F_STREAM | F_COLLIDE: return k_stream<F_STREAM | F_COLLIDE>;
-    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_STREAM | F_COLLIDE | F_PIPE: return k_stream<F_STREAM | F_COLLIDE | F_PIPE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE:
+      return k_stream<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
     case F_SHELL | F_BINROT: return k_stream<F_SHELL | F_BINROT>;
   }
   return nullptr;
@@ -257,8 +340,8 @@ __global__ void __launch_bounds__(256) k_aux_b(const SysF64 *Ss, const int *boff
 
 EventKernel event_kernel(int flags) {
   switch (flags) {
-    case F_STREAM | F_COLLIDE: return k_events<F_COLLIDE>;
-    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_events<F_COLLIDE | F_SHELL | F_BINROT>;
+    case F_STREAM | F_COLLIDE | F_PIPE: return k_events<F_COLLIDE | F_PIPE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE: return k_events<F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
     case F_SHELL | F_BINROT: return k_events<F_SHELL | F_BINROT>;
   }
   return nullptr;
@@ -527,9 +610,27 @@ static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB,
   const long long g = step * S.n_sub + (l - 1);  // substep finished (l >= 1)
   const long long gn = g + 1;                    // substep advanced to
   if (j == 0 && lane == 0) {
-    S.ss->ev_total += S.ss->nevents;
-    S.ss->nevents = 0;  // the event list of the coming streaming pass
-    if ((mode & M_ADVANCE) && (gn % S.n_sub) == S.n_sub - 1) set_shift(S, step + 2);  // it bins for the next step
+    if (S.precision == MPCD_FP64) {
+      // the list substep g's streaming pass filled has been taken over by the event
+      // pass (into the pending list, empty again after the last substep); its
+      // buffer serves substep g+2.  The grid shift of the next step's binning is
+      // drawn two substeps ahead: the last streaming pass bins with it and runs
+      // beside the finish of the substep before it.
+      const int b = (int)(g & 1);
+      const int nn = S.ss->nnew[b];
+      S.ss->ev_total += nn;
+      S.ss->nnew[b] = 0;
+      if (mode & M_FINISH) {
+        const int np = S.ss->npend + (nn < S.events_cap ? nn : S.events_cap);
+        S.ss->npend = l >= S.n_sub ? 0 : (np < S.pend_cap ? np : S.pend_cap);
+      }
+      const int ahead = S.n_sub >= 2 ? S.n_sub - 2 : 0;
+      if ((mode & M_ADVANCE) && (gn % S.n_sub) == ahead) set_shift(S, step + 2);
+    } else {
+      S.ss->ev_total += S.ss->nevents;
+      S.ss->nevents = 0;  // the event list of the coming streaming pass
+      if ((mode & M_ADVANCE) && (gn % S.n_sub) == S.n_sub - 1) set_shift(S, step + 2);  // it bins for the next step
+    }
   }
   if (j >= S.Nc || lane >= 6) return;
   const unsigned grp = 0x3Fu;  // lanes 0-5
@@ -623,6 +724,8 @@ __global__ void __launch_bounds__(128) k_colloid_setup(const SysF64 S) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     set_shift(S, step + 1);
     S.ss->nevents = 0;
+    S.ss->nnew[0] = S.ss->nnew[1] = 0;
+    S.ss->npend = 0;
   }
   if (j >= S.Nc) return;
   const int b = (int)((g0 - 1) & 1);

@@ -14,7 +14,8 @@ enum : int {
   ERRB_OCCUPANCY = 8,   // a cell holds more particles than the exact cell sums allow
   ERRB_DISPLACE = 16,   // a wall collision moved a particle further than the cell-table margin
   ERRB_SHELLSLOTS = 32, // a particle sits in the rear shells of more colloids than a record holds
-  ERRB_DELTA = 64       // a colloid momentum exchange left the range of the exact sums
+  ERRB_DELTA = 64,      // a colloid momentum exchange left the range of the exact sums
+  ERRB_EVENTS = 128     // the wall-collision event (or pending-particle) lists overflowed
 };
 
 constexpr int TCAP = 16;     // colloids per cell in the fluid-to-colloid table
@@ -45,7 +46,7 @@ struct ExchAcc {
 // event pass starts from one record instead of an index and a gather
 struct __align__(16) EventRec {
   double2 xy, zwx, wywz;
-  int p, pad;
+  int p, id;  // slot in the fluid arrays and particle id
 };
 
 // quantities that change every step, kept on the device so one captured CUDA
@@ -54,7 +55,9 @@ struct StepState {
   long long step;   // completed MPCD steps
   int err;          // error bits
   int nshell;       // run() candidate records written
-  int nevents;      // particles the streaming pass left to k_events
+  int nevents;      // particles the streaming pass left to k_events (FP32 form)
+  int nnew[2];      // FP64 form: particles the streaming pass of substep g listed, [g & 1]
+  int npend;        // FP64 form: pending particles carried from earlier substeps of this step
   long long ev_total;  // events summed over substeps (diagnostics)
   double rr[3];     // grid shift of the SRD binning the next streaming pass performs
   float rrf[3];     // the same, FP32
@@ -126,7 +129,17 @@ struct SysF64 {
   // particles near a sphere surface in the substep in flight
   int *events;
   int events_cap;
-  EventRec *evrec;  // FP64 form: the listed particles' state as the streaming pass left it
+  // FP64 form, substeps overlapped: the streaming pass of substep g tests against
+  // the colloid positions of g-1 with the displacement bound as margin and lists
+  // the particles it cannot clear in newrec[g & 1]; each becomes pending (pend[p])
+  // for the rest of the step, its state kept in prec and advanced by the event
+  // passes, so a streaming pass never touches a particle an event pass may be
+  // changing at the same time
+  EventRec *newrec[2];
+  EventRec *prec;
+  int pend_cap;
+  uint8_t *pend;    // [N]
+  float cmarginf;   // the margin (the bound cmargin2 checks), FP32
   // FP32-compensated fluid (precision MPCD_FP32C): per particle one 16-byte record
   // {cell x | y << 10 | z << 20, offset x, offset y, offset z} with offsets in
   // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32
