@@ -53,7 +53,7 @@ struct mpcd_ctx {
   cudaStream_t aux = nullptr;    // second stream: colloid work beside the fluid passes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
-  cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_fin = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_finp[2] = {nullptr, nullptr};
   cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sorts][fluid buffer]
   int step_launches[2][2] = {{0, 0}, {0, 0}};
   int fbuf = 0;                  // fluid buffer holding the current state
@@ -194,6 +194,11 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
 }
 
 static void enq_fin_on(mpcd_ctx *c, cudaStream_t s, int mode, int l) {
+  if (c->S.fin_table) {
+    // a block of four warps per colloid: warp 0 the colloid, all four its cell table
+    launch_on(c, s, "k_fin", k_fin, c->S.Nc > 0 ? c->S.Nc : 1, 128, c->S, mode, l);
+    return;
+  }
   // one warp per colloid (warp j / grid of block j % grid): each SM's FP64 unit
   // serves the chains of a few colloids only
   int g = c->fin_grid > 0 ? c->fin_grid : c->n_sm;
@@ -239,7 +244,8 @@ static void enq_run_fluid(mpcd_ctx *c) {
 }
 
 // The substeps of the FP64 form, overlapped on three streams.  Per substep l:
-//   main   k_stream(l)            needs k_stream(l-1) and k_aux(l-1) (cell table of l)
+//   main   k_stream(l)            needs k_stream(l-1) and k_fin(l-2) (cell table of l,
+//                                  positions of l-1)
 //   events k_events(l), k_fin(l)  need k_stream(l); k_fin also k_aux(l)
 //   aux    k_aux(l)               needs k_fin(l-1) (the positions of substep l)
 // so the streaming pass of l+1, bandwidth-bound, runs beside the event pass and the
@@ -255,12 +261,13 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
   if (nc) cudaStreamWaitEvent(c->aux, c->ev_start, 0);
   for (int l = 1; l <= n; ++l) {
     const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
-    if (l >= 2 && nc) cudaStreamWaitEvent(c->stream, c->ev_aux, 0);
+    // the cell table of l and the positions of l-1 come from k_fin(l-2)
+    if (l >= 3) cudaStreamWaitEvent(c->stream, c->ev_finp[l & 1], 0);
     launch(c, stream_name(flags), stream_kernel(flags), blocks_for(c->S.N, 256 * stream64_per_thread(flags)), 256,
            c->S, l, c->fbuf);
     cudaEventRecord(c->ev_str, c->stream);
     if (nc) {
-      if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_fin, 0);
+      if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
       launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, l >= 2 ? 1 : 0);
       cudaEventRecord(c->ev_aux, c->aux);
     }
@@ -269,9 +276,9 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
               l, c->fbuf);
     if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
     enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
-    cudaEventRecord(c->ev_fin, c->evs);
+    cudaEventRecord(c->ev_finp[l & 1], c->evs);
   }
-  cudaStreamWaitEvent(c->stream, c->ev_fin, 0);
+  cudaStreamWaitEvent(c->stream, c->ev_finp[n & 1], 0);
 }
 
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
@@ -430,7 +437,10 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   S.precision = p.precision;
-  S.aux_nw = 4;
+  // the FP64 form builds the cell tables in the colloid finish: its side kernel
+  // needs two warps per colloid (forces; orientation), the FP32 form's four
+  S.fin_table = p.precision == MPCD_FP64 ? 1 : 0;
+  S.aux_nw = S.fin_table ? 2 : 4;
   S.dtf = (float)dt;
   S.vmaxf = (float)vmax;
   // the FP64 form sums displacements w = v dt, the FP32 form velocities
@@ -528,7 +538,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
       cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_str, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_aux, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_fin, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_finp[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_finp[1], cudaEventDisableTiming) != cudaSuccess) {
     mpcd_destroy(c);
     return MPCD_ERR_CUDA;
   }
@@ -556,7 +567,7 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   if (c->evs) cudaStreamDestroy(c->evs);
-  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_fin})
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
   delete c;
   return MPCD_OK;
@@ -744,7 +755,7 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
   if (which == MPCD_LAUNCH_AUX) {
     if (grid > 0 && block != 64 && block != 128 && block != 256)
       return fail(c, MPCD_ERR_PARAM, "colloid side work: 64, 128 or 256 threads per colloid");
-    c->S.aux_nw = grid > 0 ? block / 32 : 4;
+    c->S.aux_nw = grid > 0 ? block / 32 : (c->S.fin_table ? 2 : 4);
     return drop_graph(c);
   }
   if (grid > 65535 || (grid > 0 && (block < 32 || block > 128 || block % 32)))

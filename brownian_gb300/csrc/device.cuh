@@ -203,25 +203,34 @@ static __device__ __forceinline__ double cd_next(CollDraw &d) {
 }
 
 // stochastic_reflection (cpp/fluid_colloid_collision.cpp:7-24): Rayleigh normal
-// speed along rs plus one Gaussian tangential component along unit(un x t)
-//
+// speed along rs plus one Gaussian tangential component along unit(un x t).
 // Draws in the reference's order: u, the three components of t, then pairs of
-// Box-Muller tries.  The first eight come from two Philox blocks taken up front,
-// so the three independent chains (the unit normal, the Rayleigh speed, the
-// Gaussian) are straight-line code that overlaps; a third block onwards serves
-// the rare case of two rejected tries.
-static __device__ d3 stochastic_reflection(const SysF64 &S, CollDraw &d, d3 rf, d3 rs) {
-  const uint4 r0 = draw4(d.key, DOM_COLL, 0, d.a, d.b, d.t), r1 = draw4(d.key, DOM_COLL, 1, d.a, d.b, d.t);
-  d.idx = 8;
-  double om = __dsub_rn(1.0, u01(r0.x));
-  double random_e = __dmul_rn(om, om);
-  // polar Box-Muller rejection; each try is a fixed function of the key, and a
-  // try is rejected with probability 1 - pi/4, so 256 tries never run out
-  // (2 ran - 1 is exact: pm1 builds it from the draw's bits)
+// Box-Muller tries.  The first eight come from two Philox blocks (refl_blocks); a
+// third block onwards serves the rare case of two rejected tries.  The four
+// independent chains below (Rayleigh speed, Gaussian, unit normal, t) are separate
+// functions so that the event pass can run them on different warps; refl_combine
+// joins them.  Each is the same sequence of rounded operations wherever it runs.
+static __device__ __forceinline__ void refl_blocks(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, uint4 &r0,
+                                                   uint4 &r1) {
+  r0 = draw4(S.key, DOM_COLL, 0, a, b, t);
+  r1 = draw4(S.key, DOM_COLL, 1, a, b, t);
+}
+
+// the Rayleigh speed: sqrt(-log((1 - u)^2) kT/m)  (/m_beta as * kT/m)
+static __device__ __forceinline__ double refl_speed(const SysF64 &S, uint4 r0) {
+  const double om = __dsub_rn(1.0, u01(r0.x));
+  const double random_e = __dmul_rn(om, om);
+  return __dsqrt_rn(__dmul_rn(-log(random_e), S.inv_m_beta));
+}
+
+// the tangential Gaussian x1 sqrt(-2 log z / z) sqrt(kT/m), polar Box-Muller: each
+// try is a fixed function of the key, a try is rejected with probability 1 - pi/4,
+// so 256 tries never run out.  The second try is computed by every lane and
+// selected (2 ran - 1 is exact: pm1 builds it from the draw's bits); only two
+// rejections in a row (1 in 22) branch.
+static __device__ __forceinline__ double refl_gauss(const SysF64 &S, uint4 r1, uint32_t a, uint32_t b, uint32_t t) {
   double x1 = pm1(r1.x), x2 = pm1(r1.y);
   double z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
-  // the second try is computed by every lane and selected, so the lanes of a warp
-  // stay together; only two rejections in a row (1 in 22) branch
   const double x1b = pm1(r1.z), x2b = pm1(r1.w);
   const double zb = __dadd_rn(__dmul_rn(x1b, x1b), __dmul_rn(x2b, x2b));
   const bool second = z > 1.0;
@@ -229,26 +238,42 @@ static __device__ d3 stochastic_reflection(const SysF64 &S, CollDraw &d, d3 rf, 
   x2 = second ? x2b : x2;
   z = second ? zb : z;
   if (z > 1.0) {
+    CollDraw d;
+    d.key = S.key; d.a = a; d.b = b; d.t = t; d.idx = 8;
     for (int it = 2; z > 1.0 && it < 256; ++it) {
       x1 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
       x2 = __dsub_rn(__dmul_rn(2.0, cd_next(d)), 1.0);
       z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
     }
   }
-  const double lre = log(random_e), lz = log(z);
-  // vector / |vector| as one reciprocal and three products (within an ulp of the
-  // reference's three divisions); likewise /m_beta as * kT/m
-  d3 n = mul3s(rs, __drcp_rn(__dsqrt_rn(norm2_ref(rs.x, rs.y, rs.z))));
-  double val = __dsqrt_rn(__dmul_rn(-lre, S.inv_m_beta));
-  double g = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lz), z));
-  d3 un = mul3s(n, val);
-  d3 t = mk(ref_img(__dsub_rn(__dmul_rn(u01(r0.y), S.dx.L), rf.x), S.dx),
+  const double g = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(z)), z));
+  return __dmul_rn(__dmul_rn(x1, g), S.sqrt_kt_m);
+}
+
+// vector / |vector| as one reciprocal and three products (within an ulp of the
+// reference's three divisions)
+static __device__ __forceinline__ d3 refl_unit(d3 v) { return mul3s(v, __drcp_rn(__dsqrt_rn(norm2_ref(v.x, v.y, v.z)))); }
+
+// t = img(ran L - rf), the random point relative to the particle
+static __device__ __forceinline__ d3 refl_point(const SysF64 &S, uint4 r0, d3 rf) {
+  return mk(ref_img(__dsub_rn(__dmul_rn(u01(r0.y), S.dx.L), rf.x), S.dx),
             ref_img(__dsub_rn(__dmul_rn(u01(r0.z), S.dy.L), rf.y), S.dy),
             ref_img(__dsub_rn(__dmul_rn(u01(r0.w), S.dz.L), rf.z), S.dz));
-  d3 ut = cross_ref(un, t);
-  ut = mul3s(ut, __drcp_rn(__dsqrt_rn(norm2_ref(ut.x, ut.y, ut.z))));
-  double v1 = __dmul_rn(__dmul_rn(x1, g), S.sqrt_kt_m);
+}
+
+// u = unit(un x t) v1 + un, un = n val
+static __device__ __forceinline__ d3 refl_combine(d3 n, double val, d3 t, double v1) {
+  const d3 un = mul3s(n, val);
+  const d3 ut = refl_unit(cross_ref(un, t));
   return add3(mul3s(ut, v1), un);
+}
+
+static __device__ d3 stochastic_reflection(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, d3 rf, d3 rs) {
+  uint4 r0, r1;
+  refl_blocks(S, a, b, t, r0, r1);
+  const double val = refl_speed(S, r0);
+  const double v1 = refl_gauss(S, r1, a, b, t);
+  return refl_combine(refl_unit(rs), val, refl_point(S, r0, rf), v1);
 }
 
 // ------------------------------------------------------------ particle stream
@@ -352,9 +377,7 @@ static __device__ __noinline__ void ev_collide(const SysF64 &S, EvState &st, int
   y = ref_mod(__dsub_rn(y, __dmul_rn(wy, 0.5)), S.dy);
   z = ref_mod(__dsub_rn(z, __dmul_rn(wz, 0.5)), S.dz);
   d3 rs = mk(ref_img(__dsub_rn(x, Xj.x), S.dx), ref_img(__dsub_rn(y, Xj.y), S.dy), ref_img(__dsub_rn(z, Xj.z), S.dz));
-  CollDraw d;
-  d.key = S.key; d.a = (uint32_t)(st.id + 1); d.b = (uint32_t)(j + 1); d.t = (uint32_t)gs; d.idx = 0;
-  d3 u = stochastic_reflection(S, d, mk(x, y, z), rs);
+  d3 u = stochastic_reflection(S, (uint32_t)(st.id + 1), (uint32_t)(j + 1), (uint32_t)gs, mk(x, y, z), rs);
   d3 vn = add3(add3(u, Vj), cross_ref(Wj, rs));
   d3 dv = sub3(mk(st.vdx, st.vdy, st.vdz), vn);
   d3 dl = cross_ref(rs, dv);
@@ -370,6 +393,92 @@ static __device__ __noinline__ void ev_collide(const SysF64 &S, EvState &st, int
   if (norm2_ref(ex, ey, ez) > S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
   st.x = x; st.y = y; st.z = z; st.wx = wx; st.wy = wy; st.wz = wz;
   st.changed = true;
+}
+
+// Per-task scratch of a cooperative collision (ev_collide_coop)
+struct CollScratch {
+  double xb[3], rs[3], n[3], tp[3], wr[3], vd[3];
+  double val, v1;
+};
+
+// The same collision as ev_collide for up to 32 gathered particles at once
+// (tasks k0.. of stask), by all four warps of a 128-thread block: lane t of each
+// warp takes task k0 + t, and the warps, one per SM scheduler, run the
+// collision's independent FP64 chains side by side (warp 0: the step back and
+// the unit normal; 1: the Rayleigh speed; 2: the Gaussian; 3: t, W x rs and the
+// velocity at the start of the collision routine); warp 0 then joins them.  Every
+// value is the same sequence of rounded operations as in ev_collide, so the
+// results are identical.  Called by every thread of the block.
+static __device__ void ev_collide_coop(const SysF64 &S, EvState *sst, const int *stask, int k0, int nt, long long gs,
+                                       int buf, CollScratch *cs) {
+  const int w = threadIdx.x >> 5, t = threadIdx.x & 31, k = k0 + t;
+  const bool act = k < nt;
+  const double *Xc = S.X[buf];
+  d3 Vj = mk(0, 0, 0);
+  if (act) {
+    const EvState &st = sst[stask[k]];
+    const int j = st.j;
+    const uint32_t a = (uint32_t)(st.id + 1), b = (uint32_t)(j + 1), tt = (uint32_t)gs;
+    CollScratch &c = cs[t];
+    if (w == 0 || w == 3) {
+      // half a substep back with the current velocity, and the particle relative to the colloid
+      const d3 Xj = mk(Xc[3 * j], Xc[3 * j + 1], Xc[3 * j + 2]);
+      if (w == 0) Vj = mk(S.V[3 * j], S.V[3 * j + 1], S.V[3 * j + 2]);  // used after the join
+      const double x = ref_mod(__dsub_rn(st.x, __dmul_rn(st.wx, 0.5)), S.dx);
+      const double y = ref_mod(__dsub_rn(st.y, __dmul_rn(st.wy, 0.5)), S.dy);
+      const double z = ref_mod(__dsub_rn(st.z, __dmul_rn(st.wz, 0.5)), S.dz);
+      const d3 rs = mk(ref_img(__dsub_rn(x, Xj.x), S.dx), ref_img(__dsub_rn(y, Xj.y), S.dy),
+                       ref_img(__dsub_rn(z, Xj.z), S.dz));
+      if (w == 0) {
+        c.xb[0] = x; c.xb[1] = y; c.xb[2] = z;
+        c.rs[0] = rs.x; c.rs[1] = rs.y; c.rs[2] = rs.z;
+        const d3 n = refl_unit(rs);
+        c.n[0] = n.x; c.n[1] = n.y; c.n[2] = n.z;
+      } else {
+        const d3 Wj = mk(S.W[3 * j], S.W[3 * j + 1], S.W[3 * j + 2]);
+        const d3 tp = refl_point(S, draw4(S.key, DOM_COLL, 0, a, b, tt), mk(x, y, z));
+        const d3 wr = cross_ref(Wj, rs);
+        c.tp[0] = tp.x; c.tp[1] = tp.y; c.tp[2] = tp.z;
+        c.wr[0] = wr.x; c.wr[1] = wr.y; c.wr[2] = wr.z;
+        // dump_vel_fl: the velocity when the collision routine began
+        if (st.dumped) {
+          c.vd[0] = st.vdx; c.vd[1] = st.vdy; c.vd[2] = st.vdz;
+        } else {
+          c.vd[0] = __dmul_rn(st.wx, S.inv_dt); c.vd[1] = __dmul_rn(st.wy, S.inv_dt); c.vd[2] = __dmul_rn(st.wz, S.inv_dt);
+        }
+      }
+    } else if (w == 1) {
+      c.val = refl_speed(S, draw4(S.key, DOM_COLL, 0, a, b, tt));
+    } else {
+      c.v1 = refl_gauss(S, draw4(S.key, DOM_COLL, 1, a, b, tt), a, b, tt);
+    }
+  }
+  __syncthreads();
+  if (w == 0 && act) {
+    EvState &st = sst[stask[k]];
+    const int j = st.j;
+    const CollScratch &c = cs[t];
+    const d3 u = refl_combine(mk(c.n[0], c.n[1], c.n[2]), c.val, mk(c.tp[0], c.tp[1], c.tp[2]), c.v1);
+    const d3 vn = add3(add3(u, Vj), mk(c.wr[0], c.wr[1], c.wr[2]));
+    const d3 vd = mk(c.vd[0], c.vd[1], c.vd[2]);
+    const d3 dv = sub3(vd, vn);
+    const d3 dl = cross_ref(mk(c.rs[0], c.rs[1], c.rs[2]), dv);
+    exch_add6(S.exch + j, dv, dl, &S.ss->err);
+    const double wx = __dmul_rn(vn.x, S.dt), wy = __dmul_rn(vn.y, S.dt), wz = __dmul_rn(vn.z, S.dt);
+    // step forward half a substep with the new velocity
+    const double x = ref_mod(__dadd_rn(c.xb[0], __dmul_rn(wx, 0.5)), S.dx);
+    const double y = ref_mod(__dadd_rn(c.xb[1], __dmul_rn(wy, 0.5)), S.dy);
+    const double z = ref_mod(__dadd_rn(c.xb[2], __dmul_rn(wz, 0.5)), S.dz);
+    // the cell table is built with a margin; a move beyond it could hide a colloid
+    const double ex = ref_img(__dsub_rn(x, st.x0), S.dx), ey = ref_img(__dsub_rn(y, st.y0), S.dy),
+                 ez = ref_img(__dsub_rn(z, st.z0), S.dz);
+    if (norm2_ref(ex, ey, ez) > S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
+    st.x = x; st.y = y; st.z = z; st.wx = wx; st.wy = wy; st.wz = wz;
+    st.vdx = vd.x; st.vdy = vd.y; st.vdz = vd.z;
+    st.dumped = true;
+    st.changed = true;
+  }
+  __syncthreads();
 }
 
 // run() candidate record of the particle at its final position: the colloids, in
@@ -550,7 +659,7 @@ static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, in
     d3 fn = wca_force(S, S.X[b], S.Xf[b], j, lane, false, pot);
     if (lane == 0) stv(S.fnew, j, fn);
   }
-  if (w >= 2 || (w == 0 && nw == 2)) {
+  if (!S.fin_table && (w >= 2 || (w == 0 && nw == 2))) {
     const long long e = g + 1;
     unsigned long long *Tc = S.Tcnt[e & 1];
     uint16_t *Tl = S.Tlist[e & 1];

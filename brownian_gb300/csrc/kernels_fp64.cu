@@ -216,6 +216,7 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
   __shared__ EvState sst[128];
   __shared__ int stask[128];
   __shared__ int sntask;
+  __shared__ CollScratch scs[32];
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const int buf = (int)(gs & 1);
@@ -271,7 +272,13 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
         __syncthreads();
         const int nt = sntask;
         if (nt == 0) break;
-        if ((int)threadIdx.x < nt) {
+        if (blockDim.x == 128) {
+          for (int k0 = 0; k0 < nt; k0 += 32) ev_collide_coop(S, sst, stask, k0, nt, gs, buf, scs);
+          if ((int)threadIdx.x < nt) {
+            EvState &t = sst[stask[threadIdx.x]];
+            t.j = ev_next_hit(S, t, buf);
+          }
+        } else if ((int)threadIdx.x < nt) {
           EvState &t = sst[stask[threadIdx.x]];
           ev_collide(S, t, t.j, gs, buf);
           t.j = ev_next_hit(S, t, buf);
@@ -603,13 +610,18 @@ __device__ __forceinline__ void set_shift(const SysF64 &S, long long nn) {
 // the following substep (update_pos_md, cpp/update.cpp:48-54).  In the fused step
 // the orientation update of substeps 1..n-1 runs in the next streaming pass
 // instead (colloid_aux), off the critical path.
+static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int lane, int mode, long long g,
+                                                     long long gn);
+
 static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB, const int NVB, int mode, int l) {
   const int lane = threadIdx.x & 31;
-  const int j = VB + NVB * (threadIdx.x >> 5);
+  // with fin_table a block per colloid (warp 0 the colloid, all warps its cell
+  // table), else a warp per colloid
+  const int j = S.fin_table ? VB : VB + NVB * (threadIdx.x >> 5);
   const long long step = S.ss->step;
   const long long g = step * S.n_sub + (l - 1);  // substep finished (l >= 1)
   const long long gn = g + 1;                    // substep advanced to
-  if (j == 0 && lane == 0) {
+  if (VB == 0 && threadIdx.x == 0) {
     if (S.precision == MPCD_FP64) {
       // the list substep g's streaming pass filled has been taken over by the event
       // pass (into the pending list, empty again after the last substep); its
@@ -632,7 +644,29 @@ static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB,
       if ((mode & M_ADVANCE) && (gn % S.n_sub) == S.n_sub - 1) set_shift(S, step + 2);  // it bins for the next step
     }
   }
-  if (j >= S.Nc || lane >= 6) return;
+  if (j >= S.Nc) return;  // (j is the block's or the warp's)
+  if (!S.fin_table) {
+    if (lane < 6) k_fin_colloid(S, j, lane, mode, g, gn);
+    return;
+  }
+  if (threadIdx.x < 6) k_fin_colloid(S, j, lane, mode, g, gn);
+  if (mode & M_ADVANCE) {
+    // the cell table of substep gn+1 from the new position, by the whole block: the
+    // streaming pass of gn+1 then needs this kernel only, not the side kernel of gn
+    __syncthreads();
+    const int nxt = (int)(gn & 1);
+    const long long e = gn + 1;
+    unsigned long long *Tc = S.Tcnt[e & 1];
+    uint16_t *Tl = S.Tlist[e & 1];
+    int *err = &S.ss->err;
+    for_reach_cells(S, S.cbox[nxt][j], S.Xf[nxt][j], table_reach(S, e), threadIdx.x, blockDim.x,
+                    [&](int cell) { tappend(Tc, Tl, cell, e, j, err); });
+  }
+}
+
+// the per-colloid part of k_fin on lanes 0-5
+static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int lane, int mode, long long g,
+                                                     long long gn) {
   const unsigned grp = 0x3Fu;  // lanes 0-5
   const int k = lane < 3 ? lane : lane - 3;
   const bool lin = lane < 3;

@@ -140,6 +140,8 @@ struct SysF64 {
   int pend_cap;
   uint8_t *pend;    // [N]
   float cmarginf;   // the margin (the bound cmargin2 checks), FP32
+  int fin_table;    // FP64 form: the colloid finish of substep g builds the cell table of
+                    // g+2 (else the side kernel of g+1 does)
   // FP32-compensated fluid (precision MPCD_FP32C): per particle one 16-byte record
   // {cell x | y << 10 | z << 20, offset x, offset y, offset z} with offsets in
   // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32
