@@ -183,6 +183,7 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
   }
   launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags),
          blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread() : stream64_per_thread(flags))), 256, c->S, l, fb);
+  if (!f32 && (flags & F_PIPE) && (flags & F_BINROT)) launch(c, "k_bin", k_bin, c->n_sm * 8, 256, c->S, fb);
   if (fork) {
     launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act);
     cudaEventRecord(c->ev_join, c->aux);
@@ -266,6 +267,8 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
     launch(c, stream_name(flags), stream_kernel(flags), blocks_for(c->S.N, 256 * stream64_per_thread(flags)), 256,
            c->S, l, c->fbuf);
     cudaEventRecord(c->ev_str, c->stream);
+    // the last substep's binning beside its event pass and colloid finish
+    if (l == n) launch(c, "k_bin", k_bin, c->n_sm * 8, 256, c->S, c->fbuf);
     if (nc) {
       if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
       launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, l >= 2 ? 1 : 0);

@@ -31,6 +31,7 @@ __global__ void k_gather_err(const SysF64 *Ss, int nrep, int *out);
 StreamKernel stream_kernel32(int flags);
 int stream32_per_thread();  // particles per thread of the FP32 streaming pass
 int stream64_per_thread(int flags);  // particles per thread of the FP64 streaming pass
+__global__ void k_bin(const SysF64 S, int fb);
 EventKernel event_kernel32(int flags);
 __global__ void k_cell_prep32(__grid_constant__ const SysF64 S);
 __global__ void k_rotate32(__grid_constant__ const SysF64 S, int fb);

@@ -23,27 +23,44 @@
 #include "device.cuh"
 
 namespace bgb {
-// the exact sums of the SRD binning for the next step: cell number, count, w, |w|^2
-__device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double x, double y, double z, double wx,
-                                                 double wy, double wz) {
+// One particle's part of the SRD binning for the next step: its cell (recorded
+// in rotcell) and the fixed-point w and |w|^2 the exact cell sums add up
+struct BinTerm {
+  int c;
+  long long fx, fy, fz, f2;
+};
+
+__device__ __forceinline__ BinTerm bin_term(const SysF64 &S, int p, double x, double y, double z, double wx,
+                                            double wy, double wz) {
   // (1 + mod(pos + rr, len).cell(len), cpp/rotation_mpcd.cpp:11)
   const double *rr = S.ss->rr;
   double ax = ref_mod(__dadd_rn(x, rr[0]), S.dx), ay = ref_mod(__dadd_rn(y, rr[1]), S.dy),
          az = ref_mod(__dadd_rn(z, rr[2]), S.dz);
   bool alias;
-  int c = cell_of_pos(S, ax, ay, az, alias);
-  S.rotcell[p] = c;
+  BinTerm t;
+  t.c = cell_of_pos(S, ax, ay, az, alias);
+  S.rotcell[p] = t.c;
   long long ax_ = dbits(wx) & 0x7FFFFFFFFFFFFFFFll, ay_ = dbits(wy) & 0x7FFFFFFFFFFFFFFFll,
             az_ = dbits(wz) & 0x7FFFFFFFFFFFFFFFll;
   if (ax_ > S.wlim_bits || ay_ > S.wlim_bits || az_ > S.wlim_bits) atomicOr(&S.ss->err, ERRB_VRANGE);
-  long long fx = to_fix(wx, S.kw), fy = to_fix(wy, S.kw), fz = to_fix(wz, S.kw);
-  long long f2 = sq_fix(fx, S.kw) + sq_fix(fy, S.kw) + sq_fix(fz, S.kw);
-  CellAcc *a = S.acc + c;
-  atomicAdd(&a->n, 1);
+  t.fx = to_fix(wx, S.kw); t.fy = to_fix(wy, S.kw); t.fz = to_fix(wz, S.kw);
+  t.f2 = sq_fix(t.fx, S.kw) + sq_fix(t.fy, S.kw) + sq_fix(t.fz, S.kw);
+  return t;
+}
+
+__device__ __forceinline__ void bin_add(CellAcc *a, int n, long long fx, long long fy, long long fz, long long f2) {
+  atomicAdd(&a->n, n);
   atomicAdd((unsigned long long *)&a->sx, (unsigned long long)fx);
   atomicAdd((unsigned long long *)&a->sy, (unsigned long long)fy);
   atomicAdd((unsigned long long *)&a->sz, (unsigned long long)fz);
   atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
+}
+
+// the exact sums of the SRD binning for the next step: cell number, count, w, |w|^2
+__device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double x, double y, double z, double wx,
+                                                 double wy, double wz) {
+  const BinTerm t = bin_term(S, p, x, y, z, wx, wy, wz);
+  bin_add(S.acc + t.c, 1, t.fx, t.fy, t.fz, t.f2);
 }
 
 // FLAGS: F_* bits.  l: substep (1..n_sub) whose streaming this is; 0 for the
@@ -81,6 +98,7 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
   // belong to the event passes and are skipped
   const int xb = (flags & F_PIPE) ? (int)((gs - 1) & 1) : buf;
   const float mg = (flags & F_PIPE) ? S.cmarginf : 0.f;
+
   double x[U], y[U], z[U], wx[U], wy[U], wz[U];
   bool valid[U], ev[U];
   unsigned members[U];  // run() shell members among the cell-table slots
@@ -307,19 +325,31 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
         o.xy = make_double2(st.x, st.y); o.zwx = make_double2(st.z, st.wx); o.wywz = make_double2(st.wy, st.wz);
         o.p = p; o.id = st.id;
         S.prec[i] = o;
-        if (flags & F_SHELL) S.pend[p] = 0;  // the last substep: back to the streaming pass next step
       }
     }
     __syncthreads();  // the next round reuses the shared state
   }
 }
 
+// The SRD binning of the particles the last streaming pass of a step finished
+// (the pending ones are binned by the event pass): a pass of its own, so that
+// its atomics run beside that substep's event pass and colloid finish.  Pending
+// marks stay set until the next step's rotation clears them.
+__global__ void __launch_bounds__(256) k_bin(const SysF64 S, int fb) {
+  const Fluid F = fluid_at(S, fb);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.N; p += gridDim.x * blockDim.x) {
+    if (S.pend[p]) continue;
+    bin_for_rotation(S, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
+  }
+}
+
 StreamKernel stream_kernel(int flags) {
-  // substeps run overlapped (F_PIPE); the set-up pass stands alone
+  // substeps run overlapped (F_PIPE; the last one's binning is k_bin); the set-up
+  // pass stands alone
   switch (flags) {
     case F_STREAM | F_COLLIDE | F_PIPE: return k_stream<F_STREAM | F_COLLIDE | F_PIPE>;
     case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE:
-      return k_stream<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
+      return k_stream<F_STREAM | F_COLLIDE | F_SHELL | F_PIPE>;
     case F_SHELL | F_BINROT: return k_stream<F_SHELL | F_BINROT>;
   }
   return nullptr;
@@ -470,6 +500,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks_b(const SysF64 *Ss, const 
 __global__ void __launch_bounds__(256) k_rotate_sort(const SysF64 S, int src, int dst) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= S.N) return;
+  S.pend[p] = 0;  // no particle is pending at the start of a step
   const Fluid F = fluid_at(S, src), G = fluid_at(S, dst);
   const int c = S.rotcell[p];
   double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
@@ -506,6 +537,7 @@ __global__ void __launch_bounds__(256) k_rotate_sort(const SysF64 S, int src, in
 __global__ void __launch_bounds__(256) k_rotate(const SysF64 S, int fb) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= S.N) return;
+  S.pend[p] = 0;  // no particle is pending at the start of a step
   const int c = S.rotcell[p];
   if (c >= S.C) return;
   const Fluid F = fluid_at(S, fb);
