@@ -31,7 +31,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
            "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
            "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
-           "mpcd_surrogate_features", "mpcd_surrogate_step"]
+           "mpcd_surrogate_features", "mpcd_surrogate_step", "mpcd_updown_velocity"]
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
@@ -103,6 +103,7 @@ def lib():
         L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.mpcd_fluid_sums_noalloc.argtypes = [vp, C.c_int64, C.c_double, vp, vp]
         L.mpcd_exchange_read.argtypes = [vp, dp, C.c_int]
+        L.mpcd_updown_velocity.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp]
         L.mpcd_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
         L.mpcd_ensemble_destroy.argtypes = [vp]
         L.mpcd_ensemble_last_error.argtypes = [vp]
@@ -218,6 +219,31 @@ class Simulation:
         out = np.empty((self.Nc, 6))
         self._ck(lib().mpcd_exchange_read(self.h, _dp(out), 1 if reset else 0))
         return out
+
+    def updown_velocity(self):
+        """updown_velocity (cpp/run.cpp:28-50) on the current state.  Per colloid: `cnt`, `up_cnt`
+        (rear-side fluid within sigma/2 + 0.5 and sigma/2 + 0.1), `vel_sum`, `up_vel_sum` (their
+        velocity sums) and the slip velocities `vel` = vel_sum/cnt - V, `up_vel` = up_vel_sum/up_cnt
+        - V (where the shell is empty, zero).  `reference` restates the routine's own arithmetic: its
+        `vel` (cpp/run.cpp:48, taken only where up_cnt > 0, else the raw sum) and its `up_vel`, a
+        single vector carried over the colloids (cpp/run.cpp:45-47)."""
+        n = self.Nc
+        cnt, up_cnt = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        vs, us = np.zeros((n, 3)), np.zeros((n, 3))
+        self._ck(lib().mpcd_updown_velocity(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            up_cnt.ctypes.data_as(C.POINTER(C.c_int32)), _dp(vs), _dp(us)))
+        V = self.get_colloids()["vel_colloid"]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            vel = np.where(cnt[:, None] > 0, vs / np.maximum(cnt, 1)[:, None] - V, 0.0)
+            up_vel = np.where(up_cnt[:, None] > 0, us / np.maximum(up_cnt, 1)[:, None] - V, 0.0)
+        ref_vel = np.empty((n, 3))
+        acc = np.zeros(3)
+        for i in range(n):
+            acc = acc + us[i]
+            acc = acc / up_cnt[i] - V[i] if up_cnt[i] > 0 else acc
+            ref_vel[i] = vs[i] / cnt[i] - V[i] if up_cnt[i] > 0 else vs[i]
+        return dict(cnt=cnt, up_cnt=up_cnt, vel_sum=vs, up_vel_sum=us, vel=vel, up_vel=up_vel,
+                    reference=dict(vel=ref_vel, up_vel=acc))
 
     def get_colloids(self):
         """The colloid arrays only (no fluid transfer)."""

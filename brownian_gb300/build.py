@@ -23,7 +23,8 @@ OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libbrownian_gb300.so")
 SHIM = os.path.join(OUT, "libbrownian_shim.so")
 
-SOURCES = ["kernels_fp64.cu", "kernels_fp32c.cu", "init_fp64.cu", "context.cu", "noalloc.cu", "mlp.cu", "surrogate.cu"]
+SOURCES = ["kernels_fp64.cu", "kernels_fp32c.cu", "init_fp64.cu", "context.cu", "noalloc.cu", "mlp.cu", "surrogate.cu",
+           "diag.cu"]
 SHIM_SOURCES = ["shim.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "--extended-lambda", "-lineinfo",
               "-Xcompiler", "-fPIC,-ffp-contract=off"]

@@ -77,6 +77,12 @@ struct mpcd_ctx {
   int nblk = 0;                  // 256-cell blocks of the counting sort
   int n_sm = 152;                // multiprocessors of the device
   int ev_grid = 0, ev_block = 128;   // k_events launch shape (grid 0: one block per SM)
+  // updown_velocity scratch, allocated on first use
+  unsigned long long *ud_Tc = nullptr;
+  uint16_t *ud_Tl = nullptr;
+  int *ud_cnt = nullptr;
+  ExchAcc *ud_acc = nullptr;
+  long long ud_epoch = -1;
   int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
 };
 
@@ -570,6 +576,8 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   if (c->evs) cudaStreamDestroy(c->evs);
+  for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc})
+    if (q) cudaFree(q);
   for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
   delete c;
@@ -1014,6 +1022,50 @@ extern "C" int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset) {
   if (reset) {
     CUDA_OK(c, cudaMemsetAsync(c->S.xacc, 0, nb, c->stream));
     CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  }
+  return MPCD_OK;
+}
+
+// updown_velocity (cpp/run.cpp:28-50) on the current state: per colloid the
+// number of fluid particles in its run() shell and in its inner shell (rear side,
+// r.V <= 0) and the sums of their velocities
+extern "C" int mpcd_updown_velocity(mpcd_ctx *c, int32_t *cnt, int32_t *up_cnt, double *vel_sum,
+                                    double *up_vel_sum) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  const SysF64 &S = c->S;
+  if (!S.Nc) return MPCD_OK;
+  if (!c->ud_Tc) {
+    if (cudaMalloc(&c->ud_Tc, sizeof(unsigned long long) * (size_t)S.C) != cudaSuccess ||
+        cudaMalloc(&c->ud_Tl, sizeof(uint16_t) * (size_t)S.C * TCAP) != cudaSuccess ||
+        cudaMalloc(&c->ud_cnt, sizeof(int) * 2 * (size_t)S.Nc) != cudaSuccess ||
+        cudaMalloc(&c->ud_acc, sizeof(ExchAcc) * (size_t)S.Nc) != cudaSuccess)
+      return fail(c, MPCD_ERR_NOMEM, "updown_velocity scratch");
+    CUDA_OK(c, cudaMemsetAsync(c->ud_Tc, 0, sizeof(unsigned long long) * (size_t)S.C, c->stream));
+  }
+  CUDA_OK(c, cudaMemsetAsync(c->ud_cnt, 0, sizeof(int) * 2 * (size_t)S.Nc, c->stream));
+  CUDA_OK(c, cudaMemsetAsync(c->ud_acc, 0, sizeof(ExchAcc) * (size_t)S.Nc, c->stream));
+  const long long e = ++c->ud_epoch;  // a stale entry of an earlier call reads as empty
+  const double sh_up = c->p.sigma * 0.5 + 0.1;
+  const double rup2 = pow(sh_up, 2);  // cpp/run.cpp:39
+  launch(c, "k_updown_table", k_updown_table, colloid_grid(c), 128, S, c->ud_Tc, c->ud_Tl, e,
+         (float)(c->p.sigma * 0.5 + 0.5 + 0.01));
+  launch(c, "k_updown", k_updown, c->n_sm * 8, 256, S, c->fbuf, (const unsigned long long *)c->ud_Tc,
+         (const uint16_t *)c->ud_Tl, e, rup2, c->ud_cnt, c->ud_acc);
+  if ((r = check_device(c))) return r;
+  std::vector<int> hc(2 * (size_t)S.Nc);
+  std::vector<ExchAcc> ha(S.Nc);
+  CUDA_OK(c, scopy(c, hc.data(), c->ud_cnt, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost));
+  CUDA_OK(c, scopy(c, ha.data(), c->ud_acc, sizeof(ExchAcc) * ha.size(), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < S.Nc; ++j) {
+    if (cnt) cnt[j] = hc[2 * j];
+    if (up_cnt) up_cnt[j] = hc[2 * j + 1];
+    for (int k = 0; k < 3; ++k) {
+      const double a = (double)ha[j].hi[k] * 0x1p-20 + (double)ha[j].lo[k] * 0x1p-72;
+      const double u = (double)ha[j].hi[3 + k] * 0x1p-20 + (double)ha[j].lo[3 + k] * 0x1p-72;
+      if (vel_sum) vel_sum[3 * j + k] = a;
+      if (up_vel_sum) up_vel_sum[3 * j + k] = u;
+    }
   }
   return MPCD_OK;
 }

@@ -32,6 +32,9 @@ StreamKernel stream_kernel32(int flags);
 int stream32_per_thread();  // particles per thread of the FP32 streaming pass
 int stream64_per_thread(int flags);  // particles per thread of the FP64 streaming pass
 __global__ void k_bin(const SysF64 S, int fb);
+__global__ void k_updown_table(const SysF64 S, unsigned long long *Tc, uint16_t *Tl, long long epoch, float reach);
+__global__ void k_updown(const SysF64 S, int fb, const unsigned long long *Tc, const uint16_t *Tl, long long epoch,
+                         double rup2, int *cnt, ExchAcc *acc);
 EventKernel event_kernel32(int flags);
 __global__ void k_cell_prep32(__grid_constant__ const SysF64 S);
 __global__ void k_rotate32(__grid_constant__ const SysF64 S, int fb);

@@ -17,7 +17,9 @@
 // initialize_fluid and the set-up's compute_force_md are uploaded.  Random
 // numbers are the library's keyed Philox draws (key = the global `seed`), not the
 // reference's ran() stream, so a run is statistically, not bitwise, the reference's.
-// updown_velocity is a no-op: the reference discards its results.
+// updown_velocity is a no-op: the reference discards its results, and the counts it leaves in
+// the globals are overwritten by run() before anything reads them (the diagnostic itself is
+// mpcd_updown_velocity).
 // A routine called out of this order sets an error; the first error is printed
 // to stderr and the process exits with status 3 (the reference's routines cannot
 // return one).

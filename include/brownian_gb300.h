@@ -158,6 +158,15 @@ int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
  * out[6 j + k], Nc x 6 doubles (NULL: reset only).  The training data of the learned closure. */
 int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset);
 
+/* ---- updown_velocity (replaces cpp/run.cpp:28-50) ---------------------------------------- */
+/* On the current state, per colloid j: the fluid particles of the 342 boxes around the colloid's
+ * box (own box excluded) on its rear side (r.V <= 0, r = img(pos_fl - pos_colloid)) within
+ * sigma/2 + 0.5 (cnt[j], the run() shell) and within sigma/2 + 0.1 (up_cnt[j]), and the sums of
+ * their velocities (vel_sum[3 j + k], up_vel_sum[3 j + k]; exact sums).  The reference's slip
+ * velocities follow from these (its results are discarded; the Python wrapper restates its
+ * arithmetic).  Any pointer may be NULL. */
+int mpcd_updown_velocity(mpcd_ctx *c, int32_t *cnt, int32_t *up_cnt, double *vel_sum, double *up_vel_sum);
+
 /* ---- batched ensemble (no counterpart in the reference) ------------------------------- */
 /* nrep independent systems with their own parameters p[0..nrep-1] (box, fluid, colloids,
  * activity, seed; all MPCD_FP32C with equal n_sub and sort_every) stepped together: every

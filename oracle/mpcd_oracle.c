@@ -552,6 +552,24 @@ int orc_updown_velocity(orc_ctx *c, double *vel_out, double *up_vel_out) {
   return 0;
 }
 
+int orc_updown_sums(orc_ctx *c, int *cnt, int *up_cnt, double *vel_sum, double *up_vel_sum) {
+  for (int i = 1; i <= c->p.n_colloid; i++) {
+    int n = 0, un = 0;
+    V3 vs = v3(0, 0, 0), us = v3(0, 0, 0), vector;
+    const ilist *nf = &c->neigh_fl[i];
+    for (int j = 0; j < nf->n; j++) {
+      vector = vimg(sub(c->pos_fl[nf->v[j]], c->pos_colloid[i]), c->len);
+      const double r2 = vsum(mulv(vector, vector)), d = vsum(mulv(vector, c->vel_colloid[i]));
+      if (r2 <= pow((c->p.sigma * 0.5 + 0.5), 2) && d <= 0.0) { n++; vs = add(vs, c->vel_fl[nf->v[j]]); }
+      if (r2 <= pow((c->p.sigma * 0.5 + 0.1), 2) && d <= 0.0) { un++; us = add(us, c->vel_fl[nf->v[j]]); }
+    }
+    cnt[i - 1] = n; up_cnt[i - 1] = un;
+    vel_sum[3 * (i - 1)] = vs.x; vel_sum[3 * (i - 1) + 1] = vs.y; vel_sum[3 * (i - 1) + 2] = vs.z;
+    up_vel_sum[3 * (i - 1)] = us.x; up_vel_sum[3 * (i - 1) + 1] = us.y; up_vel_sum[3 * (i - 1) + 2] = us.z;
+  }
+  return 0;
+}
+
 /* ------------------------------------------------- fluid_colloid_collision */
 
 /* cpp/fluid_colloid_collision.cpp:7-24 */

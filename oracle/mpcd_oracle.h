@@ -83,6 +83,9 @@ int orc_update_pos_md(orc_ctx *c);          /* cpp/update.cpp:48-54         */
 int orc_update_pos_mpcd(orc_ctx *c);        /* cpp/update.cpp:56-60         */
 int orc_update_velocity_colloid(orc_ctx *c);/* cpp/update.cpp:62-67         */
 int orc_updown_velocity(orc_ctx *c, double *vel_out /* 3*Nc */, double *up_vel_out /* 3 */); /* cpp/run.cpp:28-50 */
+/* the same selection as orc_updown_velocity: per colloid the counts of the run() shell and of
+ * the inner shell and the (sequential) sums of their velocities, 3*Nc each */
+int orc_updown_sums(orc_ctx *c, int *cnt, int *up_cnt, double *vel_sum, double *up_vel_sum);
 
 /* driver pieces (cpp/active_brownian.cpp) */
 int orc_setup(orc_ctx *c);       /* create_box, neighbour_list_mpcd, neighbour_list_md, compute_force_md (:93-96) */

@@ -75,6 +75,8 @@ def lib():
         L.orc_ran_seq.restype = C.c_double
         L.orc_ran_seq.argtypes = [vp]
         L.orc_updown_velocity.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_updown_sums.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -210,6 +212,20 @@ class Oracle:
         o = np.zeros(self.Nc, dtype=np.int32)
         lib().orc_get_shell_count(self.h, _ip(o))
         return o
+
+    def updown_velocity(self):
+        """updown_velocity (cpp/run.cpp:28-50) on the current state: the neighbour lists are
+        rebuilt from the current positions (neighbour_list_mpcd), then the routine runs; returns
+        its per-colloid counts and velocity sums and its own outputs (vel per colloid, the single
+        up_vel vector)."""
+        self._call("neighbour_list_mpcd")
+        n = self.Nc
+        cnt, up_cnt = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        vs, us = np.zeros((n, 3)), np.zeros((n, 3))
+        lib().orc_updown_sums(self.h, _ip(cnt), _ip(up_cnt), _dp(vs), _dp(us))
+        vel, up = np.zeros((n, 3)), np.zeros(3)
+        self._call("updown_velocity", _dp(vel), _dp(up))
+        return dict(cnt=cnt, up_cnt=up_cnt, vel_sum=vs, up_vel_sum=us, vel=vel, up_vel=up)
 
     def ran(self, count):
         return np.array([lib().orc_ran_seq(self.h) for _ in range(count)])
