@@ -31,7 +31,9 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
            "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
            "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
-           "mpcd_surrogate_features", "mpcd_surrogate_step", "mpcd_updown_velocity"]
+           "mpcd_surrogate_features", "mpcd_surrogate_step", "mpcd_updown_velocity", "mpcd_traj_create",
+           "mpcd_traj_destroy", "mpcd_traj_last_error", "mpcd_traj_frames", "mpcd_traj_reset", "mpcd_traj_record",
+           "mpcd_traj_record_surrogate", "mpcd_traj_analyse", "mpcd_traj_read", "mpcd_traj_write"]
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
@@ -104,6 +106,17 @@ def lib():
         L.mpcd_fluid_sums_noalloc.argtypes = [vp, C.c_int64, C.c_double, vp, vp]
         L.mpcd_exchange_read.argtypes = [vp, dp, C.c_int]
         L.mpcd_updown_velocity.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp, dp]
+        L.mpcd_traj_create.argtypes = [C.c_int, C.c_int, dp, C.POINTER(vp)]
+        L.mpcd_traj_destroy.argtypes = [vp]
+        L.mpcd_traj_last_error.argtypes = [vp]
+        L.mpcd_traj_last_error.restype = C.c_char_p
+        L.mpcd_traj_frames.argtypes = [vp]
+        L.mpcd_traj_reset.argtypes = [vp]
+        L.mpcd_traj_record.argtypes = [vp, vp]
+        L.mpcd_traj_record_surrogate.argtypes = [vp, vp]
+        L.mpcd_traj_analyse.argtypes = [vp, C.POINTER(C.c_int), C.c_int, dp, dp, dp]
+        L.mpcd_traj_read.argtypes = [vp, C.c_int, C.c_int, dp, dp, dp]
+        L.mpcd_traj_write.argtypes = [vp, C.c_char_p, C.c_double]
         L.mpcd_ensemble_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
         L.mpcd_ensemble_destroy.argtypes = [vp]
         L.mpcd_ensemble_last_error.argtypes = [vp]
@@ -129,6 +142,88 @@ def _f64(a, n):
     if a.shape != (n, 3):
         raise ValueError(f"expected shape ({n}, 3), got {a.shape}")
     return a
+
+
+class Trajectory:
+    """Colloid frames kept on the device (mpcd_traj_*): unwrapped positions, velocities and
+    orientations; `record(src)` takes a frame from a Simulation (between steps) or from a
+    closure.Surrogate; `analyse` gives MSD, VACF and orientation autocorrelation per lag (in
+    frames), reduced on the GPU."""
+
+    def __init__(self, n_colloid, max_frames, box):
+        L = lib()
+        box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+        h = C.c_void_p()
+        r = L.mpcd_traj_create(int(n_colloid), int(max_frames), _dp(box), C.byref(h))
+        if r:
+            raise MPCDError(r, "mpcd_traj_create rejected the sizes")
+        self.h, self.Nc, self.box = h, int(n_colloid), box.copy()
+
+    def _ck(self, r):
+        if r:
+            raise MPCDError(r, lib().mpcd_traj_last_error(self.h).decode())
+
+    @property
+    def frames(self):
+        return lib().mpcd_traj_frames(self.h)
+
+    def reset(self):
+        self._ck(lib().mpcd_traj_reset(self.h))
+
+    def record(self, src):
+        if isinstance(src, Simulation):
+            r = lib().mpcd_traj_record(self.h, src.h)
+            if r:
+                raise MPCDError(r, lib().mpcd_last_error(src.h).decode())
+        else:
+            self._ck(lib().mpcd_traj_record_surrogate(self.h, src.h))
+
+    def analyse(self, msd_lags=(1, 2, 5, 10, 20, 50, 100), vacf_lags=(0, 1, 2, 5, 10, 20), oacf_lags=(0, 10, 50, 100)):
+        out = {}
+        for key, lags in (("msd", msd_lags), ("vacf", vacf_lags), ("oacf", oacf_lags)):
+            lg = np.ascontiguousarray(lags, dtype=np.int32)
+            res = [np.empty(len(lg)) for _ in range(3)]
+            self._ck(lib().mpcd_traj_analyse(self.h, lg.ctypes.data_as(C.POINTER(C.c_int)), len(lg),
+                                             *[_dp(a) for a in res]))
+            out[key] = res[("msd", "vacf", "oacf").index(key)]
+        return out
+
+    def read(self, first=0, count=None):
+        count = self.frames - first if count is None else count
+        a = [np.empty((count, self.Nc, 3)) for _ in range(3)]
+        self._ck(lib().mpcd_traj_read(self.h, first, count, *[_dp(x) for x in a]))
+        return tuple(a)
+
+    def write(self, path, dt_frame=1.0):
+        self._ck(lib().mpcd_traj_write(self.h, os.fsencode(path), float(dt_frame)))
+
+    def close(self):
+        if self.h:
+            lib().mpcd_traj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def read_trajectory(path):
+    """A trajectory file written by Trajectory.write / mpcd_traj_write: dict(box, dt_frame,
+    pos, vel, ra), the arrays (n_frames, n_colloid, 3)."""
+    with open(path, "rb") as f:
+        if f.read(8) != b"BGBTRAJ1":
+            raise ValueError(f"{path}: not a trajectory file")
+        version, nc, nf, fields = np.frombuffer(f.read(16), dtype="<i4")
+        if version != 1 or fields != 7:
+            raise ValueError(f"{path}: unsupported version {version} / fields {fields}")
+        geo = np.frombuffer(f.read(32), dtype="<f8")
+        data = np.frombuffer(f.read(), dtype="<f8")
+    if data.size != nf * 3 * nc * 3:
+        raise ValueError(f"{path}: truncated")
+    d = data.reshape(nf, 3, nc, 3)
+    return dict(box=geo[:3].copy(), dt_frame=float(geo[3]), pos=d[:, 0].copy(), vel=d[:, 1].copy(), ra=d[:, 2].copy())
 
 
 def displaced_mass(radius, density, mass_fl=1.0):

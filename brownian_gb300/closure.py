@@ -279,18 +279,6 @@ def autocorr(A, lags):
                      for lag in lags])
 
 
-def trajectory(stepper, getter, steps):
-    """Runs `steps` MPCD steps, recording colloid positions, velocities and orientations."""
-    X, V, R = [], [], []
-    for _ in range(steps):
-        stepper()
-        s = getter()
-        X.append(s["pos_colloid"].copy())
-        V.append(s["vel_colloid"].copy())
-        R.append(s["ra"].copy())
-    return np.array(X), np.array(V), np.array(R)
-
-
 # ------------------------------------------------------------------ end to end
 
 def _sim(p):
@@ -339,7 +327,9 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     full.step(20)
     full.get_colloids()
     t_full = (time.perf_counter() - t0) / 20
-    runs = {"full": closure_traj(full, steps)}
+    L = float(p.Lx)
+    lag_kw = dict(msd_lags=lags, vacf_lags=vlags, oacf_lags=olags)
+    stats = {"full": device_stats(full, steps, L, **lag_kw)}
     full.close()
     sur = Surrogate(p, net)
     sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
@@ -348,23 +338,17 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     sur.step(100)
     t_sur = (time.perf_counter() - t0) / 100
     sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
-    runs["closure"] = closure_traj(sur, steps)
+    stats["closure"] = device_stats(sur, steps, L, **lag_kw)
     sur.close()
     none_net = Network(max_batch=p.n_colloid)
     none_net.set_normalisation(np.zeros(IN), np.ones(IN), np.zeros(NY), np.full(NY, 1e-20))
     none_net.set_params(np.zeros(none_net.n_params))
     bare = Surrogate(p, none_net)
     bare.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
-    runs["no_closure"] = closure_traj(bare, steps)
+    stats["no_closure"] = device_stats(bare, steps, L, **lag_kw)
     bare.close()
     none_net.close()
-    L = float(p.Lx)
     out = {"t_full_ms": t_full * 1e3, "t_surrogate_ms": t_sur * 1e3, "speedup": t_full / t_sur}
-    stats = {}
-    for name, (X, V, R) in runs.items():
-        U = unwrap(X, L)
-        stats[name] = {"msd": msd(U, lags).tolist(), "vacf": autocorr(V, vlags).tolist(),
-                       "oacf": autocorr(R, olags).tolist()}
     out["stats"] = stats
     out["lags"] = {"msd": list(lags), "vacf": list(vlags), "oacf": list(olags)}
     rel = {}
@@ -375,6 +359,17 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     return out
 
 
-def closure_traj(obj, steps):
-    getter = obj.get_colloids if hasattr(obj, "get_colloids") else obj.get_state
-    return trajectory(lambda: obj.step(1), getter, steps)
+def device_stats(obj, steps, L, **lags):
+    """MSD / VACF / OACF of `steps` steps of a Simulation or Surrogate, the frames kept and
+    reduced on the GPU (a Trajectory; no host copy per step).  Same numbers as msd / autocorr
+    on the host trajectory, to rounding."""
+    from . import Trajectory
+    tr = Trajectory(obj.Nc, steps + 1, L)
+    try:
+        tr.record(obj)
+        for _ in range(steps):
+            obj.step(1)
+            tr.record(obj)
+        return {k: v.tolist() for k, v in tr.analyse(**lags).items()}
+    finally:
+        tr.close()

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/brownian_gb300.h"
+#include "traj_internal.h"
 #include "kernels.cuh"
 
 using namespace bgb;
@@ -1068,6 +1069,17 @@ extern "C" int mpcd_updown_velocity(mpcd_ctx *c, int32_t *cnt, int32_t *up_cnt, 
     }
   }
   return MPCD_OK;
+}
+
+// a trajectory frame of this context's colloids (between steps)
+extern "C" int mpcd_traj_record(mpcd_traj *t, mpcd_ctx *c) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  if (!t || traj_colloids(t) != c->S.Nc || c->S.Nc < 1) return fail(c, MPCD_ERR_PARAM, "trajectory size");
+  if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "frames are taken between steps");
+  const int b = (int)((c->host_step * c->S.n_sub - 1) & 1);
+  r = traj_record_f64(t, c->S.X[b], c->S.V, c->S.ra, c->stream);
+  return r ? fail(c, r, mpcd_traj_last_error(t)) : MPCD_OK;
 }
 
 #include "ensemble.inc"

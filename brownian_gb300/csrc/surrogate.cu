@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/brownian_gb300.h"
+#include "traj_internal.h"
 #include "common.cuh"
 #include "mlp_internal.h"
 
@@ -515,6 +516,13 @@ extern "C" int mpcd_surrogate_get_state(mpcd_surrogate *s, double *pos, double *
     }
   }
   return MPCD_OK;
+}
+
+// a trajectory frame of the colloid-only step's state
+extern "C" int mpcd_traj_record_surrogate(mpcd_traj *t, mpcd_surrogate *s) {
+  if (!s || !t || traj_colloids(t) != s->S.Nc) return MPCD_ERR_PARAM;
+  const int r = traj_record_f4(t, s->S.X, s->S.V, s->S.ra, s->stream);
+  return r ? sfail(s, r, mpcd_traj_last_error(t)) : MPCD_OK;
 }
 
 extern "C" int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recompute) {

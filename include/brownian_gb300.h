@@ -167,6 +167,29 @@ int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset);
  * arithmetic).  Any pointer may be NULL. */
 int mpcd_updown_velocity(mpcd_ctx *c, int32_t *cnt, int32_t *up_cnt, double *vel_sum, double *up_vel_sum);
 
+/* ---- colloid trajectories and their statistics (no counterpart: the reference's analysis
+ *      prints are commented out, cpp/active_brownian.cpp:44-46) ---------------------------- */
+/* A device-resident recorder: per frame the colloids' unwrapped positions, velocities and
+ * orientations (FP64).  Frames of one trajectory come from one source, between steps. */
+typedef struct mpcd_traj mpcd_traj;
+struct mpcd_surrogate; /* the colloid-only step, declared below */
+int mpcd_traj_create(int n_colloid, int max_frames, const double *box /* 3 */, mpcd_traj **out);
+int mpcd_traj_destroy(mpcd_traj *t);
+const char *mpcd_traj_last_error(const mpcd_traj *t);
+int mpcd_traj_frames(const mpcd_traj *t);
+int mpcd_traj_reset(mpcd_traj *t);                              /* drops the frames */
+int mpcd_traj_record(mpcd_traj *t, mpcd_ctx *c);                /* a frame of a context's colloids */
+int mpcd_traj_record_surrogate(mpcd_traj *t, struct mpcd_surrogate *s); /* a frame of the colloid-only step */
+/* per lag (in frames): MSD <|U(t+lag) - U(t)|^2>, VACF <V(t+lag).V(t)>, OACF <ra(t+lag).ra(t)>,
+ * averaged over time origins and colloids (NaN where no two frames are lag apart); any output
+ * may be NULL; deterministic */
+int mpcd_traj_analyse(mpcd_traj *t, const int *lags, int nlags, double *msd, double *vacf, double *oacf);
+/* frames [first, first + count) to host arrays, count x n_colloid x 3 each (NULL: skip) */
+int mpcd_traj_read(mpcd_traj *t, int first, int count, double *pos, double *vel, double *ra);
+/* the file "BGBTRAJ1" + int32 version, n_colloid, n_frames, fields + double box[3], dt_frame,
+ * then per frame positions, velocities, orientations (n_colloid x 3 doubles each) */
+int mpcd_traj_write(mpcd_traj *t, const char *path, double dt_frame);
+
 /* ---- batched ensemble (no counterpart in the reference) ------------------------------- */
 /* nrep independent systems with their own parameters p[0..nrep-1] (box, fluid, colloids,
  * activity, seed; all MPCD_FP32C with equal n_sub and sort_every) stepped together: every
