@@ -36,6 +36,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_traj_record_surrogate", "mpcd_traj_analyse", "mpcd_traj_read", "mpcd_traj_write"]
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
+PHYSICS_REFERENCE, PHYSICS_FIXED = 0, 1
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
 
 
@@ -54,6 +55,7 @@ class Params(C.Structure):
         ("eps", C.c_double), ("sigma", C.c_double), ("I_colloid", C.c_double), ("v0", C.c_double),
         ("theta_deg", C.c_double), ("Dr", C.c_double), ("seed", C.c_uint64), ("precision", C.c_int),
         ("max_per_cell", C.c_int), ("vmax", C.c_double), ("init_gap", C.c_double), ("sort_every", C.c_int),
+        ("physics", C.c_int),
     ]
 
 
@@ -233,13 +235,14 @@ def displaced_mass(radius, density, mass_fl=1.0):
 
 def make_params(L, n_fluid, n_colloid, *, n_sub=10, kbt=1.0, kbt1=1.0, ndt=0.1, mass_fl=1.0, mass_colloid=654.1,
                 sig_colloid=5.0, eps=1.0, sigma=None, I_colloid=None, v0=0.0, theta_deg=130.0, Dr=0.0, seed=77777,
-                precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5, sort_every=0):
+                precision=FP64, max_per_cell=0, vmax=0.0, init_gap=0.5, sort_every=0, physics=0):
     """mpcd_params of one system (defaults: the reference's, cpp/active_brownian.cpp:3-7)."""
     Lx, Ly, Lz = (L, L, L) if np.isscalar(L) else L
     sigma = 0.8 * sig_colloid if sigma is None else sigma          # cpp/active_brownian.cpp:7
     I_colloid = 0.1 * mass_colloid * sigma * sigma if I_colloid is None else I_colloid
     return Params(Lx, Ly, Lz, n_fluid, n_colloid, n_sub, kbt, kbt1, ndt, mass_fl, mass_colloid, sig_colloid, eps,
-                  sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell, vmax, init_gap, sort_every)
+                  sigma, I_colloid, v0, theta_deg, Dr, seed, precision, max_per_cell, vmax, init_gap, sort_every,
+                  physics)
 
 
 class Simulation:

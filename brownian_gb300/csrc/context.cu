@@ -375,6 +375,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   if (p.n_colloid > 0 && (!(p.mass_colloid > 0) || !(p.I_colloid > 0) || !(p.sigma > 0) || !(p.sig_colloid > 0)))
     return MPCD_ERR_PARAM;
   if (p.precision != MPCD_FP64 && p.precision != MPCD_FP32C) return MPCD_ERR_PARAM;
+  if (p.physics != MPCD_PHYSICS_REFERENCE && p.physics != MPCD_PHYSICS_FIXED) return MPCD_ERR_PARAM;
   if (p.precision == MPCD_FP32C && (p.Lx > 1023 || p.Ly > 1023 || p.Lz > 1023)) return MPCD_ERR_PARAM;
   long long C = (long long)p.Lx * p.Ly * p.Lz;
   if (C > (1ll << 30)) return MPCD_ERR_PARAM;
@@ -450,6 +451,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   // the FP64 form builds the cell tables in the colloid finish: its side kernel
   // needs two warps per colloid (forces; orientation), the FP32 form's four
   S.fin_table = p.precision == MPCD_FP64 ? 1 : 0;
+  S.physics = p.physics == MPCD_PHYSICS_FIXED ? 1 : 0;
   S.aux_nw = S.fin_table ? 2 : 4;
   S.dtf = (float)dt;
   S.vmaxf = (float)vmax;

@@ -24,7 +24,8 @@ static __device__ __forceinline__ bool off_ok(int d, int L) {
 // excluded)?  Cell numbers >= C (a coordinate exactly at L past the last row)
 // have no neighbour entries in the reference.
 static __device__ __forceinline__ bool in_block(const SysF64 &S, int cb, int lin) {
-  if (cb >= S.C || lin >= S.C || cb == lin) return false;
+  if (cb >= S.C || lin >= S.C) return false;
+  if (cb == lin) return S.physics != 0;  // the reference skips the own box; the fixed rules keep it
   int cx = cb % S.Lx, ct = cb / S.Lx, cy = ct % S.Ly, cz = ct / S.Ly;
   int bx = lin % S.Lx, bt = lin / S.Lx, by = bt % S.Ly, bz = bt / S.Ly;
   return off_ok(bx - cx, S.Lx) && off_ok(by - cy, S.Ly) && off_ok(bz - cz, S.Lz);
@@ -223,12 +224,14 @@ static __device__ __forceinline__ double refl_speed(const SysF64 &S, uint4 r0) {
   return __dsqrt_rn(__dmul_rn(-log(random_e), S.inv_m_beta));
 }
 
-// the tangential Gaussian x1 sqrt(-2 log z / z) sqrt(kT/m), polar Box-Muller: each
-// try is a fixed function of the key, a try is rejected with probability 1 - pi/4,
-// so 256 tries never run out.  The second try is computed by every lane and
-// selected (2 ran - 1 is exact: pm1 builds it from the draw's bits); only two
-// rejections in a row (1 in 22) branch.
-static __device__ __forceinline__ double refl_gauss(const SysF64 &S, uint4 r1, uint32_t a, uint32_t b, uint32_t t) {
+// the tangential Gaussians x1 sqrt(-2 log z / z) sqrt(kT/m) (and, into *v2, the
+// same with x2, which only the fixed rules use), polar Box-Muller: each try is a
+// fixed function of the key, a try is rejected with probability 1 - pi/4, so 256
+// tries never run out.  The second try is computed by every lane and selected
+// (2 ran - 1 is exact: pm1 builds it from the draw's bits); only two rejections
+// in a row (1 in 22) branch.
+static __device__ __forceinline__ double refl_gauss(const SysF64 &S, uint4 r1, uint32_t a, uint32_t b, uint32_t t,
+                                                    double *v2) {
   double x1 = pm1(r1.x), x2 = pm1(r1.y);
   double z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
   const double x1b = pm1(r1.z), x2b = pm1(r1.w);
@@ -247,6 +250,7 @@ static __device__ __forceinline__ double refl_gauss(const SysF64 &S, uint4 r1, u
     }
   }
   const double g = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(z)), z));
+  *v2 = __dmul_rn(__dmul_rn(x2, g), S.sqrt_kt_m);
   return __dmul_rn(__dmul_rn(x1, g), S.sqrt_kt_m);
 }
 
@@ -261,19 +265,22 @@ static __device__ __forceinline__ d3 refl_point(const SysF64 &S, uint4 r0, d3 rf
             ref_img(__dsub_rn(__dmul_rn(u01(r0.w), S.dz.L), rf.z), S.dz));
 }
 
-// u = unit(un x t) v1 + un, un = n val
-static __device__ __forceinline__ d3 refl_combine(d3 n, double val, d3 t, double v1) {
+// u = unit(un x t) v1 + un, un = n val; with the fixed rules also the second
+// tangential component, (n x unit(un x t)) v2
+static __device__ __forceinline__ d3 refl_combine(const SysF64 &S, d3 n, double val, d3 t, double v1, double v2) {
   const d3 un = mul3s(n, val);
   const d3 ut = refl_unit(cross_ref(un, t));
-  return add3(mul3s(ut, v1), un);
+  if (!S.physics) return add3(mul3s(ut, v1), un);
+  return add3(add3(mul3s(ut, v1), mul3s(cross_ref(n, ut), v2)), un);
 }
 
 static __device__ d3 stochastic_reflection(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, d3 rf, d3 rs) {
   uint4 r0, r1;
   refl_blocks(S, a, b, t, r0, r1);
   const double val = refl_speed(S, r0);
-  const double v1 = refl_gauss(S, r1, a, b, t);
-  return refl_combine(refl_unit(rs), val, refl_point(S, r0, rf), v1);
+  double v2;
+  const double v1 = refl_gauss(S, r1, a, b, t, &v2);
+  return refl_combine(S, refl_unit(rs), val, refl_point(S, r0, rf), v1, v2);
 }
 
 // ------------------------------------------------------------ particle stream
@@ -398,7 +405,7 @@ static __device__ __noinline__ void ev_collide(const SysF64 &S, EvState &st, int
 // Per-task scratch of a cooperative collision (ev_collide_coop)
 struct CollScratch {
   double xb[3], rs[3], n[3], tp[3], wr[3], vd[3];
-  double val, v1;
+  double val, v1, v2;
 };
 
 // The same collision as ev_collide for up to 32 gathered particles at once
@@ -450,7 +457,7 @@ static __device__ void ev_collide_coop(const SysF64 &S, EvState *sst, const int 
     } else if (w == 1) {
       c.val = refl_speed(S, draw4(S.key, DOM_COLL, 0, a, b, tt));
     } else {
-      c.v1 = refl_gauss(S, draw4(S.key, DOM_COLL, 1, a, b, tt), a, b, tt);
+      c.v1 = refl_gauss(S, draw4(S.key, DOM_COLL, 1, a, b, tt), a, b, tt, &c.v2);
     }
   }
   __syncthreads();
@@ -458,7 +465,7 @@ static __device__ void ev_collide_coop(const SysF64 &S, EvState *sst, const int 
     EvState &st = sst[stask[k]];
     const int j = st.j;
     const CollScratch &c = cs[t];
-    const d3 u = refl_combine(mk(c.n[0], c.n[1], c.n[2]), c.val, mk(c.tp[0], c.tp[1], c.tp[2]), c.v1);
+    const d3 u = refl_combine(S, mk(c.n[0], c.n[1], c.n[2]), c.val, mk(c.tp[0], c.tp[1], c.tp[2]), c.v1, c.v2);
     const d3 vn = add3(add3(u, Vj), mk(c.wr[0], c.wr[1], c.wr[2]));
     const d3 vd = mk(c.vd[0], c.vd[1], c.vd[2]);
     const d3 dv = sub3(vd, vn);
@@ -625,7 +632,7 @@ static __device__ void for_reach_cells(const SysF64 &S, int cb, float4 xc, float
   const float iLx = __frcp_rn(Lx), iLy = __frcp_rn(Ly), iLz = __frcp_rn(Lz);
   for (int q = first; q < 343; q += stride) {
     int ox = q % 7 - 3, oy = (q / 7) % 7 - 3, oz = q / 49 - 3;
-    if (!ox && !oy && !oz) continue;
+    if (!ox && !oy && !oz && !S.physics) continue;  // the own box (kept by the fixed rules)
     int bx = cx + ox, by = cy + oy, bz = cz + oz;
     bx += bx < 0 ? S.Lx : 0; bx -= bx >= S.Lx ? S.Lx : 0;
     by += by < 0 ? S.Ly : 0; by -= by >= S.Ly ? S.Ly : 0;

@@ -251,15 +251,21 @@ __device__ f3 reflect32(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, f3 
   tt.x -= S.Lxf * rintf(tt.x / S.Lxf); tt.y -= S.Lyf * rintf(tt.y / S.Lyf); tt.z -= S.Lzf * rintf(tt.z / S.Lzf);
   f3 ut = fcross(un, tt);
   float iu = rsqrtf(ut.x * ut.x + ut.y * ut.y + ut.z * ut.z);
-  float x1 = 0.f, z = 2.f;
+  float x1 = 0.f, x2 = 0.f, z = 2.f;
   for (int it = 0; z > 1.f && it < 256; ++it) {
     x1 = 2.f * next() - 1.f;
-    float x2 = 2.f * next() - 1.f;
+    x2 = 2.f * next() - 1.f;
     z = x1 * x1 + x2 * x2;
   }
   z = sqrtf(-2.f * logf(z) / z);
   float v1 = x1 * z * (float)S.sqrt_kt_m;
-  return fm(ut.x * iu * v1 + un.x, ut.y * iu * v1 + un.y, ut.z * iu * v1 + un.z);
+  f3 res = fm(ut.x * iu * v1 + un.x, ut.y * iu * v1 + un.y, ut.z * iu * v1 + un.z);
+  if (S.physics) {  // the fixed rules: the second tangential component along n x unit(ut)
+    const float v2 = x2 * z * (float)S.sqrt_kt_m;
+    const f3 t2 = fcross(fm(rs.x * ir, rs.y * ir, rs.z * ir), fm(ut.x * iu, ut.y * iu, ut.z * iu));
+    res = fm(res.x + t2.x * v2, res.y + t2.y * v2, res.z + t2.z * v2);
+  }
+  return res;
 }
 
 // wall collisions of the listed particles in colloid order, then (last substep)

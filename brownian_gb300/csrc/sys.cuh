@@ -139,6 +139,7 @@ struct SysF64 {
   EventRec *prec;
   int pend_cap;
   uint8_t *pend;    // [N]
+  int physics;      // MPCD_PHYSICS_FIXED: own box among the candidates, 2-D tangential reflection
   float cmarginf;   // the margin (the bound cmargin2 checks), FP32
   int fin_table;    // FP64 form: the colloid finish of substep g builds the cell table of
                     // g+2 (else the side kernel of g+1 does)

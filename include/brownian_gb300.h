@@ -67,7 +67,15 @@ typedef struct {
   double vmax;             /* speed bound of one fluid particle for the exact sums (0: 24*sqrt(kbt/mass_fl)) */
   double init_gap;         /* MPCD_INIT_PHYSICAL: minimum surface gap between colloids    */
   int sort_every;          /* reorder the fluid by cell every this many steps (0: 10; <0: never) */
+  int physics;             /* MPCD_PHYSICS_REFERENCE (0) or MPCD_PHYSICS_FIXED (1)           */
 } mpcd_params;
+
+/* collision rules: the reference's (bit parity), or corrected ones: a colloid's own box among
+ * its candidate boxes (the reference skips it, cpp/neighbour_list.cpp:20) and both tangential
+ * Gaussian components of the wall reflection (the reference draws two and uses one,
+ * cpp/fluid_colloid_collision.cpp:22-23).  The initial state is chosen apart (mpcd_initialize:
+ * MPCD_INIT_PHYSICAL gives Maxwell-Boltzmann velocities and isotropic orientations). */
+enum { MPCD_PHYSICS_REFERENCE = 0, MPCD_PHYSICS_FIXED = 1 };
 
 typedef struct {
   int64_t step;            /* completed MPCD steps                                        */

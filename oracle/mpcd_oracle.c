@@ -365,7 +365,7 @@ int orc_box_neighbours(const orc_ctx *c, int b, int32_t *out) {
   V3 start = sub(iter, v3(3, 3, 3)), stop = add(iter, v3(3, 3, 3)), jiter = start;
   for (int j = 1; j <= 343; j++) {
     int tbox = vcell(sub(cmod(jiter, c->len), v3(0, 1, 1)), c->len);
-    if (tbox != box) out[nb++] = tbox;
+    if (tbox != box || c->p.physics) out[nb++] = tbox;  /* the corrected rules keep the own box */
     /* point::next(len, inc, start) (cpp/parameters.hpp:66-70) */
     jiter.x += 1;
     if (jiter.x > stop.x) jiter.y += 1, jiter.x = start.x;
@@ -590,7 +590,8 @@ static V3 stochastic_reflection(orc_ctx *c, drawseq *d, V3 rf, V3 rs) {
   z = sqrt((-2.0 * log(z)) / z);
   v[1] = x[1] * z * sqrt(kbt / mass_fl);
   v[2] = x[2] * z * sqrt(kbt / mass_fl);
-  (void)v[2];
+  if (c->p.physics) /* the corrected rules: the second tangential component along n x ut */
+    return add(add(muls(ut, v[1]), muls(cross(n, ut), v[2])), un);
   return add(muls(ut, v[1]), un);
 }
 

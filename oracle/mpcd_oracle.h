@@ -59,6 +59,8 @@ typedef struct {
   double Dr;               /* rotational diffusion (no reference counterpart; 0 reproduces it) */
   int rng_mode;            /* ORC_RNG_SEQ or ORC_RNG_KEYED                      */
   int64_t seed;            /* SEQ: initial reference `seed`; KEYED: Philox key  */
+  int physics;             /* 1: the corrected rules (own box a candidate, 2-D tangential
+                              reflection) the library offers as MPCD_PHYSICS_FIXED; 0: the reference */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

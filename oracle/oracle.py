@@ -26,7 +26,7 @@ class Params(C.Structure):
         ("mass_fl", C.c_double), ("mass_colloid", C.c_double),
         ("sig_colloid", C.c_double), ("eps", C.c_double), ("sigma", C.c_double),
         ("I_colloid", C.c_double), ("v0", C.c_double), ("theta_deg", C.c_double), ("Dr", C.c_double),
-        ("rng_mode", C.c_int), ("seed", C.c_int64),
+        ("rng_mode", C.c_int), ("seed", C.c_int64), ("physics", C.c_int),
     ]
 
 
