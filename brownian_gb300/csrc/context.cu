@@ -55,6 +55,7 @@ struct mpcd_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
   cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_finp[2] = {nullptr, nullptr};
+
   cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [sorts][fluid buffer]
   int step_launches[2][2] = {{0, 0}, {0, 0}};
   int fbuf = 0;                  // fluid buffer holding the current state
@@ -243,12 +244,51 @@ static void enq_rotation(mpcd_ctx *c, bool sort) {
   }
 }
 
+// run(), cpp/run.cpp:10-26: the rear-shell test and count over the candidates the
+// last substep recorded, then the compensating kick of the shell fluid
+static void enq_run_shell(mpcd_ctx *c, cudaStream_t s, int fb) {
+  const bool f32 = c->S.precision == MPCD_FP32C;
+  launch_on(c, s, "k_run_shell", f32 ? k_run_shell32 : k_run_shell, 152 * 4, 256, c->S, fb);
+}
+
+static void enq_run_kick(mpcd_ctx *c) {
+  const bool f32 = c->S.precision == MPCD_FP32C;
+  launch(c, "k_run_kick", f32 ? k_run_kick32 : k_run_kick, 152 * 4, 256, c->S, c->fbuf);
+}
+
 static void enq_run_fluid(mpcd_ctx *c) {
+  if (c->S.Nc == 0) return;
+  enq_run_shell(c, c->stream, c->fbuf);
+  enq_run_kick(c);
+}
+
+// rotation_mpcd and run of a step: the rear-shell test reads only the records, the
+// positions and the colloids, none of which the cell pass or the in-place rotation
+// touch, so it runs on the side stream beside them (before a sort's scatter, which
+// moves the particles and rewrites their slots)
+static void enq_rotation_run(mpcd_ctx *c, bool sort) {
+  if (c->S.Nc == 0) {
+    enq_rotation(c, sort);
+    return;
+  }
+  cudaEventRecord(c->ev_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+  enq_run_shell(c, c->aux, c->fbuf);
+  cudaEventRecord(c->ev_join, c->aux);
   const SysF64 &S = c->S;
-  if (S.Nc == 0) return;
   const bool f32 = S.precision == MPCD_FP32C;
-  launch(c, "k_run_shell", f32 ? k_run_shell32 : k_run_shell, 152 * 4, 256, S, c->fbuf);
-  launch(c, "k_run_kick", f32 ? k_run_kick32 : k_run_kick, 152 * 4, 256, S, c->fbuf);
+  launch(c, "k_cell_prep", f32 ? k_cell_prep32 : k_cell_prep, prep_blocks(S), 256, S);
+  if (sort) {
+    cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+    launch(c, "k_scan_blocks", k_scan_blocks, 1, 1024, S, c->nblk);
+    launch(c, "k_rotate_sort", f32 ? k_rotate_sort32 : k_rotate_sort, blocks_for(S.N, 256), 256, S, c->fbuf,
+           1 - c->fbuf);
+    c->fbuf = 1 - c->fbuf;
+  } else {
+    launch(c, "k_rotate", f32 ? k_rotate32 : k_rotate, blocks_for(S.N, 256), 256, S, c->fbuf);
+    cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+  }
+  enq_run_kick(c);
 }
 
 // The substeps of the FP64 form, overlapped on three streams.  Per substep l:
@@ -294,8 +334,7 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
 static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
-  enq_rotation(c, sort);
-  enq_run_fluid(c);
+  enq_rotation_run(c, sort);
   enq_fin(c, M_KICK | M_ADVANCE, 0);
   if (c->S.precision == MPCD_FP64) {
     enq_substeps_overlapped(c);
@@ -807,6 +846,7 @@ extern "C" int mpcd_setup(mpcd_ctx *c) {
   // cell table around each colloid (cpp/active_brownian.cpp:93-96)
   // no particle is pending between steps (a step cut short by an error may have left marks)
   if (c->S.pend) CUDA_OK(c, cudaMemsetAsync(c->S.pend, 0, (size_t)c->S.N, c->stream));
+  if (c->S.Nc) CUDA_OK(c, cudaMemsetAsync(c->S.shell_cnt, 0, sizeof(int) * (size_t)c->S.Nc, c->stream));
   launch(c, "k_colloid_setup", k_colloid_setup, colloid_grid(c), 128, c->S);
   // neighbour_list_mpcd seen from the fluid: run() candidates of the first step, and the
   // SRD binning of its rotation_mpcd

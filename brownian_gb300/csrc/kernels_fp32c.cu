@@ -178,7 +178,7 @@ static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const in
     if (ev[u]) {
       const int i = bev + __popc(mev & lt);
       if (i < S.events_cap) S.events[i] = p;
-      else atomicOr(&S.ss->err, ERRB_SHELL);
+      else atomicOr(&S.ss->err, ERRB_EVENTS);
     }
     if (has_rec) {
       const int i = brec + __popc(mrec & lt);
@@ -441,7 +441,6 @@ EventKernelB event_kernel32_b(int flags) {
 // as the FP32 affine map v' = A v + b; plus the occupancy prefix of the counting sort.
 static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const int VB, const int NVB) {
   const int c = VB * blockDim.x + threadIdx.x;
-  if (c < S.Nc) S.shell_cnt[c] = 0;
   CellAcc a = CellAcc{0, 0, 0, 0, 0, 0};
   if (c < S.Cpad) {
     a = S.acc[c];

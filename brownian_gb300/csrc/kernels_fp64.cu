@@ -394,7 +394,6 @@ EventKernel event_kernel(int flags) {
 // Consumes (and clears) the exact sums k_stream accumulated.
 __global__ void __launch_bounds__(256) k_cell_prep(const SysF64 S) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < S.Nc) S.shell_cnt[c] = 0;
   CellAcc a = CellAcc{0, 0, 0, 0, 0, 0};
   if (c < S.Cpad) {
     a = S.acc[c];
@@ -824,7 +823,11 @@ __global__ void __launch_bounds__(128) k_colloid_pot(const SysF64 S) {
 
 // completes a step: bumps the step counter
 static __device__ __forceinline__ void k_end_step_body(const SysF64 &S, const int VB, const int NVB) {
-  if (threadIdx.x == 0 && VB == 0) S.ss->step += 1;
+  if (VB != 0) return;
+  if (threadIdx.x == 0) S.ss->step += 1;
+  // run()'s shell counts start from zero for the next step (its rear-shell test runs beside
+  // the next step's cell pass, so the cell pass cannot clear them)
+  for (int j = threadIdx.x; j < S.Nc; j += blockDim.x) S.shell_cnt[j] = 0;
 }
 
 __global__ void k_end_step(__grid_constant__ const SysF64 S) {
