@@ -245,6 +245,14 @@ class Surrogate:
         self._ck(lib().mpcd_surrogate_features(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), 1 if recompute else 0))
         return out
 
+    def outputs(self):
+        """The network's outputs of the last step in physical units (means 6, log-variances 6)."""
+        out = np.empty((self.Nc, NY * 2), dtype=np.float32)
+        f = lib().mpcd_surrogate_outputs
+        f.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+        self._ck(f(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
     def step(self, nsteps=1):
         self._ck(lib().mpcd_surrogate_step(self.h, nsteps))
 

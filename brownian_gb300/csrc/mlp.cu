@@ -61,7 +61,9 @@ struct Gemm {
   int kchunk;          // K range of one blockIdx.z
 };
 
-__device__ __forceinline__ float sigm(float z) { return 1.f / (1.f + __expf(-z)); }
+// the logistic function, branch free (fast reciprocal: within 2 ulp, and 0 once e^-z overflows);
+// the colloid-only step evaluates the network with the same arithmetic
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
 
 __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
   asm volatile(
@@ -600,14 +602,9 @@ extern "C" int mpcd_mlp_train_step(mpcd_mlp *nn, const float *x, const float *y,
 
 MlpIO mlp_io(mpcd_mlp *nn) {
   MlpIO io;
-  io.X = nn->X;
   io.xmean = nn->xmean; io.xistd = nn->xistd;
-  io.O = nn->O;
   io.ymean = nn->ymean; io.yistd = nn->yistd;
-  io.max_batch = nn->max_batch;
+  for (int l = 0; l < 4; ++l) io.w[l] = nn->w[l];
+  io.bias = nn->bias;
   return io;
 }
-
-int mlp_stage(mpcd_mlp *nn, const float *x, int rows, cudaStream_t s) { return stage_inputs(nn, x, rows, s); }
-
-void mlp_layers(mpcd_mlp *nn, int rows, cudaStream_t s) { forward(nn, rows, s); }

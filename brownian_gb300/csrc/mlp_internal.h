@@ -1,24 +1,18 @@
 // Internal interface between the closure network (mlp.cu) and the colloid-only
-// step (surrogate.cu): the step writes the network's normalised BF16 inputs and
-// reads its normalised outputs directly, so that one MPCD step is the network's
-// four GEMMs and one dynamics kernel.
+// step (surrogate.cu): the step reads the network's weights, biases and
+// normalisation directly and evaluates the network inside its own kernel.
 #pragma once
 #include <cuda_runtime.h>
 
 #include "../../include/brownian_gb300.h"
 
 struct MlpIO {
-  void *X;                     // normalised BF16 inputs [max_batch][MLP_IN_PADDED]
   const float *xmean, *xistd;  // input normalisation
-  const float *O;              // normalised outputs [max_batch][MLP_OUT_PADDED]
   const float *ymean, *yistd;  // output normalisation
-  int max_batch;
+  const void *w[4];            // BF16 weights [k][n] of the four layers (96 x 256, 256 x 256 twice, 256 x 16)
+  const float *bias;           // FP32 biases, 256 + 256 + 256 + 16
 };
 constexpr int MLP_IN_PADDED = 96, MLP_OUT_PADDED = 16;
 constexpr float MLP_INPUT_CLIP = 6.f, MLP_LOGVAR_CLAMP = 6.f;
 
 MlpIO mlp_io(mpcd_mlp *n);
-// normalise raw inputs [rows][81] into X
-int mlp_stage(mpcd_mlp *n, const float *x, int rows, cudaStream_t s);
-// the four layers on rows of X into O
-void mlp_layers(mpcd_mlp *n, int rows, cudaStream_t s);

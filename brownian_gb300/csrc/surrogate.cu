@@ -6,11 +6,22 @@
 // forces, the active kick (run(), cpp/run.cpp:13) and the orientation update
 // (cpp/update.cpp:34-46, plus rotational diffusion Dr), in FP32.
 //
-// Per step: the network's forward pass (mlp.cu) on the features the previous step
-// left, then k_sur_md (one block: the impulse and the active kick, the substeps,
-// and the next step's features; the substeps need every colloid's new position,
-// and a block barrier is the cheapest wait at these sizes).  The step is one CUDA
-// graph.  k_sur_features computes the inputs of a state set from the host.
+// Per step, two kernels (one CUDA graph):
+//   k_sur_net, one block per 16 colloids over the whole GPU: each colloid's
+//     neighbours (all pairs, one warp per four colloids), its 81 network inputs and
+//     its force partners for the step, the whole network (four layers, BF16
+//     mma.sync with FP32 accumulation, activations in shared memory, the weights
+//     streamed through a ring of shared-memory stages by cp.async while the block
+//     computes), the Gaussian draw of the exchange and the step's
+//     rotational-diffusion draws;
+//   k_sur_md, one block: the active kick and the n_sub substeps (each needs every
+//     colloid's new position, and a block barrier is the cheapest wait at these
+//     sizes).
+// The packed weights (the layout k_sur_net reads) are rebuilt from the network at
+// every mpcd_surrogate_step call.  k_sur_features computes the inputs of the
+// current state on request.
+#include <cuda_bf16.h>
+
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -25,24 +36,35 @@
 namespace {
 
 using namespace bgb;
+typedef __nv_bfloat16 bf16;
 
-constexpr int NF = MPCD_MLP_IN, NO = MPCD_MLP_OUT, KNEAR = 12, MAXC = MPCD_SURROGATE_MAX_COLLOIDS, MAXNB = 64;
+constexpr int NF = MPCD_MLP_IN, NO = MPCD_MLP_OUT, KNEAR = 12, MAXC = MPCD_SURROGATE_MAX_COLLOIDS, CAND = 64;
+constexpr int H = MPCD_MLP_HIDDEN, INP = MLP_IN_PADDED, OUTP = MLP_OUT_PADDED;
 constexpr uint32_t DOM_SUR_KICK = 20, DOM_SUR_ROT = 21;
+constexpr int MAXF = 24;  // force partners per colloid (within the WCA cutoff plus the skin)
 
 struct Sur {
   int Nc, n_sub;
   float L[3], iL[3];
   float M, I, dt, v0, rotdiff_s, ct_feat2;
-  float sig6, sig12, eps, rc2, fc, rlist2, half_skin2, rforce2;
+  float sig6, sig12, eps, rc2, fc, rforce2, rscan2, rlist2, half_skin2;
   uint2 key;
   long long *step;  // device step counter
   float4 *X, *V, *W, *ra, *f;
-  float *feat, *out;
-  int *nbr, *nnb;
-  float4 *xref;     // positions at the last neighbour-list build
-  int *built;       // a list exists
+  float *feat;      // the last step's network inputs [Nc][81]
+  float *out;       // the last step's normalised network outputs [Nc][16]
+  float4 *imp;      // per-substep linear impulse of the drawn exchange [Nc], orientation at the step's start [Nc]
+  uint16_t *fpart;  // force partners [Nc][MAXF], ascending index
+  uint8_t *fpn;     // their count
+  uint16_t *nbl;    // candidate neighbours [Nc][CAND] (within rlist at the last rebuild), ascending index
+  int *nbn;         // their count
+  float4 *xref;     // positions at the last rebuild
+  int *rebuild;     // a colloid moved more than half the skin since (or no lists yet)
   int *err;
-  const float *On, *ymean, *yistd;  // the network's normalised outputs and their normalisation
+  const uint4 *wpk;                   // the packed BF16 weights (k_sur_pack)
+  const float *bias;                  // the network's biases [256][256][256][16]
+  const float *xmean, *xistd;         // input normalisation
+  const float *ymean, *yistd;         // output normalisation
 };
 
 __device__ __forceinline__ float wrapd(float d, float L, float iL) { return d - L * rintf(d * iL); }
@@ -120,6 +142,579 @@ __global__ void __launch_bounds__(128) k_sur_features(const Sur S) {
   }
 }
 
+// ---- the network block ---------------------------------------------------------
+// Weights in fragment order: chunk g holds, for every 8-column tile t of a layer and
+// lane l, one 16-byte word with the lane's mma.sync B fragments of two consecutive
+// 16-deep K steps (k0 = 32 c + 2 (l & 3), rows k0 + {0, 1}, + 8, + 16, + 24 of column
+// 8 t + (l >> 2)), so that a warp's fragments are one conflict-free 16-byte shared
+// load each.  Chunks 0-2: layer 1 (K 96), 3-10: layer 2, 11-18: layer 3 (32 K rows
+// x 256 columns, 16 KB each), 19: layer 4 (K 256 x 16 columns, 8 KB).
+constexpr int ROWS = 16, NCW = 8, NET_THREADS = 32 * (NCW + 1), CHUNK_U4 = 1024, NCHUNK = 20, NSTAGE = 6,
+              LDA = H + 8;
+constexpr int PACK_U4 = 19 * CHUNK_U4 + 512;
+
+constexpr int MAXSUB = 32;  // substeps per MPCD step the colloid-only step supports
+
+struct __align__(128) NetSmem {
+  uint4 ring[NSTAGE][CHUNK_U4];
+  union {
+    float4 xall[MAXC];  // every colloid's position (candidate-list rebuilds)
+    struct {
+      float4 cx[ROWS][CAND], cv[ROWS][CAND];  // the candidates' positions and velocities
+    } c;
+  } u;
+  float4 nz[ROWS][MAXSUB];   // rotational-diffusion Gaussians of the step's substeps
+  float4 sc1[ROWS][MAXSUB];  // sin, cos of the Euler angles Omega dt (x, y) per substep
+  float2 sc2[ROWS][MAXSUB];  // (z)
+  float4 row[4][ROWS];       // the rows' X, V, Omega, ra at the step's start
+  float4 pa[ROWS];           // per-substep angular impulse of the drawn exchange
+  bf16 act[2][ROWS][LDA];
+  float cd[ROWS][CAND];      // candidates within the scan distance: squared distance,
+  int ck[ROWS][CAND];        // colloid,
+  int ce[ROWS][CAND];        // slot in the candidate list
+  alignas(16) uint16_t lst[ROWS][CAND];  // candidate lists
+  int lstn[ROWS];
+  int cn[ROWS];              // candidates within the scan distance per row
+  float feat[ROWS][NF];
+  float out[ROWS][OUTP];
+  alignas(16) float bias[3 * H + OUTP];
+  float xi[ROWS][NO / 2];  // the exchange's Gaussians
+  float xm[NF], xs[NF], ym[NO / 2], ys[NO / 2];
+  unsigned long long full[NSTAGE], empty[NSTAGE];  // a chunk landed / every compute warp is done with it
+  int abort;
+};
+
+__device__ __forceinline__ uint32_t bf16_bits(const bf16 *w, long long i) {
+  return (uint32_t)__bfloat16_as_ushort(w[i]);
+}
+
+// the fragment-order copy of the BF16 weights ([k][n] matrices of 256 / 16 columns)
+__global__ void k_sur_pack(const bf16 *w0, const bf16 *w1, const bf16 *w2, const bf16 *w3, uint4 *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= PACK_U4) return;
+  const bf16 *W;
+  int npad, k0, n;
+  if (i < 19 * CHUNK_U4) {
+    const int g = i / CHUNK_U4, within = i % CHUNK_U4, t = within >> 5, lane = within & 31;
+    const int c = g < 3 ? g : (g < 11 ? g - 3 : g - 11);
+    W = g < 3 ? w0 : (g < 11 ? w1 : w2);
+    npad = H;
+    k0 = 32 * c + 2 * (lane & 3);
+    n = 8 * t + (lane >> 2);
+  } else {
+    const int within = i - 19 * CHUNK_U4, kp = within >> 6, t = (within >> 5) & 1, lane = within & 31;
+    W = w3;
+    npad = OUTP;
+    k0 = 32 * kp + 2 * (lane & 3);
+    n = 8 * t + (lane >> 2);
+  }
+  uint32_t word[4];
+#pragma unroll
+  for (int h = 0; h < 4; ++h) {
+    const long long kb = k0 + 8 * h;
+    word[h] = bf16_bits(W, kb * npad + n) | (bf16_bits(W, (kb + 1) * npad + n) << 16);
+  }
+  out[i] = make_uint4(word[0], word[1], word[2], word[3]);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for phase `parity` of a stage's barrier: gives up after 100 ms (a
+// chunk arrives in microseconds) or 2^24 tries
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity) {
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (int it = 0; it < (1 << 24); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > 100000000ull) break;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// weight chunk g into its stage, one bulk copy counted on the stage's full barrier
+__device__ __forceinline__ void issue_chunk(const Sur &S, NetSmem &sm, int g) {
+  const uint32_t bytes = g < 19 ? CHUNK_U4 * 16 : 512 * 16;
+  unsigned long long *bar = &sm.full[g % NSTAGE];
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(sm.ring[g % NSTAGE])),
+               "l"(S.wpk + (size_t)g * CHUNK_U4), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// a compute warp's wait for chunk g (lane 0, bounded).  After a wait that gave up
+// (or once any wait has) the warp goes on without the chunk and without releasing
+// its stage, so the producer stops too; the results are then flagged, not used.
+__device__ __forceinline__ bool chunk_ready(const Sur &S, NetSmem &sm, int g) {
+  int ok = 0;
+  if ((threadIdx.x & 31) == 0) {
+    volatile int *ab = &sm.abort;
+    ok = !*ab && mbar_wait_bounded(&sm.full[g % NSTAGE], (uint32_t)((g / NSTAGE) & 1));
+    if (!ok && !*ab) {
+      atomicOr(S.err, 4);
+      *ab = 1;
+    }
+  }
+  return __shfl_sync(0xFFFFFFFFu, ok, 0) != 0;
+}
+
+__device__ __forceinline__ void chunk_release(NetSmem &sm, int g, bool ok) {
+  __syncwarp();
+  if (ok && (threadIdx.x & 31) == 0) mbar_arrive(&sm.empty[g % NSTAGE]);
+}
+
+__device__ __forceinline__ void compute_barrier() {  // the compute warps only
+  asm volatile("bar.sync 1, %0;" ::"n"(NCW * 32) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// the A fragment of K step kk (16 rows of the activations)
+__device__ __forceinline__ void a_frag(const bf16 (*A)[LDA], int kk, int gq, int q, uint32_t a[4]) {
+  a[0] = *reinterpret_cast<const uint32_t *>(&A[gq][kk + 2 * q]);
+  a[1] = *reinterpret_cast<const uint32_t *>(&A[gq + 8][kk + 2 * q]);
+  a[2] = *reinterpret_cast<const uint32_t *>(&A[gq][kk + 2 * q + 8]);
+  a[3] = *reinterpret_cast<const uint32_t *>(&A[gq + 8][kk + 2 * q + 8]);
+}
+
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }  // as mlp.cu
+
+// One block per 16 colloids: eight compute warps (two colloids each in the
+// neighbour and feature phases, 32 columns each in the network) and one producer
+// warp that streams the weights.
+//   neighbours within max(three radii, the force cutoff plus the skin): from each
+//   colloid's candidate list (colloids within that distance plus a skin of 1 at the
+//   last rebuild, ascending index), or, when k_sur_md has flagged that a colloid
+//   moved more than half the skin since then, from all pairs (and the lists rebuilt);
+//   the features (V, Omega, ra, then the 12 nearest within three radii, nearest first,
+//   ties by index, zero padded: the layout of brownian_gb300.closure.features), raw
+//   to S.feat and normalised (clipped to six standard deviations) as the BF16 input
+//   rows; the force partners (within the cutoff plus the skin, ascending index);
+//   the step's draws (rotational diffusion, the exchange's Gaussians);
+//   the four layers (the mlp.cu forward pass: K steps in ascending order into one
+//   FP32 accumulator, bias, SiLU, BF16 between layers), the weights streamed by bulk
+//   copies NSTAGE chunks ahead (full / empty barriers per stage); from the outputs
+//   the Gaussian draw of the exchange (per-substep impulses for k_sur_md);
+//   the orientation over the step's substeps: Omega takes its share of the angular
+//   exchange each substep and ra the Euler rotation and the rotational diffusion
+//   (update_activity_direction); neither depends on positions or forces.
+__global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
+  extern __shared__ __align__(128) unsigned char net_smem[];
+  NetSmem &sm = *reinterpret_cast<NetSmem *>(net_smem);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gq = lane >> 2, q = lane & 3;
+  const unsigned lt = (1u << lane) - 1u;
+  const int j0 = blockIdx.x * ROWS;
+  const uint32_t step = (uint32_t)*S.step;
+  const bool producer = warp == NCW;
+  if (tid == NCW * 32) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], NCW);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    sm.abort = 0;
+    // the first weight chunks stream in while the neighbours are found
+    for (int g = 0; g < NSTAGE; ++g) issue_chunk(S, sm, g);
+  }
+  // the rows' state, the biases, the normalisation and the candidate lists (or every
+  // position, for a rebuild): independent loads, all in flight together
+  const bool rebuild = *S.rebuild != 0;
+  if (tid < 4 * ROWS) {
+    const int r = tid % ROWS, f = tid / ROWS, j = j0 + r;
+    const float4 *src = f == 0 ? S.X : (f == 1 ? S.V : (f == 2 ? S.W : S.ra));
+    if (j < S.Nc) sm.row[f][r] = src[j];
+  }
+  static_assert((3 * H + OUTP) / 4 <= NET_THREADS && NF <= NET_THREADS, "one load per thread");
+  if (tid < (3 * H + OUTP) / 4) reinterpret_cast<uint4 *>(sm.bias)[tid] = reinterpret_cast<const uint4 *>(S.bias)[tid];
+  if (tid < NF) {
+    sm.xm[tid] = S.xmean[tid];
+    sm.xs[tid] = S.xistd[tid];
+  }
+  if (tid < NO / 2) {
+    sm.ym[tid] = S.ymean[tid];
+    sm.ys[tid] = S.yistd[tid];
+  }
+  if (rebuild) {
+    for (int i0 = tid; i0 < S.Nc; i0 += 8 * NET_THREADS) {  // eight loads in flight per thread
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i0 + u * NET_THREADS < S.Nc) v[u] = S.X[i0 + u * NET_THREADS];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i0 + u * NET_THREADS < S.Nc) sm.u.xall[i0 + u * NET_THREADS] = v[u];
+    }
+  } else {
+    static_assert(ROWS * CAND / 8 <= NET_THREADS, "one 16-byte piece of the lists per thread");
+    if (tid < ROWS * CAND / 8) {
+      const int r = tid / (CAND / 8), qv = tid % (CAND / 8), j = j0 + r;
+      if (j < S.Nc)
+        reinterpret_cast<uint4 *>(sm.lst[r])[qv] = reinterpret_cast<const uint4 *>(S.nbl + (size_t)j * CAND)[qv];
+    }
+    if (tid < ROWS) sm.lstn[tid] = j0 + tid < S.Nc ? S.nbn[j0 + tid] : 0;
+  }
+  __syncthreads();
+  if (rebuild) {
+    // all pairs: colloids within the list distance, ascending index
+    for (int c = 0; c < ROWS / NCW && !producer; ++c) {
+      const int r = (ROWS / NCW) * warp + c, j = j0 + r;
+      if (j >= S.Nc) {
+        if (lane == 0) sm.lstn[r] = 0;
+        continue;
+      }
+      const float4 xj = sm.row[0][r];
+      int nl = 0;
+      for (int k0 = 0; k0 < S.Nc; k0 += 32) {
+        const int k = k0 + lane;
+        float d2 = 1e30f;
+        if (k < S.Nc && k != j) {
+          const float4 xk = sm.u.xall[k];
+          const float dx = wrapd(xk.x - xj.x, S.L[0], S.iL[0]), dy = wrapd(xk.y - xj.y, S.L[1], S.iL[1]),
+                      dz = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
+          d2 = dx * dx + dy * dy + dz * dz;
+        }
+        const bool inl = d2 < S.rlist2;
+        const unsigned ml = __ballot_sync(0xFFFFFFFFu, inl);
+        if (inl) {
+          const int slot = nl + __popc(ml & lt);
+          if (slot < CAND) {
+            S.nbl[(size_t)j * CAND + slot] = (uint16_t)k;
+            sm.lst[r][slot] = (uint16_t)k;
+          }
+        }
+        nl += __popc(ml);
+      }
+      if (lane == 0) {
+        sm.lstn[r] = min(nl, CAND);
+        S.nbn[j] = min(nl, CAND);
+        S.xref[j] = xj;
+        if (nl > CAND) atomicOr(S.err, 1);
+      }
+    }
+    __syncthreads();  // (the candidates' positions below overwrite xall)
+  }
+  // the candidates' positions and velocities, all loads in flight together
+  {
+    constexpr int PT = (ROWS * CAND + NET_THREADS - 1) / NET_THREADS;
+    float4 px[PT], pv[PT];
+#pragma unroll
+    for (int u = 0; u < PT; ++u) {
+      const int i = tid + NET_THREADS * u, r = i / CAND, e = i % CAND;
+      if (i < ROWS * CAND && e < sm.lstn[r]) {
+        const int k = sm.lst[r][e];
+        px[u] = S.X[k];
+        pv[u] = S.V[k];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < PT; ++u) {
+      const int i = tid + NET_THREADS * u, r = i / CAND, e = i % CAND;
+      if (i < ROWS * CAND && e < sm.lstn[r]) {
+        sm.u.c.cx[r][e] = px[u];
+        sm.u.c.cv[r][e] = pv[u];
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = 0; c < ROWS / NCW && !producer; ++c) {
+    const int r = (ROWS / NCW) * warp + c, j = j0 + r;
+    float *o = sm.feat[r];
+    for (int col = lane; col < NF; col += 32) o[col] = 0.f;
+    __syncwarp();
+    if (j >= S.Nc) continue;
+    const float4 xj = sm.row[0][r], vj = sm.row[1][r];
+    // neighbours within the scan distance, ascending index
+    const int nlst = sm.lstn[r];
+    int n = 0;
+    for (int e0 = 0; e0 < nlst; e0 += 32) {
+      const int e = e0 + lane;
+      float d2 = 1e30f;
+      if (e < nlst) {
+        const float4 xk = sm.u.c.cx[r][e];
+        const float dx = wrapd(xk.x - xj.x, S.L[0], S.iL[0]), dy = wrapd(xk.y - xj.y, S.L[1], S.iL[1]),
+                    dz = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
+        d2 = dx * dx + dy * dy + dz * dz;
+      }
+      const bool in = d2 < S.rscan2;
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, in);
+      if (in) {
+        const int slot = n + __popc(m & lt);  // slot <= e < CAND
+        sm.cd[r][slot] = d2;
+        sm.ck[r][slot] = sm.lst[r][e];
+        sm.ce[r][slot] = e;
+      }
+      n += __popc(m);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      o[0] = vj.x; o[1] = vj.y; o[2] = vj.z;
+      const float4 wj = sm.row[2][r], aj = sm.row[3][r];
+      o[3] = wj.x; o[4] = wj.y; o[5] = wj.z; o[6] = aj.x; o[7] = aj.y; o[8] = aj.z;
+    }
+    // the 12 nearest within three radii: each candidate's rank by (distance, index)
+    for (int e0 = 0; e0 < n; e0 += 32) {
+      const int e = e0 + lane;
+      const bool have = e < n;
+      const float d2 = have ? sm.cd[r][e] : 3.0e38f;
+      const int k = have ? sm.ck[r][e] : 0x7FFFFFFF;
+      int rank = 0;
+      if (n <= 32) {
+        for (int f = 0; f < n; ++f) {
+          const float df = __shfl_sync(0xFFFFFFFFu, d2, f);
+          const int kf = __shfl_sync(0xFFFFFFFFu, k, f);
+          rank += (df < S.ct_feat2) && (df < d2 || (df == d2 && kf < k));
+        }
+      } else {
+        for (int f = 0; f < n; ++f) {
+          const float df = sm.cd[r][f];
+          rank += (df < S.ct_feat2) && (df < d2 || (df == d2 && sm.ck[r][f] < k));
+        }
+      }
+      if (have && d2 < S.ct_feat2 && rank < KNEAR) {
+        const int ce = sm.ce[r][e];
+        const float4 xk = sm.u.c.cx[r][ce], vk = sm.u.c.cv[r][ce];
+        float *qf = o + 9 + 6 * rank;
+        qf[0] = wrapd(xk.x - xj.x, S.L[0], S.iL[0]);
+        qf[1] = wrapd(xk.y - xj.y, S.L[1], S.iL[1]);
+        qf[2] = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
+        qf[3] = vk.x - vj.x; qf[4] = vk.y - vj.y; qf[5] = vk.z - vj.z;
+      }
+    }
+    // the force partners, ascending index
+    int m = 0;
+    for (int e0 = 0; e0 < n; e0 += 32) {
+      const int e = e0 + lane;
+      const bool in = e < n && sm.cd[r][e] < S.rforce2;
+      const unsigned b = __ballot_sync(0xFFFFFFFFu, in);
+      if (in) {
+        const int slot = m + __popc(b & lt);
+        if (slot < MAXF) S.fpart[(size_t)j * MAXF + slot] = (uint16_t)sm.ck[r][e];
+      }
+      m += __popc(b);
+    }
+    if (lane == 0) {
+      S.fpn[j] = (uint8_t)min(m, MAXF);
+      if (m > MAXF) atomicOr(S.err, 2);
+    }
+  }
+  // the step's draws: rotational diffusion per substep, the exchange's six Gaussians
+  for (int i = tid; i < ROWS * (S.n_sub + 1); i += NET_THREADS) {
+    const int r = i % ROWS, l = i / ROWS, j = j0 + r;
+    if (j >= S.Nc) continue;
+    if (l < S.n_sub) {
+      if (S.rotdiff_s > 0.f) {
+        const uint4 d = draw4(S.key, DOM_SUR_ROT, 0, (uint32_t)(j + 1), 0, step * S.n_sub + l);
+        const float2 g0 = normal2(d.x, d.y), g1 = normal2(d.z, d.w);
+        sm.nz[r][l] = make_float4(g0.x, g0.y, g1.x, 0.f);
+      }
+    } else {
+      const uint4 r0 = draw4(S.key, DOM_SUR_KICK, 0, (uint32_t)(j + 1), 0, step);
+      const uint4 r1 = draw4(S.key, DOM_SUR_KICK, 1, (uint32_t)(j + 1), 0, step);
+      const float2 g0 = normal2(r0.x, r0.y), g1 = normal2(r0.z, r0.w), g2 = normal2(r1.x, r1.y);
+      sm.xi[r][0] = g0.x; sm.xi[r][1] = g0.y; sm.xi[r][2] = g1.x;
+      sm.xi[r][3] = g1.y; sm.xi[r][4] = g2.x; sm.xi[r][5] = g2.y;
+    }
+  }
+  __syncthreads();
+  // raw inputs to S.feat, normalised BF16 rows to act[0]
+  for (int i = tid; i < ROWS * INP; i += NET_THREADS) {
+    const int r = i / INP, c = i % INP, j = j0 + r;
+    float z = 0.f;
+    if (c < NF) {
+      const float x = sm.feat[r][c];
+      if (j < S.Nc) S.feat[(size_t)j * NF + c] = x;
+      z = (x - sm.xm[c]) * sm.xs[c];
+    }
+    sm.act[0][r][c] = __float2bfloat16(fminf(fmaxf(z, -MLP_INPUT_CLIP), MLP_INPUT_CLIP));
+  }
+  __syncthreads();
+  if (producer) {
+    if (lane == 0) {
+      // chunk g into its stage once every compute warp is done with chunk g - NSTAGE
+      volatile int *ab = &sm.abort;
+      int issued = NSTAGE;
+      for (int g = NSTAGE; g < NCHUNK && !*ab; ++g) {
+        if (!mbar_wait_bounded(&sm.empty[g % NSTAGE], (uint32_t)((g / NSTAGE - 1) & 1))) {
+          atomicOr(S.err, 4);
+          *ab = 1;
+          break;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue_chunk(S, sm, g);
+        issued = g + 1;
+      }
+      // every copy issued (the last one into each stage) lands before the block exits
+      for (int c = issued > NSTAGE ? issued - NSTAGE : 0; c < issued; ++c)
+        mbar_wait_bounded(&sm.full[c % NSTAGE], (uint32_t)((c / NSTAGE) & 1));
+    }
+  } else {
+    // three hidden layers: compute warp w takes columns 32 w .. 32 w + 31
+    int g = 0;
+#pragma unroll 1
+    for (int layer = 0; layer < 3; ++layer) {
+      const bf16(*A)[LDA] = sm.act[layer & 1];
+      bf16(*Z)[LDA] = sm.act[(layer + 1) & 1];
+      const int nch = layer == 0 ? INP / 32 : H / 32;
+      float acc[4][4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[t][e] = 0.f;
+#pragma unroll 1
+      for (int c = 0; c < nch; ++c, ++g) {
+        const bool ok = chunk_ready(S, sm, g);
+        const uint4 *B = sm.ring[g % NSTAGE];
+        uint4 b[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) b[t] = B[(4 * warp + t) * 32 + lane];
+        uint32_t a[4];
+        a_frag(A, 32 * c, gq, q, a);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) mma_bf16(acc[t], a, b[t].x, b[t].y);
+        a_frag(A, 32 * c + 16, gq, q, a);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) mma_bf16(acc[t], a, b[t].z, b[t].w);
+        chunk_release(sm, g, ok);
+      }
+      const float *bias = sm.bias + H * layer;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int n0 = 8 * (4 * warp + t) + 2 * q;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float v0 = acc[t][2 * h] + bias[n0], v1 = acc[t][2 * h + 1] + bias[n0 + 1];
+          v0 = v0 * sigm(v0);
+          v1 = v1 * sigm(v1);
+          __nv_bfloat162 pr;
+          pr.x = __float2bfloat16(v0);
+          pr.y = __float2bfloat16(v1);
+          *reinterpret_cast<__nv_bfloat162 *>(&Z[gq + 8 * h][n0]) = pr;
+        }
+      }
+      compute_barrier();
+    }
+    // the output layer (16 columns, 12 used): compute warps 0 and 1, one 8-column tile each
+    if (warp < 2) {
+      const bool ok = chunk_ready(S, sm, g);
+      (void)ok;
+      const uint4 *B = sm.ring[g % NSTAGE];
+      const bf16(*A)[LDA] = sm.act[1];
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+      for (int kp = 0; kp < H / 32; ++kp) {
+        const uint4 b = B[(2 * kp + warp) * 32 + lane];
+        uint32_t a[4];
+        a_frag(A, 32 * kp, gq, q, a);
+        mma_bf16(acc, a, b.x, b.y);
+        a_frag(A, 32 * kp + 16, gq, q, a);
+        mma_bf16(acc, a, b.z, b.w);
+      }
+      const float *bias = sm.bias + 3 * H;
+      const int n0 = 8 * warp + 2 * q;
+      sm.out[gq][n0] = acc[0] + bias[n0];
+      sm.out[gq][n0 + 1] = acc[1] + bias[n0 + 1];
+      sm.out[gq + 8][n0] = acc[2] + bias[n0];
+      sm.out[gq + 8][n0 + 1] = acc[3] + bias[n0 + 1];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < ROWS * OUTP; i += NET_THREADS) {
+    const int r = i / OUTP, j = j0 + r;
+    if (j < S.Nc) S.out[(size_t)j * OUTP + i % OUTP] = sm.out[r][i % OUTP];
+  }
+  if (tid < ROWS && j0 + tid < S.Nc) {
+    const int r = tid, j = j0 + r;
+    // the exchange: the network's normalised outputs -> mean and standard deviation in
+    // physical units, the Gaussian draw, spread in equal parts over the substeps (the
+    // fluid collides every substep)
+    const float *o = sm.out[r];
+    float dp[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float is = sm.ys[k];
+      const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
+      dp[k] = (o[k] + __expf(0.5f * lv) * sm.xi[r][k]) / is + sm.ym[k];
+    }
+    const float fm = 1.f / (S.M * S.n_sub), fi = 1.f / (S.I * S.n_sub);
+    sm.pa[r] = make_float4(dp[3] * fi, dp[4] * fi, dp[5] * fi, 0.f);
+    S.imp[j] = make_float4(dp[0] * fm, dp[1] * fm, dp[2] * fm, 0.f);
+    S.imp[S.Nc + j] = sm.row[3][r];  // the orientation run()'s kick uses
+  }
+  __syncthreads();
+  // per (row, substep): Omega after the substep's share of the angular exchange (the
+  // same sequence of additions as the substeps make) and the sines and cosines of
+  // its Euler angles, all substeps at once
+  for (int i = tid; i < ROWS * S.n_sub; i += NET_THREADS) {
+    const int r = i % ROWS, l = i / ROWS;
+    if (j0 + r >= S.Nc) continue;
+    float4 w = sm.row[2][r];
+    const float4 pa = sm.pa[r];
+    for (int s = 0; s <= l; ++s) {
+      w.x += pa.x; w.y += pa.y; w.z += pa.z;
+    }
+    float sx, cx, sy, cy, sz, cz;
+    __sincosf(w.x * S.dt, &sx, &cx); __sincosf(w.y * S.dt, &sy, &cy); __sincosf(w.z * S.dt, &sz, &cz);
+    sm.sc1[r][l] = make_float4(sx, cx, sy, cy);
+    sm.sc2[r][l] = make_float2(sz, cz);
+  }
+  __syncthreads();
+  // the orientation through the substeps: the Euler matrix of Omega dt, then the
+  // rotational diffusion (update_activity_direction plus Dr)
+  if (tid < ROWS && j0 + tid < S.Nc) {
+    const int r = tid, j = j0 + r;
+    float4 w = sm.row[2][r], a = sm.row[3][r];
+    const float4 pa = sm.pa[r];
+    for (int l = 0; l < S.n_sub; ++l) {
+      w.x += pa.x; w.y += pa.y; w.z += pa.z;
+      const float4 s1 = sm.sc1[r][l];
+      const float2 s2 = sm.sc2[r][l];
+      const float sx = s1.x, cx = s1.y, sy = s1.z, cy = s1.w, sz = s2.x, cz = s2.y;
+      const float4 aa = a;
+      float ax = cy * cz * aa.x - cy * sz * aa.y + sy * aa.z;
+      float ay = (sx * sy * cz + cx * sz) * aa.x + (-sx * sy * sz + cx * cz) * aa.y - sx * cy * aa.z;
+      float az = (-cx * sy * cz + sx * sz) * aa.x + (cx * sy * sz + sx * cz) * aa.y + cx * cy * aa.z;
+      if (S.rotdiff_s > 0.f) {
+        const float4 gz = sm.nz[r][l];
+        const float d = gz.x * ax + gz.y * ay + gz.z * az;
+        ax += S.rotdiff_s * (gz.x - d * ax); ay += S.rotdiff_s * (gz.y - d * ay); az += S.rotdiff_s * (gz.z - d * az);
+      }
+      const float in = rsqrtf(ax * ax + ay * ay + az * az);
+      a = make_float4(ax * in, ay * in, az * in, 0.f);
+    }
+    S.W[j] = w;
+    S.ra[j] = a;
+  }
+}
+
+// ---- the substeps ---------------------------------------------------------------
 __device__ __forceinline__ float3 wca_pair(const Sur &S, float dx, float dy, float dz) {
   const float r2 = dx * dx + dy * dy + dz * dz;
   if (!(r2 < S.rc2)) return make_float3(0.f, 0.f, 0.f);
@@ -128,106 +723,43 @@ __device__ __forceinline__ float3 wca_pair(const Sur &S, float dx, float dy, flo
   return make_float3(mag * dx * ir, mag * dy * ir, mag * dz * ir);
 }
 
-// One MPCD step of every colloid in one block (one or two colloids per thread,
-// their velocity, angular velocity, orientation and force in registers, all
-// positions and velocities in shared memory):
-//   the fluid's exchange drawn from the network's Gaussian (its outputs S.On), applied in equal
-//   parts after each substep's position update, and run()'s kick at the start;
-//   the neighbour list (pairs within three radii plus a skin), rebuilt only when a
-//   colloid has moved more than half the skin since the last build;
-//   n_sub substeps of update_pos_md, update_activity_direction, compute_force_md,
-//   update_velocity_colloid;
-//   the network inputs of the next step (S.feat).
-constexpr int MAXF = 24;  // force partners per colloid (within the WCA cutoff plus the skin)
-
+// One block, one or two colloids per thread (velocity, force and the step's
+// impulse in registers; positions and force partners in shared memory): run()'s
+// kick along the orientation at the step's start, then n_sub substeps of
+// update_pos_md, the substep's share of the exchange, compute_force_md at the new
+// positions and update_velocity_colloid.  At the end: whether a colloid has moved
+// more than half the skin since the candidate lists were built.
 template <int PER>  // colloids per thread: 1 up to 1024 colloids, 2 up to MAXC
 __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
   extern __shared__ float4 smem[];
-  float4 *sX = smem, *sV = smem + MAXC;
-  uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);  // [MAXC][MAXF] force partners
+  float4 *sX = smem;
+  uint16_t *sF = reinterpret_cast<uint16_t *>(smem + MAXC);      // [MAXC][MAXF] force partners
   uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MAXC * MAXF);  // [MAXC] their count
-  __shared__ int s_rebuild;
   const int T = blockDim.x, tid = threadIdx.x;
-  float4 v[PER], w[PER], a[PER], fo[PER], pl[PER], pa[PER];
-  const uint32_t step = (uint32_t)*S.step;
-  if (tid == 0) s_rebuild = 0;
-  __syncthreads();
+  float4 v[PER], fo[PER], pl[PER];
+  {
+    const uint4 *src = reinterpret_cast<const uint4 *>(S.fpart);
+    uint4 *dst = reinterpret_cast<uint4 *>(sF);
+    const int nq = S.Nc * (MAXF * 2 / 16);
+    for (int i0 = tid; i0 < nq; i0 += 4 * T) {  // four loads in flight per thread
+      uint4 qv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * T < nq) qv[u] = src[i0 + u * T];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * T < nq) dst[i0 + u * T] = qv[u];
+    }
+    for (int i = tid; i < S.Nc; i += T) sFn[i] = S.fpn[i];
+  }
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
-    const float4 x = S.X[j];
-    sX[j] = x;
-    v[u] = S.V[j]; w[u] = S.W[j]; a[u] = S.ra[j]; fo[u] = S.f[j];
-    // the exchange and the active kick
-    // the network's normalised outputs -> mean and standard deviation in physical units
-    const float *o = S.On + (size_t)j * MLP_OUT_PADDED;
-    const uint4 r0 = draw4(S.key, DOM_SUR_KICK, 0, (uint32_t)(j + 1), 0, step);
-    const uint4 r1 = draw4(S.key, DOM_SUR_KICK, 1, (uint32_t)(j + 1), 0, step);
-    const float2 g0 = normal2(r0.x, r0.y), g1 = normal2(r0.z, r0.w), g2 = normal2(r1.x, r1.y);
-    const float xi[6] = {g0.x, g0.y, g1.x, g1.y, g2.x, g2.y};
-    float dp[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const float is = S.yistd[k];
-      const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
-      dp[k] = (o[k] + __expf(0.5f * lv) * xi[k]) / is + S.ymean[k];
-    }
-    // the exchange arrives over the step's substeps (the fluid collides every substep),
-    // the active kick at its start (run())
-    const float fm = 1.f / (S.M * S.n_sub), fi = 1.f / (S.I * S.n_sub);
-    pl[u] = make_float4(dp[0] * fm, dp[1] * fm, dp[2] * fm, 0.f);
-    pa[u] = make_float4(dp[3] * fi, dp[4] * fi, dp[5] * fi, 0.f);
-    v[u].x += S.v0 * a[u].x; v[u].y += S.v0 * a[u].y; v[u].z += S.v0 * a[u].z;
-    const float4 x0 = S.xref[j];
-    const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
-                dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
-    if (dx * dx + dy * dy + dz * dz > S.half_skin2 || *S.built == 0) s_rebuild = 1;
-  }
-  __syncthreads();
-  if (s_rebuild) {
-#pragma unroll
-    for (int u = 0; u < PER; ++u) {
-      const int j = tid + T * u;
-      if (j >= S.Nc) continue;
-      int n = 0;
-      const float4 xj = sX[j];
-      for (int k = 0; k < S.Nc; ++k) {
-        if (k == j) continue;
-        const float4 xk = sX[k];
-        const float dx = wrapd(xj.x - xk.x, S.L[0], S.iL[0]), dy = wrapd(xj.y - xk.y, S.L[1], S.iL[1]),
-                    dz = wrapd(xj.z - xk.z, S.L[2], S.iL[2]);
-        if (dx * dx + dy * dy + dz * dz < S.rlist2) {
-          if (n < MAXNB) S.nbr[j * MAXNB + n] = k;
-          else atomicOr(S.err, 1);
-          ++n;
-        }
-      }
-      S.nnb[j] = min(n, MAXNB);
-      S.xref[j] = xj;
-    }
-    if (tid == 0) *S.built = 1;
-  }
-  // the force partners of this step (pairs within the cutoff plus the skin), in shared memory
-#pragma unroll
-  for (int u = 0; u < PER; ++u) {
-    const int j = tid + T * u;
-    if (j >= S.Nc) continue;
-    const float4 xj = sX[j];
-    const int n = S.nnb[j];
-    int m = 0;
-    for (int e = 0; e < n; ++e) {
-      const int k = S.nbr[j * MAXNB + e];
-      const float4 xk = sX[k];
-      const float dx = wrapd(xj.x - xk.x, S.L[0], S.iL[0]), dy = wrapd(xj.y - xk.y, S.L[1], S.iL[1]),
-                  dz = wrapd(xj.z - xk.z, S.L[2], S.iL[2]);
-      if (dx * dx + dy * dy + dz * dz < S.rforce2) {
-        if (m < MAXF) sF[j * MAXF + m] = (uint16_t)k;
-        else atomicOr(S.err, 2);
-        ++m;
-      }
-    }
-    sFn[j] = (uint8_t)min(m, MAXF);
+    sX[j] = S.X[j];
+    v[u] = S.V[j]; fo[u] = S.f[j]; pl[u] = S.imp[j];
+    const float4 a = S.imp[S.Nc + j];
+    v[u].x += S.v0 * a.x; v[u].y += S.v0 * a.y; v[u].z += S.v0 * a.z;
   }
   const float hdt2m = 0.5f * S.dt * S.dt / S.M, hdtm = 0.5f * S.dt / S.M;
   for (int l = 0; l < S.n_sub; ++l) {
@@ -249,92 +781,54 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
       if (j >= S.Nc) continue;
       // this substep's share of the fluid exchange (fluid_colloid_collision)
       v[u].x += pl[u].x; v[u].y += pl[u].y; v[u].z += pl[u].z;
-      w[u].x += pa[u].x; w[u].y += pa[u].y; w[u].z += pa[u].z;
-      // update_activity_direction: the Euler matrix of Omega dt, then rotational diffusion
-      float sx, cx, sy, cy, sz, cz;
-      __sincosf(w[u].x * S.dt, &sx, &cx); __sincosf(w[u].y * S.dt, &sy, &cy); __sincosf(w[u].z * S.dt, &sz, &cz);
-      const float4 aa = a[u];
-      float ax = cy * cz * aa.x - cy * sz * aa.y + sy * aa.z;
-      float ay = (sx * sy * cz + cx * sz) * aa.x + (-sx * sy * sz + cx * cz) * aa.y - sx * cy * aa.z;
-      float az = (-cx * sy * cz + sx * sz) * aa.x + (cx * sy * sz + sx * cz) * aa.y + cx * cy * aa.z;
-      if (S.rotdiff_s > 0.f) {
-        const uint4 r = draw4(S.key, DOM_SUR_ROT, 0, (uint32_t)(j + 1), 0, step * S.n_sub + l);
-        const float2 g0 = normal2(r.x, r.y), g1 = normal2(r.z, r.w);
-        const float d = g0.x * ax + g0.y * ay + g1.x * az;
-        ax += S.rotdiff_s * (g0.x - d * ax); ay += S.rotdiff_s * (g0.y - d * ay); az += S.rotdiff_s * (g1.x - d * az);
-      }
-      const float in = rsqrtf(ax * ax + ay * ay + az * az);
-      a[u] = make_float4(ax * in, ay * in, az * in, 0.f);
       // compute_force_md at the new positions, update_velocity_colloid
       float3 fn = make_float3(0.f, 0.f, 0.f);
       const float4 xj = sX[j];
       const int n = sFn[j];
-      for (int e = 0; e < n; ++e) {
-        const float4 xk = sX[sF[j * MAXF + e]];
-        const float3 fp = wca_pair(S, wrapd(xj.x - xk.x, S.L[0], S.iL[0]), wrapd(xj.y - xk.y, S.L[1], S.iL[1]),
-                                   wrapd(xj.z - xk.z, S.L[2], S.iL[2]));
-        fn.x += fp.x; fn.y += fp.y; fn.z += fp.z;
+      for (int e = 0; e < n; e += 4) {  // four partners' positions fetched together, summed in order
+        const uint2 kk = *reinterpret_cast<const uint2 *>(sF + j * MAXF + e);
+        const int k4[4] = {(int)(kk.x & 0xFFFFu), (int)(kk.x >> 16), (int)(kk.y & 0xFFFFu), (int)(kk.y >> 16)};
+        float4 xk[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) xk[i] = sX[e + i < n ? k4[i] : j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (e + i >= n) break;
+          const float3 fp = wca_pair(S, wrapd(xj.x - xk[i].x, S.L[0], S.iL[0]), wrapd(xj.y - xk[i].y, S.L[1], S.iL[1]),
+                                     wrapd(xj.z - xk[i].z, S.L[2], S.iL[2]));
+          fn.x += fp.x; fn.y += fp.y; fn.z += fp.z;
+        }
       }
       v[u].x += (fo[u].x + fn.x) * hdtm; v[u].y += (fo[u].y + fn.y) * hdtm; v[u].z += (fo[u].z + fn.z) * hdtm;
       fo[u] = make_float4(fn.x, fn.y, fn.z, 0.f);
     }
   }
+  int moved = 0;
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
-    sV[j] = v[u];
-    S.X[j] = sX[j]; S.V[j] = v[u]; S.W[j] = w[u]; S.ra[j] = a[u]; S.f[j] = fo[u];
+    const float4 x = sX[j], x0 = S.xref[j];
+    S.X[j] = x; S.V[j] = v[u]; S.f[j] = fo[u];
+    const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
+                dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
+    moved |= dx * dx + dy * dy + dz * dz > S.half_skin2;
   }
-  __syncthreads();
-  // the next step's network inputs: the 12 nearest colloids within three radii from the list
-#pragma unroll
-  for (int u = 0; u < PER; ++u) {
-    const int j = tid + T * u;
-    if (j >= S.Nc) continue;
-    // the nearest KNEAR as (d2, k) in registers: every candidate is passed down a
-    // fully unrolled chain of compare-and-swap, nearest (then lowest index) first
-    float bd[KNEAR];
-    int bk[KNEAR];
-#pragma unroll
-    for (int m = 0; m < KNEAR; ++m) { bd[m] = 3.0e38f; bk[m] = 0x7FFFFFFF; }
-    const float4 xj = sX[j];
-    const int n = S.nnb[j];
-    for (int e = 0; e < n; ++e) {
-      int k = S.nbr[j * MAXNB + e];
-      const float4 xk = sX[k];
-      const float dx = wrapd(xk.x - xj.x, S.L[0], S.iL[0]), dy = wrapd(xk.y - xj.y, S.L[1], S.iL[1]),
-                  dz = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
-      float d2 = dx * dx + dy * dy + dz * dz;
-      if (!(d2 < S.ct_feat2)) continue;
-#pragma unroll
-      for (int m = 0; m < KNEAR; ++m) {
-        const bool less = d2 < bd[m] || (d2 == bd[m] && k < bk[m]);
-        const float td = less ? bd[m] : d2;
-        const int tk = less ? bk[m] : k;
-        bd[m] = less ? d2 : bd[m];
-        bk[m] = less ? k : bk[m];
-        d2 = td;
-        k = tk;
-      }
-    }
-    float *o = S.feat + (size_t)j * NF;
-    o[0] = v[u].x; o[1] = v[u].y; o[2] = v[u].z; o[3] = w[u].x; o[4] = w[u].y; o[5] = w[u].z;
-    o[6] = a[u].x; o[7] = a[u].y; o[8] = a[u].z;
-#pragma unroll
-    for (int m = 0; m < KNEAR; ++m) {
-      float *q = o + 9 + 6 * m;
-      if (bk[m] != 0x7FFFFFFF) {
-        const float4 xk = sX[bk[m]], vk = sV[bk[m]];
-        q[0] = wrapd(xk.x - xj.x, S.L[0], S.iL[0]); q[1] = wrapd(xk.y - xj.y, S.L[1], S.iL[1]);
-        q[2] = wrapd(xk.z - xj.z, S.L[2], S.iL[2]);
-        q[3] = vk.x - v[u].x; q[4] = vk.y - v[u].y; q[5] = vk.z - v[u].z;
-      } else {
-        q[0] = q[1] = q[2] = q[3] = q[4] = q[5] = 0.f;
-      }
-    }
+  moved = __syncthreads_or(moved);
+  if (tid == 0) {
+    *S.rebuild = moved;
+    *S.step += 1;
   }
-  if (tid == 0) *S.step += 1;
+}
+
+// normalised outputs -> physical units (the arithmetic of mpcd_mlp_forward)
+__global__ void k_sur_denorm(const Sur S, float *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S.Nc * NO) return;
+  const int r = i / NO, k = i % NO, ny = NO / 2;
+  const float v = S.out[(size_t)r * OUTP + k];
+  out[i] = k < ny ? v / S.yistd[k] + S.ymean[k]
+                  : fminf(fmaxf(v, -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP) - 2.f * __logf(S.yistd[k - ny]);
 }
 
 __global__ void k_sur_forces(const Sur S) {
@@ -365,6 +859,8 @@ struct mpcd_surrogate {
   mpcd_mlp *net = nullptr;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t exec = nullptr;
+  uint4 *wpk = nullptr;
+  float *outd = nullptr;  // the outputs in physical units (mpcd_surrogate_outputs)
   std::vector<void *> allocs;
   std::string err;
 };
@@ -388,17 +884,27 @@ T *salloc(mpcd_surrogate *s, size_t n) {
   return static_cast<T *>(p);
 }
 
-constexpr size_t kSmem = 2 * MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16_t) + MAXC;
+constexpr size_t kMdSmem = MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16_t) + MAXC;
+constexpr size_t kNetSmem = sizeof(NetSmem);
 
 int enqueue_step(mpcd_surrogate *s) {
   const Sur &S = s->S;
-  // S.feat holds the current state's network inputs (set_state, or the previous step)
-  int r = mlp_stage(s->net, S.feat, S.Nc, s->stream);
-  if (r) return sfail(s, r, std::string("closure network: ") + mpcd_mlp_last_error(s->net));
-  mlp_layers(s->net, S.Nc, s->stream);
-  if (S.Nc <= 1024) k_sur_md<1><<<1, 1024, kSmem, s->stream>>>(S);
-  else k_sur_md<2><<<1, 1024, kSmem, s->stream>>>(S);
-  return MPCD_OK;
+  k_sur_net<<<(S.Nc + ROWS - 1) / ROWS, NET_THREADS, kNetSmem, s->stream>>>(S);
+  if (S.Nc <= 1024) k_sur_md<1><<<1, (S.Nc + 31) / 32 * 32, kMdSmem, s->stream>>>(S);
+  else k_sur_md<2><<<1, 1024, kMdSmem, s->stream>>>(S);
+  return cudaGetLastError() == cudaSuccess ? MPCD_OK : sfail(s, MPCD_ERR_CUDA, "step launch");
+}
+
+// the network's current weights in the order k_sur_net reads them
+int pack_weights(mpcd_surrogate *s) {
+  const MlpIO io = mlp_io(s->net);
+  s->S.bias = io.bias;
+  s->S.xmean = io.xmean; s->S.xistd = io.xistd;
+  s->S.ymean = io.ymean; s->S.yistd = io.yistd;
+  k_sur_pack<<<(PACK_U4 + 255) / 256, 256, 0, s->stream>>>(
+      static_cast<const bf16 *>(io.w[0]), static_cast<const bf16 *>(io.w[1]), static_cast<const bf16 *>(io.w[2]),
+      static_cast<const bf16 *>(io.w[3]), s->wpk);
+  return cudaGetLastError() == cudaSuccess ? MPCD_OK : sfail(s, MPCD_ERR_CUDA, "weight packing");
 }
 
 }  // namespace
@@ -406,18 +912,13 @@ int enqueue_step(mpcd_surrogate *s) {
 extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_surrogate **out) {
   if (!p || !net || !out) return MPCD_ERR_PARAM;
   *out = nullptr;
-  if (p->n_colloid < 1 || p->n_colloid > MAXC || p->n_sub < 1 || !(p->ndt > 0) || !(p->mass_colloid > 0) ||
+  if (p->n_colloid < 1 || p->n_colloid > MAXC || p->n_sub < 1 || p->n_sub > MAXSUB || !(p->ndt > 0) || !(p->mass_colloid > 0) ||
       !(p->I_colloid > 0) || p->Lx < 1 || p->Ly < 1 || p->Lz < 1)
     return MPCD_ERR_PARAM;
-  if (mlp_io(net).max_batch < p->n_colloid) return MPCD_ERR_CAPACITY;
   mpcd_surrogate *s = new mpcd_surrogate();
   s->net = net;
   Sur &S = s->S;
   memset(&S, 0, sizeof S);
-  const MlpIO io = mlp_io(net);
-  S.On = io.O;
-  S.ymean = io.ymean;
-  S.yistd = io.yistd;
   S.Nc = p->n_colloid;
   S.n_sub = p->n_sub;
   const int Ls[3] = {p->Lx, p->Ly, p->Lz};
@@ -440,23 +941,35 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   S.eps = (float)p->eps;
   S.fc = (float)(4.0 * p->eps * (12.0 * (std::pow(p->sig_colloid, 12) / std::pow(rc, 13)) -
                                  6.0 * (std::pow(p->sig_colloid, 6) / std::pow(rc, 7))));  // cpp/update.cpp:4
-  // the list serves the forces (rc) and the features (three radii); skin 1
-  const double rl = (rc > 3.0 * radius ? rc : 3.0 * radius) + 1.0;
+  // force partners within the cutoff plus a skin of 1 (a colloid moves far less in one
+  // step), features within three radii; one all-pairs scan finds both
+  S.rforce2 = (float)((rc + 1.0) * (rc + 1.0));
+  S.rscan2 = S.rforce2 > S.ct_feat2 ? S.rforce2 : S.ct_feat2;
+  // candidate lists: within that distance plus a skin of 1, rebuilt once a colloid has
+  // moved half the skin
+  const double rl = std::sqrt((double)S.rscan2) + 1.0;
   S.rlist2 = (float)(rl * rl);
   S.half_skin2 = 0.25f;
-  S.rforce2 = (float)((rc + 1.0) * (rc + 1.0));
   S.key = make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32));
   const size_t Nc = S.Nc;
   S.step = salloc<long long>(s, 1);
   S.X = salloc<float4>(s, Nc); S.V = salloc<float4>(s, Nc); S.W = salloc<float4>(s, Nc);
   S.ra = salloc<float4>(s, Nc); S.f = salloc<float4>(s, Nc);
-  S.feat = salloc<float>(s, Nc * NF); S.out = salloc<float>(s, Nc * NO);
-  S.nbr = salloc<int>(s, Nc * MAXNB); S.nnb = salloc<int>(s, Nc);
-  S.xref = salloc<float4>(s, Nc); S.built = salloc<int>(s, 1);
+  S.feat = salloc<float>(s, Nc * NF); S.out = salloc<float>(s, Nc * OUTP);
+  S.imp = salloc<float4>(s, 2 * Nc);
+  S.nbl = salloc<uint16_t>(s, Nc * CAND); S.nbn = salloc<int>(s, Nc);
+  S.xref = salloc<float4>(s, Nc); S.rebuild = salloc<int>(s, 1);
+  if (S.rebuild) cudaMemset(S.rebuild, 1, sizeof(int));  // no candidate lists yet
+  S.fpart = salloc<uint16_t>(s, Nc * MAXF); S.fpn = salloc<uint8_t>(s, Nc);
   S.err = salloc<int>(s, 1);
+  s->wpk = salloc<uint4>(s, PACK_U4);
+  S.wpk = s->wpk;
+  s->outd = salloc<float>(s, Nc * NO);
   if (!s->err.empty() || cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaFuncSetAttribute(k_sur_md<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess ||
-      cudaFuncSetAttribute(k_sur_md<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess) {
+      cudaFuncSetAttribute(k_sur_net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMdSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMdSmem) != cudaSuccess ||
+      pack_weights(s) != MPCD_OK) {
     mpcd_surrogate_destroy(s);
     return MPCD_ERR_NOMEM;
   }
@@ -496,7 +1009,7 @@ extern "C" int mpcd_surrogate_set_state(mpcd_surrogate *s, const double *pos, co
   }
   k_sur_forces<<<(S.Nc + 127) / 128, 128, 0, s->stream>>>(S);
   k_sur_features<<<(S.Nc + 3) / 4, 128, 0, s->stream>>>(S);
-  if (cudaMemsetAsync(S.built, 0, sizeof(int), s->stream) != cudaSuccess) return sfail(s, MPCD_ERR_CUDA, "set-up");
+  if (cudaMemsetAsync(S.rebuild, 1, sizeof(int), s->stream) != cudaSuccess) return sfail(s, MPCD_ERR_CUDA, "set-up");
   return cudaStreamSynchronize(s->stream) == cudaSuccess ? MPCD_OK : sfail(s, MPCD_ERR_CUDA, "set-up forces");
 }
 
@@ -535,8 +1048,20 @@ extern "C" int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recomp
   return MPCD_OK;
 }
 
+// the network's outputs of the last step in physical units (n_colloid x 12, host)
+extern "C" int mpcd_surrogate_outputs(mpcd_surrogate *s, float *out) {
+  if (!s || !out) return MPCD_ERR_PARAM;
+  const Sur &S = s->S;
+  k_sur_denorm<<<(S.Nc * NO + 255) / 256, 256, 0, s->stream>>>(S, s->outd);
+  if (cudaMemcpyAsync(out, s->outd, sizeof(float) * NO * S.Nc, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+      cudaStreamSynchronize(s->stream) != cudaSuccess)
+    return sfail(s, MPCD_ERR_CUDA, "outputs");
+  return MPCD_OK;
+}
+
 extern "C" int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps) {
   if (!s || nsteps < 0) return MPCD_ERR_PARAM;
+  if (nsteps > 0 && pack_weights(s) != MPCD_OK) return MPCD_ERR_CUDA;
   if (!s->exec) {
     cudaGraph_t g;
     if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
@@ -556,6 +1081,7 @@ extern "C" int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps) {
       cudaStreamSynchronize(s->stream) != cudaSuccess)
     return sfail(s, MPCD_ERR_CUDA, std::string("step: ") + cudaGetErrorString(cudaGetLastError()));
   if (bits) return sfail(s, MPCD_ERR_CAPACITY, "a colloid has more neighbours than its lists hold (64 within three "
-                                             "radii plus the skin, 24 within the force cutoff plus the skin)");
+                                             "radii or the force cutoff plus the skin, 24 within the force cutoff "
+                                             "plus the skin)");
   return MPCD_OK;
 }

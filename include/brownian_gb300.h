@@ -250,12 +250,14 @@ int mpcd_mlp_grad(mpcd_mlp *n, const float *x, const float *y, int rows, float *
 int mpcd_mlp_train_step(mpcd_mlp *n, const float *x, const float *y, int rows, float lr, double *loss_host);
 
 /* ---- colloid-only dynamics with the learned closure (no counterpart in the reference) -- */
-/* The colloids of p (box, n_colloid <= MPCD_SURROGATE_MAX_COLLOIDS, n_sub, ndt, masses, WCA
+/* The colloids of p (box, n_colloid <= MPCD_SURROGATE_MAX_COLLOIDS, n_sub <= 32, ndt, masses, WCA
  * sig_colloid/eps, sphere diameter sigma, v0, Dr, seed; n_fluid ignored) without the fluid:
- * each MPCD step the network `net` (max_batch >= n_colloid; borrowed, not owned) predicts
- * every colloid's fluid exchange, a Gaussian draw of it is applied as an impulse together with
- * run()'s active kick, then n_sub velocity-Verlet substeps with WCA forces and the orientation
- * update, in FP32 (one CUDA graph per step). */
+ * each MPCD step the network `net` (borrowed, not owned; its weights are read at every
+ * mpcd_surrogate_step call) predicts every colloid's fluid exchange, a Gaussian draw of it is
+ * applied as an impulse together with run()'s active kick, then n_sub velocity-Verlet substeps
+ * with WCA forces and the orientation update, in FP32.  One CUDA graph of two kernels per
+ * step: the features and the whole network in one kernel over the GPU (16 colloids per
+ * block), the substeps in one block. */
 #define MPCD_SURROGATE_MAX_COLLOIDS 2048
 typedef struct mpcd_surrogate mpcd_surrogate;
 int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_surrogate **out);
@@ -265,9 +267,12 @@ const char *mpcd_surrogate_last_error(const mpcd_surrogate *s);
 int mpcd_surrogate_set_state(mpcd_surrogate *s, const double *pos, const double *vel, const double *ang_vel,
                              const double *ra);
 int mpcd_surrogate_get_state(mpcd_surrogate *s, double *pos, double *vel, double *ang_vel, double *ra);
-/* the network inputs of the current state (n_colloid x 81 floats, host): computed afresh
- * (recompute != 0) or as the last step left them for the next one */
+/* network inputs (n_colloid x 81 floats, host): those of the current state (recompute != 0),
+ * or those the last step fed the network (recompute = 0: the state before that step) */
 int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recompute);
+/* the network's outputs of the last step in physical units (n_colloid x 12 floats, host; the
+ * arithmetic of mpcd_mlp_forward on the last step's inputs) */
+int mpcd_surrogate_outputs(mpcd_surrogate *s, float *out);
 /* nsteps MPCD steps; synchronises */
 int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps);
 

@@ -1,5 +1,7 @@
-"""Colloid-only dynamics with the closure: the GPU feature kernel gives the
-network inputs of brownian_gb300.closure.features, and the step runs."""
+"""Colloid-only dynamics with the closure: the GPU feature kernels give the
+network inputs of brownian_gb300.closure.features, the network inside the step
+gives the outputs of mpcd_mlp_forward on the same inputs bit for bit, and the
+step runs."""
 import numpy as np
 import pytest
 
@@ -52,7 +54,9 @@ def test_surrogate_steps_stay_finite_and_move():
     sur = closure.Surrogate(_params(L, nc), net)
     pos, vel, w, ra = _state(L, nc, 2)
     sur.set_state(pos, vel, w, ra)
-    sur.step(50)
+    sur.step(49)
+    before = sur.features(recompute=True)
+    sur.step(1)
     st = sur.get_state()
     for k, v in st.items():
         assert np.all(np.isfinite(v)), k
@@ -60,9 +64,35 @@ def test_surrogate_steps_stay_finite_and_move():
     d = st["pos_colloid"] - pos
     d -= L * np.round(d / L)
     assert np.mean(np.linalg.norm(d, axis=1)) > 0.05
-    # the inputs the step left for the next one are the features of the new state
+    # the inputs the last step fed its network are the features of the state before it
     fused = sur.features(recompute=False)
-    fresh = sur.features(recompute=True)
-    assert np.allclose(fused, fresh, atol=2e-5), np.max(np.abs(fused - fresh))
+    assert np.array_equal(fused, before), np.max(np.abs(fused - before))
+    sur.close()
+    net.close()
+
+
+@pytest.mark.parametrize("nc", [150, 700])
+def test_step_network_matches_mlp_forward(nc):
+    import torch
+
+    from brownian_gb300 import closure
+    L = 30 if nc == 150 else 52
+    rng = np.random.default_rng(nc)
+    net = closure.Network(max_batch=1024, seed=4)
+    net.set_params(rng.normal(0, 0.06, net.n_params).astype(np.float32))
+    net.set_normalisation(rng.normal(0, 0.2, 81).astype(np.float32), rng.uniform(0.5, 2, 81).astype(np.float32),
+                          rng.normal(0, 0.1, 6).astype(np.float32), rng.uniform(5, 20, 6).astype(np.float32))
+    sur = closure.Surrogate(_params(L, nc), net)
+    sur.set_state(*_state(L, nc, 5))
+    sur.step(3)
+    x = sur.features(recompute=False)
+    got = sur.outputs()
+    xd = torch.from_numpy(x).cuda()
+    od = torch.empty((nc, 12), dtype=torch.float32, device="cuda")
+    net.forward(xd.data_ptr(), od.data_ptr(), nc)
+    torch.cuda.synchronize()
+    ref = od.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert np.array_equal(got, ref), np.max(np.abs(got - ref))
     sur.close()
     net.close()
