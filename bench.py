@@ -370,6 +370,36 @@ def run_ensemble(nrep, steps, rank):
             "timing": "wall clock around mpcd_ensemble_step(K) (it ends with a device synchronisation)"}
 
 
+def _speed_row(row, p, net, closure, bg, _t):
+    """Time per MPCD step of full MPCD (FP64 and FP32 forms) and of the colloid-only step
+    from the full run's colloid state, into row."""
+    c0 = None
+    for prec, name in ((bg.FP64, "full_fp64"), (bg.FP32C, "full_fp32c")):
+        p.precision = prec
+        full = closure._sim(p)
+        full.initialize(bg.INIT_PHYSICAL)
+        full.setup()
+        full.step(3)
+        t0 = _t.perf_counter()
+        full.step(10)
+        row[name + "_ms"] = (_t.perf_counter() - t0) / 10 * 1e3
+        if c0 is None:
+            c0 = full.get_colloids()
+        full.close()
+    sur = closure.Surrogate(p, net)
+    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    sur.step(5)
+    t0 = _t.perf_counter()
+    sur.step(200)
+    row["surrogate_ms"] = (_t.perf_counter() - t0) / 200 * 1e3
+    sur.close()
+    row["speedup_vs_fp64"] = row["full_fp64_ms"] / row["surrogate_ms"]
+    row["speedup_vs_fp32c"] = row["full_fp32c_ms"] / row["surrogate_ms"]
+    row["colloid_time_per_wall_s"] = {"surrogate": 0.1 / (row["surrogate_ms"] / 1e3),
+                                      "full_fp64": 0.1 / (row["full_fp64_ms"] / 1e3),
+                                      "full_fp32c": 0.1 / (row["full_fp32c_ms"] / 1e3)}
+
+
 def run_closure(samples_steps, deploy_steps):
     """The learned closure: training samples from full MPCD of the 64^3 system with v0 swept
     over [0, 0.1] (500 colloids x 5 activities x samples_steps steps), GPU training, then
@@ -404,43 +434,30 @@ def run_closure(samples_steps, deploy_steps):
     free = closure.free_nll(Y[:cut], Y[cut:])
     L500 = int(round((500 * 4.0 / 3.0 * np.pi * RADIUS ** 3 / 0.1) ** (1.0 / 3.0)))
     res = closure.compare(P(L500, 500, 0.05, 901), net, steps=deploy_steps)
-    # timing at 2000 colloids, volume fraction 0.1
-    L2k = int(round((2000 * 4.0 / 3.0 * np.pi * RADIUS ** 3 / 0.1) ** (1.0 / 3.0)))
-    p2k = P(L2k, 2000, 0.05, 902)
-    full = closure._sim(p2k)
-    full.initialize(bg.INIT_PHYSICAL)
-    full.setup()
-    full.step(3)
-    t0 = _t.perf_counter()
-    full.step(10)
-    t_full2k = (_t.perf_counter() - t0) / 10
-    c0 = full.get_colloids()
-    full.close()
-    net2k = closure.Network(max_batch=2048)
-    net2k.set_params(net.params())
-    net2k.set_normalisation(*net.norm)
-    sur = closure.Surrogate(p2k, net2k)
-    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
-    sur.step(5)
-    t0 = _t.perf_counter()
-    sur.step(100)
-    t_sur2k = (_t.perf_counter() - t0) / 100
-    sur.close()
-    net2k.close()
+    # colloid time per wall-second across the deployment range (500 and 2000 colloids,
+    # volume fraction 0.05-0.2): full MPCD, the plain FP64 form and the FP32 form, against
+    # the colloid-only step started from the full run's colloid state
+    table = []
+    for i, (nc, phi) in enumerate(((500, 0.1), (500, 0.05), (2000, 0.2), (2000, 0.1), (2000, 0.05))):
+        Lr = int(round((nc * 4.0 / 3.0 * np.pi * RADIUS ** 3 / phi) ** (1.0 / 3.0)))
+        row = {"colloids": nc, "volume_fraction": phi, "L": Lr, "fluid_particles": Lr ** 3 * DENSITY}
+        try:
+            _speed_row(row, P(Lr, nc, 0.05, 910 + i), net, closure, bg, _t)
+        except Exception as e:  # a row that fails is reported, the others still run
+            row["error"] = str(e)
+        table.append(row)
     net.close()
-    ndt = 0.1
     return {"workload": "closure trained on 64^3 / 500 colloids, v0 in {0, .025, .05, .075, .1}; deployed on "
                         f"{L500}^3 / 500 colloids (volume fraction 0.1, v0 = 0.05) against full MPCD",
             "samples": int(X.shape[0]), "data_s": t_data, "train_s": t_train, "epochs": len(losses),
             "train_loss_first_last": [losses[0], losses[-1]],
             "heldout_nll": held, "heldout_nll_without_network": free,
-            "colloid_time_per_wall_s": {"surrogate_500": ndt / (res["t_surrogate_ms"] / 1e3),
-                                        "full_500": ndt / (res["t_full_ms"] / 1e3),
-                                        "surrogate_2000": ndt / t_sur2k, "full_2000": ndt / t_full2k},
-            "speedup_500": res["speedup"], "speedup_2000": t_full2k / t_sur2k,
+            "speed": table,
+            "speedup_500_vs_fp32c_in_comparison_run": res["speedup"],
             "deploy_steps": deploy_steps, "lags": res["lags"], "rel_diff_vs_full": res["rel_diff_vs_full"],
             "stats": res["stats"],
-            "timing": "wall clock around step calls (each ends with a synchronisation)"}
+            "timing": "wall clock around step calls (each ends with a synchronisation); full MPCD 10 steps after 3, "
+                      "the colloid-only step 200 after 5"}
 
 
 def run_ours(args, rank, world, dist):

@@ -14,12 +14,13 @@
 //     streamed through a ring of shared-memory stages by cp.async while the block
 //     computes), the Gaussian draw of the exchange and the step's
 //     rotational-diffusion draws;
-//   k_sur_md, one block: the active kick and the n_sub substeps (each needs every
-//     colloid's new position, and a block barrier is the cheapest wait at these
-//     sizes).
+//   k_sur_md, one cluster of 8 blocks: the active kick and the n_sub substeps (each
+//     needs every colloid's new position: distributed shared memory and one cluster
+//     barrier per substep).
 // The packed weights (the layout k_sur_net reads) are rebuilt from the network at
 // every mpcd_surrogate_step call.  k_sur_features computes the inputs of the
 // current state on request.
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -149,9 +150,10 @@ __global__ void __launch_bounds__(128) k_sur_features(const Sur S) {
 // 8 t + (l >> 2)), so that a warp's fragments are one conflict-free 16-byte shared
 // load each.  Chunks 0-2: layer 1 (K 96), 3-10: layer 2, 11-18: layer 3 (32 K rows
 // x 256 columns, 16 KB each), 19: layer 4 (K 256 x 16 columns, 8 KB).
-constexpr int ROWS = 16, NCW = 8, NET_THREADS = 32 * (NCW + 1), CHUNK_U4 = 1024, NCHUNK = 20, NSTAGE = 6,
+constexpr int ROWS = 16, NCW = 16, TPW = 32 / NCW, NET_THREADS = 32 * (NCW + 1), CHUNK_U4 = 1024, NCHUNK = 20, NSTAGE = 6,
               LDA = H + 8;
 constexpr int PACK_U4 = 19 * CHUNK_U4 + 512;
+static_assert(ROWS == NCW, "one row per compute warp");
 
 constexpr int MAXSUB = 32;  // substeps per MPCD step the colloid-only step supports
 
@@ -163,11 +165,10 @@ struct __align__(128) NetSmem {
       float4 cx[ROWS][CAND], cv[ROWS][CAND];  // the candidates' positions and velocities
     } c;
   } u;
-  float4 nz[ROWS][MAXSUB];   // rotational-diffusion Gaussians of the step's substeps
-  float4 sc1[ROWS][MAXSUB];  // sin, cos of the Euler angles Omega dt (x, y) per substep
-  float2 sc2[ROWS][MAXSUB];  // (z)
+  float4 nz[ROWS][MAXSUB];     // rotational-diffusion Gaussians of the step's substeps
+  float4 rm[ROWS][MAXSUB][3];  // the Euler matrix of Omega dt per substep (rows)
   float4 row[4][ROWS];       // the rows' X, V, Omega, ra at the step's start
-  float4 pa[ROWS];           // per-substep angular impulse of the drawn exchange
+  float dp[ROWS][NO / 2];    // the drawn exchange (momentum, angular momentum)
   bf16 act[2][ROWS][LDA];
   float cd[ROWS][CAND];      // candidates within the scan distance: squared distance,
   int ck[ROWS][CAND];        // colloid,
@@ -268,11 +269,16 @@ __device__ __forceinline__ void issue_chunk(const Sur &S, NetSmem &sm, int g) {
 __device__ __forceinline__ bool chunk_ready(const Sur &S, NetSmem &sm, int g) {
   int ok = 0;
   if ((threadIdx.x & 31) == 0) {
-    volatile int *ab = &sm.abort;
-    ok = !*ab && mbar_wait_bounded(&sm.full[g % NSTAGE], (uint32_t)((g / NSTAGE) & 1));
-    if (!ok && !*ab) {
-      atomicOr(S.err, 4);
-      *ab = 1;
+    unsigned long long *bar = &sm.full[g % NSTAGE];
+    const uint32_t parity = (uint32_t)((g / NSTAGE) & 1);
+    ok = mbar_try_wait(bar, parity);
+    if (!ok) {
+      volatile int *ab = &sm.abort;
+      ok = !*ab && mbar_wait_bounded(bar, parity);
+      if (!ok && !*ab) {
+        atomicOr(S.err, 4);
+        *ab = 1;
+      }
     }
   }
   return __shfl_sync(0xFFFFFFFFu, ok, 0) != 0;
@@ -362,6 +368,14 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     sm.ym[tid] = S.ymean[tid];
     sm.ys[tid] = S.yistd[tid];
   }
+  // the lists (read on every step, so that no load waits for the flag; a rebuild replaces them)
+  static_assert(ROWS * CAND / 8 <= NET_THREADS, "one 16-byte piece of the lists per thread");
+  if (tid < ROWS * CAND / 8) {
+    const int r = tid / (CAND / 8), qv = tid % (CAND / 8), j = j0 + r;
+    if (j < S.Nc)
+      reinterpret_cast<uint4 *>(sm.lst[r])[qv] = reinterpret_cast<const uint4 *>(S.nbl + (size_t)j * CAND)[qv];
+  }
+  if (tid < ROWS) sm.lstn[tid] = j0 + tid < S.Nc ? S.nbn[j0 + tid] : 0;
   if (rebuild) {
     for (int i0 = tid; i0 < S.Nc; i0 += 8 * NET_THREADS) {  // eight loads in flight per thread
       float4 v[8];
@@ -372,24 +386,12 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
       for (int u = 0; u < 8; ++u)
         if (i0 + u * NET_THREADS < S.Nc) sm.u.xall[i0 + u * NET_THREADS] = v[u];
     }
-  } else {
-    static_assert(ROWS * CAND / 8 <= NET_THREADS, "one 16-byte piece of the lists per thread");
-    if (tid < ROWS * CAND / 8) {
-      const int r = tid / (CAND / 8), qv = tid % (CAND / 8), j = j0 + r;
-      if (j < S.Nc)
-        reinterpret_cast<uint4 *>(sm.lst[r])[qv] = reinterpret_cast<const uint4 *>(S.nbl + (size_t)j * CAND)[qv];
-    }
-    if (tid < ROWS) sm.lstn[tid] = j0 + tid < S.Nc ? S.nbn[j0 + tid] : 0;
   }
   __syncthreads();
   if (rebuild) {
-    // all pairs: colloids within the list distance, ascending index
-    for (int c = 0; c < ROWS / NCW && !producer; ++c) {
-      const int r = (ROWS / NCW) * warp + c, j = j0 + r;
-      if (j >= S.Nc) {
-        if (lane == 0) sm.lstn[r] = 0;
-        continue;
-      }
+    // all pairs: colloids within the list distance, ascending index (compute warp w: row w)
+    const int r = warp, j = j0 + r;
+    if (!producer && j < S.Nc) {
       const float4 xj = sm.row[0][r];
       int nl = 0;
       for (int k0 = 0; k0 < S.Nc; k0 += 32) {
@@ -418,6 +420,8 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
         S.xref[j] = xj;
         if (nl > CAND) atomicOr(S.err, 1);
       }
+    } else if (!producer && lane == 0) {
+      sm.lstn[r] = 0;
     }
     __syncthreads();  // (the candidates' positions below overwrite xall)
   }
@@ -444,12 +448,12 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     }
   }
   __syncthreads();
-  for (int c = 0; c < ROWS / NCW && !producer; ++c) {
-    const int r = (ROWS / NCW) * warp + c, j = j0 + r;
+  if (!producer) {  // compute warp w: row w
+    const int r = warp, j = j0 + r;
     float *o = sm.feat[r];
     for (int col = lane; col < NF; col += 32) o[col] = 0.f;
     __syncwarp();
-    if (j >= S.Nc) continue;
+    if (j < S.Nc) {
     const float4 xj = sm.row[0][r], vj = sm.row[1][r];
     // neighbours within the scan distance, ascending index
     const int nlst = sm.lstn[r];
@@ -524,6 +528,7 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
       S.fpn[j] = (uint8_t)min(m, MAXF);
       if (m > MAXF) atomicOr(S.err, 2);
     }
+    }
   }
   // the step's draws: rotational diffusion per substep, the exchange's six Gaussians
   for (int i = tid; i < ROWS * (S.n_sub + 1); i += NET_THREADS) {
@@ -576,38 +581,54 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
         mbar_wait_bounded(&sm.full[c % NSTAGE], (uint32_t)((c / NSTAGE) & 1));
     }
   } else {
-    // three hidden layers: compute warp w takes columns 32 w .. 32 w + 31
+    // three hidden layers: compute warp w takes columns 8 TPW w .. 8 TPW (w + 1) - 1, two
+    // weight chunks per wait
     int g = 0;
 #pragma unroll 1
     for (int layer = 0; layer < 3; ++layer) {
       const bf16(*A)[LDA] = sm.act[layer & 1];
       bf16(*Z)[LDA] = sm.act[(layer + 1) & 1];
       const int nch = layer == 0 ? INP / 32 : H / 32;
-      float acc[4][4];
+      float acc[TPW][4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t)
+      for (int t = 0; t < TPW; ++t)
 #pragma unroll
         for (int e = 0; e < 4; ++e) acc[t][e] = 0.f;
 #pragma unroll 1
-      for (int c = 0; c < nch; ++c, ++g) {
-        const bool ok = chunk_ready(S, sm, g);
-        const uint4 *B = sm.ring[g % NSTAGE];
-        uint4 b[4];
+      for (int c = 0; c < nch; c += 2) {
+        const bool two = c + 1 < nch;
+        const bool ok0 = chunk_ready(S, sm, g), ok1 = two ? chunk_ready(S, sm, g + 1) : true;
+        const uint4 *B0 = sm.ring[g % NSTAGE], *B1 = sm.ring[(g + 1) % NSTAGE];
+        uint4 b0[TPW], b1[TPW];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) b[t] = B[(4 * warp + t) * 32 + lane];
+        for (int t = 0; t < TPW; ++t) b0[t] = B0[(TPW * warp + t) * 32 + lane];
+        if (two) {
+#pragma unroll
+          for (int t = 0; t < TPW; ++t) b1[t] = B1[(TPW * warp + t) * 32 + lane];
+        }
         uint32_t a[4];
         a_frag(A, 32 * c, gq, q, a);
 #pragma unroll
-        for (int t = 0; t < 4; ++t) mma_bf16(acc[t], a, b[t].x, b[t].y);
+        for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b0[t].x, b0[t].y);
         a_frag(A, 32 * c + 16, gq, q, a);
 #pragma unroll
-        for (int t = 0; t < 4; ++t) mma_bf16(acc[t], a, b[t].z, b[t].w);
-        chunk_release(sm, g, ok);
+        for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b0[t].z, b0[t].w);
+        if (two) {
+          a_frag(A, 32 * c + 32, gq, q, a);
+#pragma unroll
+          for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b1[t].x, b1[t].y);
+          a_frag(A, 32 * c + 48, gq, q, a);
+#pragma unroll
+          for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b1[t].z, b1[t].w);
+        }
+        chunk_release(sm, g, ok0);
+        if (two) chunk_release(sm, g + 1, ok1);
+        g += two ? 2 : 1;
       }
       const float *bias = sm.bias + H * layer;
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int n0 = 8 * (4 * warp + t) + 2 * q;
+      for (int t = 0; t < TPW; ++t) {
+        const int n0 = 8 * (TPW * warp + t) + 2 * q;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           float v0 = acc[t][2 * h] + bias[n0], v1 = acc[t][2 * h + 1] + bias[n0 + 1];
@@ -650,57 +671,50 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     const int r = i / OUTP, j = j0 + r;
     if (j < S.Nc) S.out[(size_t)j * OUTP + i % OUTP] = sm.out[r][i % OUTP];
   }
-  if (tid < ROWS && j0 + tid < S.Nc) {
-    const int r = tid, j = j0 + r;
-    // the exchange: the network's normalised outputs -> mean and standard deviation in
-    // physical units, the Gaussian draw, spread in equal parts over the substeps (the
-    // fluid collides every substep)
+  // the exchange, one (row, component) per thread: the network's normalised outputs ->
+  // mean and standard deviation in physical units, and the Gaussian draw
+  if (tid < ROWS * (NO / 2)) {
+    const int r = tid / (NO / 2), k = tid % (NO / 2);
     const float *o = sm.out[r];
-    float dp[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const float is = sm.ys[k];
-      const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
-      dp[k] = (o[k] + __expf(0.5f * lv) * sm.xi[r][k]) / is + sm.ym[k];
-    }
-    const float fm = 1.f / (S.M * S.n_sub), fi = 1.f / (S.I * S.n_sub);
-    sm.pa[r] = make_float4(dp[3] * fi, dp[4] * fi, dp[5] * fi, 0.f);
-    S.imp[j] = make_float4(dp[0] * fm, dp[1] * fm, dp[2] * fm, 0.f);
-    S.imp[S.Nc + j] = sm.row[3][r];  // the orientation run()'s kick uses
+    const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
+    sm.dp[r][k] = (o[k] + __expf(0.5f * lv) * sm.xi[r][k]) / sm.ys[k] + sm.ym[k];
   }
   __syncthreads();
-  // per (row, substep): Omega after the substep's share of the angular exchange (the
-  // same sequence of additions as the substeps make) and the sines and cosines of
-  // its Euler angles, all substeps at once
+  // per (row, substep): Omega after the substep's share of the angular exchange (spread
+  // in equal parts over the substeps: the fluid collides every substep; the same
+  // sequence of additions as the substeps make) and the Euler matrix of Omega dt
+  const float fm = 1.f / (S.M * S.n_sub), fi = 1.f / (S.I * S.n_sub);
   for (int i = tid; i < ROWS * S.n_sub; i += NET_THREADS) {
-    const int r = i % ROWS, l = i / ROWS;
-    if (j0 + r >= S.Nc) continue;
+    const int r = i % ROWS, l = i / ROWS, j = j0 + r;
+    if (j >= S.Nc) continue;
+    if (l == 0) {
+      S.imp[j] = make_float4(sm.dp[r][0] * fm, sm.dp[r][1] * fm, sm.dp[r][2] * fm, 0.f);
+      S.imp[S.Nc + j] = sm.row[3][r];  // the orientation run()'s kick uses
+    }
+    const float pax = sm.dp[r][3] * fi, pay = sm.dp[r][4] * fi, paz = sm.dp[r][5] * fi;
     float4 w = sm.row[2][r];
-    const float4 pa = sm.pa[r];
     for (int s = 0; s <= l; ++s) {
-      w.x += pa.x; w.y += pa.y; w.z += pa.z;
+      w.x += pax; w.y += pay; w.z += paz;
     }
     float sx, cx, sy, cy, sz, cz;
     __sincosf(w.x * S.dt, &sx, &cx); __sincosf(w.y * S.dt, &sy, &cy); __sincosf(w.z * S.dt, &sz, &cz);
-    sm.sc1[r][l] = make_float4(sx, cx, sy, cy);
-    sm.sc2[r][l] = make_float2(sz, cz);
+    sm.rm[r][l][0] = make_float4(cy * cz, -(cy * sz), sy, 0.f);
+    sm.rm[r][l][1] = make_float4(sx * sy * cz + cx * sz, -sx * sy * sz + cx * cz, -(sx * cy), 0.f);
+    sm.rm[r][l][2] = make_float4(-cx * sy * cz + sx * sz, cx * sy * sz + sx * cz, cx * cy, 0.f);
   }
   __syncthreads();
-  // the orientation through the substeps: the Euler matrix of Omega dt, then the
-  // rotational diffusion (update_activity_direction plus Dr)
+  // the orientation through the substeps: the Euler rotation, then the rotational
+  // diffusion (update_activity_direction plus Dr)
   if (tid < ROWS && j0 + tid < S.Nc) {
     const int r = tid, j = j0 + r;
+    const float pax = sm.dp[r][3] * fi, pay = sm.dp[r][4] * fi, paz = sm.dp[r][5] * fi;
     float4 w = sm.row[2][r], a = sm.row[3][r];
-    const float4 pa = sm.pa[r];
     for (int l = 0; l < S.n_sub; ++l) {
-      w.x += pa.x; w.y += pa.y; w.z += pa.z;
-      const float4 s1 = sm.sc1[r][l];
-      const float2 s2 = sm.sc2[r][l];
-      const float sx = s1.x, cx = s1.y, sy = s1.z, cy = s1.w, sz = s2.x, cz = s2.y;
-      const float4 aa = a;
-      float ax = cy * cz * aa.x - cy * sz * aa.y + sy * aa.z;
-      float ay = (sx * sy * cz + cx * sz) * aa.x + (-sx * sy * sz + cx * cz) * aa.y - sx * cy * aa.z;
-      float az = (-cx * sy * cz + sx * sz) * aa.x + (cx * sy * sz + sx * cz) * aa.y + cx * cy * aa.z;
+      w.x += pax; w.y += pay; w.z += paz;
+      const float4 m0 = sm.rm[r][l][0], m1 = sm.rm[r][l][1], m2 = sm.rm[r][l][2];
+      float ax = m0.x * a.x + m0.y * a.y + m0.z * a.z;
+      float ay = m1.x * a.x + m1.y * a.y + m1.z * a.z;
+      float az = m2.x * a.x + m2.y * a.y + m2.z * a.z;
       if (S.rotdiff_s > 0.f) {
         const float4 gz = sm.nz[r][l];
         const float d = gz.x * ax + gz.y * ay + gz.z * az;
@@ -715,28 +729,51 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
 }
 
 // ---- the substeps ---------------------------------------------------------------
+// the force-shifted WCA pair force (cpp/update.cpp:14-32) in FP32, branch free: 1/r by
+// the fast reciprocal square root, 1/r^6 from 1/r^2
 __device__ __forceinline__ float3 wca_pair(const Sur &S, float dx, float dy, float dz) {
   const float r2 = dx * dx + dy * dy + dz * dz;
-  if (!(r2 < S.rc2)) return make_float3(0.f, 0.f, 0.f);
-  const float r = sqrtf(r2), ir = 1.f / r, ir6 = 1.f / (r2 * r2 * r2);
+  const float ir = rsqrtf(r2), ir2 = ir * ir, ir6 = ir2 * ir2 * ir2;
   const float mag = 4.f * S.eps * (12.f * S.sig12 * ir6 * ir6 * ir - 6.f * S.sig6 * ir6 * ir) - S.fc;
-  return make_float3(mag * dx * ir, mag * dy * ir, mag * dz * ir);
+  const float f = r2 < S.rc2 ? mag * ir : 0.f;
+  return make_float3(f * dx, f * dy, f * dz);
 }
 
-// One block, one or two colloids per thread (velocity, force and the step's
-// impulse in registers; positions and force partners in shared memory): run()'s
-// kick along the orientation at the step's start, then n_sub substeps of
-// update_pos_md, the substep's share of the exchange, compute_force_md at the new
-// positions and update_velocity_colloid.  At the end: whether a colloid has moved
-// more than half the skin since the candidate lists were built.
-template <int PER>  // colloids per thread: 1 up to 1024 colloids, 2 up to MAXC
-__global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
+// the WCA forces on a colloid at x from its n partners (ids in row, ascending; positions
+// in P), four positions fetched together, summed in partner order
+__device__ __forceinline__ float3 partner_forces(const Sur &S, float4 x, const float4 *P, const uint16_t *row, int n,
+                                                 int self) {
+  float3 fn = make_float3(0.f, 0.f, 0.f);
+  for (int e = 0; e < n; e += 4) {
+    const uint2 kk = *reinterpret_cast<const uint2 *>(row + e);
+    const int k4[4] = {(int)(kk.x & 0xFFFFu), (int)(kk.x >> 16), (int)(kk.y & 0xFFFFu), (int)(kk.y >> 16)};
+    float4 xk[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) xk[i] = P[e + i < n ? k4[i] : self];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (e + i >= n) break;
+      const float3 fp = wca_pair(S, wrapd(x.x - xk[i].x, S.L[0], S.iL[0]), wrapd(x.y - xk[i].y, S.L[1], S.iL[1]),
+                                 wrapd(x.z - xk[i].z, S.L[2], S.iL[2]));
+      fn.x += fp.x; fn.y += fp.y; fn.z += fp.z;
+    }
+  }
+  return fn;
+}
+
+// One block, PER colloids per thread (position, velocity, force and the step's impulse
+// in registers; positions, two copies by substep parity, and force partners in shared
+// memory): run()'s kick along the orientation at the step's start, then n_sub substeps
+// of update_pos_md, the substep's share of the exchange, compute_force_md at the new
+// positions and update_velocity_colloid, one block barrier per substep (the copy a
+// substep writes was last read two substeps before).  At the end: whether a colloid has
+// moved more than half the skin since the candidate lists were built.
+template <int PER>
+__global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
   extern __shared__ float4 smem[];
-  float4 *sX = smem;
-  uint16_t *sF = reinterpret_cast<uint16_t *>(smem + MAXC);      // [MAXC][MAXF] force partners
-  uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MAXC * MAXF);  // [MAXC] their count
+  uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);  // [MAXC][MAXF] force partners
+  uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MAXC * MAXF);   // [MAXC] their count
   const int T = blockDim.x, tid = threadIdx.x;
-  float4 v[PER], fo[PER], pl[PER];
   {
     const uint4 *src = reinterpret_cast<const uint4 *>(S.fpart);
     uint4 *dst = reinterpret_cast<uint4 *>(sF);
@@ -752,27 +789,28 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
     }
     for (int i = tid; i < S.Nc; i += T) sFn[i] = S.fpn[i];
   }
+  float4 x[PER], v[PER], fo[PER], pl[PER];
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
-    sX[j] = S.X[j];
-    v[u] = S.V[j]; fo[u] = S.f[j]; pl[u] = S.imp[j];
+    x[u] = S.X[j]; v[u] = S.V[j]; fo[u] = S.f[j]; pl[u] = S.imp[j];
     const float4 a = S.imp[S.Nc + j];
     v[u].x += S.v0 * a.x; v[u].y += S.v0 * a.y; v[u].z += S.v0 * a.z;
   }
   const float hdt2m = 0.5f * S.dt * S.dt / S.M, hdtm = 0.5f * S.dt / S.M;
   for (int l = 0; l < S.n_sub; ++l) {
-    __syncthreads();
+    float4 *P = (l & 1) ? smem : smem + MAXC;  // this substep's copy
 #pragma unroll
     for (int u = 0; u < PER; ++u) {  // update_pos_md
       const int j = tid + T * u;
       if (j >= S.Nc) continue;
-      float4 x = sX[j];
-      x.x += v[u].x * S.dt + fo[u].x * hdt2m; x.y += v[u].y * S.dt + fo[u].y * hdt2m;
-      x.z += v[u].z * S.dt + fo[u].z * hdt2m;
-      x.x -= S.L[0] * floorf(x.x * S.iL[0]); x.y -= S.L[1] * floorf(x.y * S.iL[1]); x.z -= S.L[2] * floorf(x.z * S.iL[2]);
-      sX[j] = x;
+      float4 &xx = x[u];
+      xx.x += v[u].x * S.dt + fo[u].x * hdt2m; xx.y += v[u].y * S.dt + fo[u].y * hdt2m;
+      xx.z += v[u].z * S.dt + fo[u].z * hdt2m;
+      xx.x -= S.L[0] * floorf(xx.x * S.iL[0]); xx.y -= S.L[1] * floorf(xx.y * S.iL[1]);
+      xx.z -= S.L[2] * floorf(xx.z * S.iL[2]);
+      P[j] = xx;
     }
     __syncthreads();
 #pragma unroll
@@ -782,23 +820,7 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
       // this substep's share of the fluid exchange (fluid_colloid_collision)
       v[u].x += pl[u].x; v[u].y += pl[u].y; v[u].z += pl[u].z;
       // compute_force_md at the new positions, update_velocity_colloid
-      float3 fn = make_float3(0.f, 0.f, 0.f);
-      const float4 xj = sX[j];
-      const int n = sFn[j];
-      for (int e = 0; e < n; e += 4) {  // four partners' positions fetched together, summed in order
-        const uint2 kk = *reinterpret_cast<const uint2 *>(sF + j * MAXF + e);
-        const int k4[4] = {(int)(kk.x & 0xFFFFu), (int)(kk.x >> 16), (int)(kk.y & 0xFFFFu), (int)(kk.y >> 16)};
-        float4 xk[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) xk[i] = sX[e + i < n ? k4[i] : j];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          if (e + i >= n) break;
-          const float3 fp = wca_pair(S, wrapd(xj.x - xk[i].x, S.L[0], S.iL[0]), wrapd(xj.y - xk[i].y, S.L[1], S.iL[1]),
-                                     wrapd(xj.z - xk[i].z, S.L[2], S.iL[2]));
-          fn.x += fp.x; fn.y += fp.y; fn.z += fp.z;
-        }
-      }
+      const float3 fn = partner_forces(S, x[u], P, sF + j * MAXF, sFn[j], j);
       v[u].x += (fo[u].x + fn.x) * hdtm; v[u].y += (fo[u].y + fn.y) * hdtm; v[u].z += (fo[u].z + fn.z) * hdtm;
       fo[u] = make_float4(fn.x, fn.y, fn.z, 0.f);
     }
@@ -808,15 +830,89 @@ __global__ void __launch_bounds__(1024) k_sur_md(const Sur S) {
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
-    const float4 x = sX[j], x0 = S.xref[j];
-    S.X[j] = x; S.V[j] = v[u]; S.f[j] = fo[u];
-    const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
-                dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
+    const float4 x0 = S.xref[j];
+    S.X[j] = x[u]; S.V[j] = v[u]; S.f[j] = fo[u];
+    const float dx = wrapd(x[u].x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x[u].y - x0.y, S.L[1], S.iL[1]),
+                dz = wrapd(x[u].z - x0.z, S.L[2], S.iL[2]);
     moved |= dx * dx + dy * dy + dz * dz > S.half_skin2;
   }
   moved = __syncthreads_or(moved);
   if (tid == 0) {
     *S.rebuild = moved;
+    *S.step += 1;
+  }
+}
+
+// One cluster of MDC blocks, one colloid per thread (block b takes colloids
+// [b per, (b + 1) per)): position, velocity, force and the step's impulse in
+// registers, force partners in shared memory.  run()'s kick along the orientation at
+// the step's start, then n_sub substeps of update_pos_md, the substep's share of the
+// exchange, compute_force_md at the new positions and update_velocity_colloid.  Each
+// substep's new positions go to every block's copy (distributed shared memory, two
+// copies by substep parity), then one cluster barrier: the copy a substep writes was
+// last read two substeps before, behind the barrier in between.  At the end: whether
+// a colloid has moved more than half the skin since the candidate lists were built.
+constexpr int MDC = 8, MD_MAXT = MAXC / MDC;
+
+__global__ void __cluster_dims__(MDC, 1, 1) __launch_bounds__(MD_MAXT) k_sur_md(const Sur S) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ float4 smem[];
+  uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);          // [MD_MAXT][MAXF] force partners
+  uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MD_MAXT * MAXF);       // [MD_MAXT] their count
+  int *sMoved = reinterpret_cast<int *>(sFn + MD_MAXT);                  // [MDC] (block 0)
+  const int tid = threadIdx.x, rank = (int)cl.block_rank();
+  const int per = (S.Nc + MDC - 1) / MDC, j = rank * per + tid;
+  const bool own = tid < per && j < S.Nc;
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f), v = x, fo = x, pl = x;
+  int n = 0;
+  if (own) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(S.fpart + (size_t)j * MAXF);
+    uint4 *dst = reinterpret_cast<uint4 *>(sF + tid * MAXF);
+    const uint4 p0 = src[0], p1 = src[1], p2 = src[2];
+    n = S.fpn[j];
+    x = S.X[j]; v = S.V[j]; fo = S.f[j]; pl = S.imp[j];
+    const float4 a = S.imp[S.Nc + j];
+    dst[0] = p0; dst[1] = p1; dst[2] = p2;
+    v.x += S.v0 * a.x; v.y += S.v0 * a.y; v.z += S.v0 * a.z;
+  }
+  cl.sync();  // every block has started before any writes to its copies
+  const float hdt2m = 0.5f * S.dt * S.dt / S.M, hdtm = 0.5f * S.dt / S.M;
+  for (int l = 0; l < S.n_sub; ++l) {
+    const int nb = (l + 1) & 1;
+    if (own) {  // update_pos_md
+      x.x += v.x * S.dt + fo.x * hdt2m; x.y += v.y * S.dt + fo.y * hdt2m; x.z += v.z * S.dt + fo.z * hdt2m;
+      x.x -= S.L[0] * floorf(x.x * S.iL[0]); x.y -= S.L[1] * floorf(x.y * S.iL[1]); x.z -= S.L[2] * floorf(x.z * S.iL[2]);
+      float4 *mine = (nb ? smem + MAXC : smem) + j;
+#pragma unroll
+      for (int b = 0; b < MDC; ++b) *cl.map_shared_rank(mine, b) = x;
+    }
+    cl.sync();
+    if (own) {
+      const float4 *P = nb ? smem + MAXC : smem;  // positions, by substep parity
+      // this substep's share of the fluid exchange (fluid_colloid_collision)
+      v.x += pl.x; v.y += pl.y; v.z += pl.z;
+      // compute_force_md at the new positions, update_velocity_colloid
+      const float3 fn = partner_forces(S, x, P, sF + tid * MAXF, n, j);
+      v.x += (fo.x + fn.x) * hdtm; v.y += (fo.y + fn.y) * hdtm; v.z += (fo.z + fn.z) * hdtm;
+      fo = make_float4(fn.x, fn.y, fn.z, 0.f);
+    }
+  }
+  int moved = 0;
+  if (own) {
+    const float4 x0 = S.xref[j];
+    S.X[j] = x; S.V[j] = v; S.f[j] = fo;
+    const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
+                dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
+    moved = dx * dx + dy * dy + dz * dz > S.half_skin2;
+  }
+  moved = __syncthreads_or(moved);
+  if (tid == 0) *cl.map_shared_rank(sMoved + rank, 0) = moved;
+  cl.sync();  // (also: no block leaves while another may still write its copies)
+  if (rank == 0 && tid == 0) {
+    int any = 0;
+    for (int b = 0; b < MDC; ++b) any |= sMoved[b];
+    *S.rebuild = any;
     *S.step += 1;
   }
 }
@@ -884,14 +980,21 @@ T *salloc(mpcd_surrogate *s, size_t n) {
   return static_cast<T *>(p);
 }
 
-constexpr size_t kMdSmem = MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16_t) + MAXC;
+constexpr size_t kMd1Smem = 2 * MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16_t) + MAXC;
+constexpr int kMdBlockMax = 1024;  // colloids up to which the substeps run in one block, else in a cluster
+constexpr size_t kMdSmem = 2 * MAXC * sizeof(float4) + MD_MAXT * MAXF * sizeof(uint16_t) + MD_MAXT + MDC * sizeof(int);
 constexpr size_t kNetSmem = sizeof(NetSmem);
 
 int enqueue_step(mpcd_surrogate *s) {
   const Sur &S = s->S;
   k_sur_net<<<(S.Nc + ROWS - 1) / ROWS, NET_THREADS, kNetSmem, s->stream>>>(S);
-  if (S.Nc <= 1024) k_sur_md<1><<<1, (S.Nc + 31) / 32 * 32, kMdSmem, s->stream>>>(S);
-  else k_sur_md<2><<<1, 1024, kMdSmem, s->stream>>>(S);
+  if (S.Nc <= kMdBlockMax) {
+    if (S.Nc <= 1024) k_sur_md1<1><<<1, (S.Nc + 31) / 32 * 32, kMd1Smem, s->stream>>>(S);
+    else k_sur_md1<2><<<1, 1024, kMd1Smem, s->stream>>>(S);
+  } else {
+    const int per = (S.Nc + MDC - 1) / MDC;
+    k_sur_md<<<MDC, (per + 31) / 32 * 32, kMdSmem, s->stream>>>(S);
+  }
   return cudaGetLastError() == cudaSuccess ? MPCD_OK : sfail(s, MPCD_ERR_CUDA, "step launch");
 }
 
@@ -967,8 +1070,9 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   s->outd = salloc<float>(s, Nc * NO);
   if (!s->err.empty() || cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaFuncSetAttribute(k_sur_net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem) != cudaSuccess ||
-      cudaFuncSetAttribute(k_sur_md<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMdSmem) != cudaSuccess ||
-      cudaFuncSetAttribute(k_sur_md<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMdSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMdSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md1<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMd1Smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_sur_md1<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMd1Smem) != cudaSuccess ||
       pack_weights(s) != MPCD_OK) {
     mpcd_surrogate_destroy(s);
     return MPCD_ERR_NOMEM;

@@ -257,7 +257,7 @@ int mpcd_mlp_train_step(mpcd_mlp *n, const float *x, const float *y, int rows, f
  * applied as an impulse together with run()'s active kick, then n_sub velocity-Verlet substeps
  * with WCA forces and the orientation update, in FP32.  One CUDA graph of two kernels per
  * step: the features and the whole network in one kernel over the GPU (16 colloids per
- * block), the substeps in one block. */
+ * block), the substeps in one cluster of 8 blocks. */
 #define MPCD_SURROGATE_MAX_COLLOIDS 2048
 typedef struct mpcd_surrogate mpcd_surrogate;
 int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_surrogate **out);
