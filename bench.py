@@ -455,6 +455,7 @@ def run_closure(samples_steps, deploy_steps):
             "speed": table,
             "speedup_500_vs_fp32c_in_comparison_run": res["speedup"],
             "deploy_steps": deploy_steps, "lags": res["lags"], "rel_diff_vs_full": res["rel_diff_vs_full"],
+            "fast_steps": res["fast_steps"],
             "stats": res["stats"],
             "timing": "wall clock around step calls (each ends with a synchronisation); full MPCD 10 steps after 3, "
                       "the colloid-only step 200 after 5"}

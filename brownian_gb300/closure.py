@@ -256,6 +256,14 @@ class Surrogate:
     def step(self, nsteps=1):
         self._ck(lib().mpcd_surrogate_step(self.h, nsteps))
 
+    def fast_steps(self):
+        """Steps in which some colloid moved more than half the force-partner skin."""
+        f = lib().mpcd_surrogate_fast_steps
+        f.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        c = C.c_int64()
+        self._ck(f(self.h, C.byref(c)))
+        return c.value
+
     def close(self):
         if getattr(self, "h", None):
             lib().mpcd_surrogate_destroy(self.h)
@@ -347,6 +355,7 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     t_sur = (time.perf_counter() - t0) / 100
     sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
     stats["closure"] = device_stats(sur, steps, L, **lag_kw)
+    fast = {"closure": sur.fast_steps()}
     sur.close()
     none_net = Network(max_batch=p.n_colloid)
     none_net.set_normalisation(np.zeros(IN), np.ones(IN), np.zeros(NY), np.full(NY, 1e-20))
@@ -354,10 +363,12 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     bare = Surrogate(p, none_net)
     bare.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
     stats["no_closure"] = device_stats(bare, steps, L, **lag_kw)
+    fast["no_closure"] = bare.fast_steps()
     bare.close()
     none_net.close()
     out = {"t_full_ms": t_full * 1e3, "t_surrogate_ms": t_sur * 1e3, "speedup": t_full / t_sur}
     out["stats"] = stats
+    out["fast_steps"] = fast  # steps in which a colloid outran half its force-partner skin
     out["lags"] = {"msd": list(lags), "vacf": list(vlags), "oacf": list(olags)}
     rel = {}
     for name in ("closure", "no_closure"):

@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -42,13 +43,16 @@ typedef __nv_bfloat16 bf16;
 constexpr int NF = MPCD_MLP_IN, NO = MPCD_MLP_OUT, KNEAR = 12, MAXC = MPCD_SURROGATE_MAX_COLLOIDS, CAND = 64;
 constexpr int H = MPCD_MLP_HIDDEN, INP = MLP_IN_PADDED, OUTP = MLP_OUT_PADDED;
 constexpr uint32_t DOM_SUR_KICK = 20, DOM_SUR_ROT = 21;
-constexpr int MAXF = 24;  // force partners per colloid (within the WCA cutoff plus the skin)
+constexpr int MAXF = 32;  // force partners per colloid (within the WCA cutoff plus the skin)
 
 struct Sur {
   int Nc, n_sub;
   float L[3], iL[3];
   float M, I, dt, v0, rotdiff_s, ct_feat2;
-  float sig6, sig12, eps, rc2, fc, rforce2, rscan2, rlist2, half_skin2;
+  float sig6, sig12, eps, rc2, fc, rscan2, rlist2, half_skin2;
+  float rc;          // WCA cutoff
+  float *vmax;       // the largest colloid speed at the end of the last step
+  long long *fast;   // steps in which a colloid moved more than half the step's partner skin
   uint2 key;
   long long *step;  // device step counter
   float4 *X, *V, *W, *ra, *f;
@@ -69,6 +73,14 @@ struct Sur {
 };
 
 __device__ __forceinline__ float wrapd(float d, float L, float iL) { return d - L * rintf(d * iL); }
+
+// the skin of a step's force partners (pairs within the cutoff plus it): 2.5 times the
+// largest displacement the last step's speeds give, within [0.5, 2]; the candidate lists
+// cover the largest
+__device__ __forceinline__ float partner_skin(const Sur &S) {
+  return fminf(fmaxf(2.5f * *S.vmax * S.dt * S.n_sub, 0.5f), 2.0f);
+}
+
 
 __device__ __forceinline__ float u01f(uint32_t w) { return ((float)(w >> 9) + 0.5f) * 1.1920928955078125e-7f; }
 
@@ -301,12 +313,17 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// the A fragment of K step kk (16 rows of the activations)
+// the A fragment of K step kk (16 rows of the activations), one ldmatrix.x4: lane l
+// gives the address of row l % 16 at column kk + 8 (l / 16)
 __device__ __forceinline__ void a_frag(const bf16 (*A)[LDA], int kk, int gq, int q, uint32_t a[4]) {
-  a[0] = *reinterpret_cast<const uint32_t *>(&A[gq][kk + 2 * q]);
-  a[1] = *reinterpret_cast<const uint32_t *>(&A[gq + 8][kk + 2 * q]);
-  a[2] = *reinterpret_cast<const uint32_t *>(&A[gq][kk + 2 * q + 8]);
-  a[3] = *reinterpret_cast<const uint32_t *>(&A[gq + 8][kk + 2 * q + 8]);
+  (void)gq;
+  (void)q;
+  const int lane = threadIdx.x & 31;
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(&A[lane & 15][kk + 8 * (lane >> 4)]);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+               : "r"(addr)
+               : "memory");
 }
 
 __device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }  // as mlp.cu
@@ -315,7 +332,7 @@ __device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __
 // neighbour and feature phases, 32 columns each in the network) and one producer
 // warp that streams the weights.
 //   neighbours within max(three radii, the force cutoff plus the skin): from each
-//   colloid's candidate list (colloids within that distance plus a skin of 1 at the
+//   colloid's candidate list (colloids within that distance plus a skin of 2 at the
 //   last rebuild, ascending index), or, when k_sur_md has flagged that a colloid
 //   moved more than half the skin since then, from all pairs (and the lists rebuilt);
 //   the features (V, Omega, ra, then the 12 nearest within three radii, nearest first,
@@ -339,6 +356,7 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
   const int j0 = blockIdx.x * ROWS;
   const uint32_t step = (uint32_t)*S.step;
   const bool producer = warp == NCW;
+  const float rfp = S.rc + partner_skin(S), rforce2 = rfp * rfp;
   if (tid == NCW * 32) {
     for (int s = 0; s < NSTAGE; ++s) {
       mbar_init(&sm.full[s], 1);
@@ -516,7 +534,7 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     int m = 0;
     for (int e0 = 0; e0 < n; e0 += 32) {
       const int e = e0 + lane;
-      const bool in = e < n && sm.cd[r][e] < S.rforce2;
+      const bool in = e < n && sm.cd[r][e] < rforce2;
       const unsigned b = __ballot_sync(0xFFFFFFFFu, in);
       if (in) {
         const int slot = m + __popc(b & lt);
@@ -709,9 +727,13 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     const int r = tid, j = j0 + r;
     const float pax = sm.dp[r][3] * fi, pay = sm.dp[r][4] * fi, paz = sm.dp[r][5] * fi;
     float4 w = sm.row[2][r], a = sm.row[3][r];
+    float4 n0 = sm.rm[r][0][0], n1 = sm.rm[r][0][1], n2 = sm.rm[r][0][2];
     for (int l = 0; l < S.n_sub; ++l) {
       w.x += pax; w.y += pay; w.z += paz;
-      const float4 m0 = sm.rm[r][l][0], m1 = sm.rm[r][l][1], m2 = sm.rm[r][l][2];
+      const float4 m0 = n0, m1 = n1, m2 = n2;
+      if (l + 1 < S.n_sub) {  // the next substep's matrix, in flight meanwhile
+        n0 = sm.rm[r][l + 1][0]; n1 = sm.rm[r][l + 1][1]; n2 = sm.rm[r][l + 1][2];
+      }
       float ax = m0.x * a.x + m0.y * a.y + m0.z * a.z;
       float ay = m1.x * a.x + m1.y * a.y + m1.z * a.z;
       float az = m2.x * a.x + m2.y * a.y + m2.z * a.z;
@@ -729,18 +751,17 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
 }
 
 // ---- the substeps ---------------------------------------------------------------
-// the force-shifted WCA pair force (cpp/update.cpp:14-32) in FP32, branch free: 1/r by
-// the fast reciprocal square root, 1/r^6 from 1/r^2
-__device__ __forceinline__ float3 wca_pair(const Sur &S, float dx, float dy, float dz) {
-  const float r2 = dx * dx + dy * dy + dz * dz;
-  const float ir = rsqrtf(r2), ir2 = ir * ir, ir6 = ir2 * ir2 * ir2;
-  const float mag = 4.f * S.eps * (12.f * S.sig12 * ir6 * ir6 * ir - 6.f * S.sig6 * ir6 * ir) - S.fc;
-  const float f = r2 < S.rc2 ? mag * ir : 0.f;
-  return make_float3(f * dx, f * dy, f * dz);
+// squared displacement from xs to x (minimum image)
+__device__ __forceinline__ float step_moved2(const Sur &S, float4 x, float4 xs) {
+  const float dx = wrapd(x.x - xs.x, S.L[0], S.iL[0]), dy = wrapd(x.y - xs.y, S.L[1], S.iL[1]),
+              dz = wrapd(x.z - xs.z, S.L[2], S.iL[2]);
+  return dx * dx + dy * dy + dz * dz;
 }
 
 // the WCA forces on a colloid at x from its n partners (ids in row, ascending; positions
-// in P), four positions fetched together, summed in partner order
+// in P): the force-shifted WCA pair force (cpp/update.cpp:14-32) in FP32 for the pairs
+// within the cutoff (1/r by the fast reciprocal square root, 1/r^6 from 1/r^2), four
+// positions fetched together, summed in partner order
 __device__ __forceinline__ float3 partner_forces(const Sur &S, float4 x, const float4 *P, const uint16_t *row, int n,
                                                  int self) {
   float3 fn = make_float3(0.f, 0.f, 0.f);
@@ -752,10 +773,14 @@ __device__ __forceinline__ float3 partner_forces(const Sur &S, float4 x, const f
     for (int i = 0; i < 4; ++i) xk[i] = P[e + i < n ? k4[i] : self];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      if (e + i >= n) break;
-      const float3 fp = wca_pair(S, wrapd(x.x - xk[i].x, S.L[0], S.iL[0]), wrapd(x.y - xk[i].y, S.L[1], S.iL[1]),
-                                 wrapd(x.z - xk[i].z, S.L[2], S.iL[2]));
-      fn.x += fp.x; fn.y += fp.y; fn.z += fp.z;
+      const float dx = wrapd(x.x - xk[i].x, S.L[0], S.iL[0]), dy = wrapd(x.y - xk[i].y, S.L[1], S.iL[1]),
+                  dz = wrapd(x.z - xk[i].z, S.L[2], S.iL[2]);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (e + i < n && r2 < S.rc2) {
+        const float ir = rsqrtf(r2), ir2 = ir * ir, ir6 = ir2 * ir2 * ir2;
+        const float f = (4.f * S.eps * (12.f * S.sig12 * ir6 * ir6 * ir - 6.f * S.sig6 * ir6 * ir) - S.fc) * ir;
+        fn.x += f * dx; fn.y += f * dy; fn.z += f * dz;
+      }
     }
   }
   return fn;
@@ -771,9 +796,12 @@ __device__ __forceinline__ float3 partner_forces(const Sur &S, float4 x, const f
 template <int PER>
 __global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
   extern __shared__ float4 smem[];
+  __shared__ unsigned s_vmax;  // the largest speed at the end (float bits, non-negative)
+  const float hs = 0.5f * partner_skin(S), hs2 = hs * hs;
   uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);  // [MAXC][MAXF] force partners
   uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MAXC * MAXF);   // [MAXC] their count
   const int T = blockDim.x, tid = threadIdx.x;
+  if (tid == 0) s_vmax = 0u;
   {
     const uint4 *src = reinterpret_cast<const uint4 *>(S.fpart);
     uint4 *dst = reinterpret_cast<uint4 *>(sF);
@@ -825,20 +853,25 @@ __global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
       fo[u] = make_float4(fn.x, fn.y, fn.z, 0.f);
     }
   }
-  int moved = 0;
+  int moved = 0, fast = 0;
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
     const int j = tid + T * u;
     if (j >= S.Nc) continue;
-    const float4 x0 = S.xref[j];
+    const float4 x0 = S.xref[j], xs = S.X[j];
     S.X[j] = x[u]; S.V[j] = v[u]; S.f[j] = fo[u];
     const float dx = wrapd(x[u].x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x[u].y - x0.y, S.L[1], S.iL[1]),
                 dz = wrapd(x[u].z - x0.z, S.L[2], S.iL[2]);
     moved |= dx * dx + dy * dy + dz * dz > S.half_skin2;
+    fast |= step_moved2(S, x[u], xs) > hs2;
+    atomicMax(&s_vmax, __float_as_uint(sqrtf(v[u].x * v[u].x + v[u].y * v[u].y + v[u].z * v[u].z)));
   }
   moved = __syncthreads_or(moved);
+  fast = __syncthreads_or(fast);
   if (tid == 0) {
     *S.rebuild = moved;
+    if (fast) *S.fast += 1;
+    *S.vmax = __uint_as_float(s_vmax);
     *S.step += 1;
   }
 }
@@ -861,19 +894,26 @@ __global__ void __cluster_dims__(MDC, 1, 1) __launch_bounds__(MD_MAXT) k_sur_md(
   uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);          // [MD_MAXT][MAXF] force partners
   uint8_t *sFn = reinterpret_cast<uint8_t *>(sF + MD_MAXT * MAXF);       // [MD_MAXT] their count
   int *sMoved = reinterpret_cast<int *>(sFn + MD_MAXT);                  // [MDC] (block 0)
+  unsigned *sVmax = reinterpret_cast<unsigned *>(sMoved + MDC);         // [MDC] (block 0)
+  __shared__ unsigned s_vmax;
+  const float hs = 0.5f * partner_skin(S), hs2 = hs * hs;
   const int tid = threadIdx.x, rank = (int)cl.block_rank();
   const int per = (S.Nc + MDC - 1) / MDC, j = rank * per + tid;
   const bool own = tid < per && j < S.Nc;
+  if (tid == 0) s_vmax = 0u;
   float4 x = make_float4(0.f, 0.f, 0.f, 0.f), v = x, fo = x, pl = x;
   int n = 0;
   if (own) {
     const uint4 *src = reinterpret_cast<const uint4 *>(S.fpart + (size_t)j * MAXF);
     uint4 *dst = reinterpret_cast<uint4 *>(sF + tid * MAXF);
-    const uint4 p0 = src[0], p1 = src[1], p2 = src[2];
+    uint4 pp[MAXF * 2 / 16];
+#pragma unroll
+    for (int i = 0; i < MAXF * 2 / 16; ++i) pp[i] = src[i];
     n = S.fpn[j];
     x = S.X[j]; v = S.V[j]; fo = S.f[j]; pl = S.imp[j];
     const float4 a = S.imp[S.Nc + j];
-    dst[0] = p0; dst[1] = p1; dst[2] = p2;
+#pragma unroll
+    for (int i = 0; i < MAXF * 2 / 16; ++i) dst[i] = pp[i];
     v.x += S.v0 * a.x; v.y += S.v0 * a.y; v.z += S.v0 * a.z;
   }
   cl.sync();  // every block has started before any writes to its copies
@@ -900,19 +940,29 @@ __global__ void __cluster_dims__(MDC, 1, 1) __launch_bounds__(MD_MAXT) k_sur_md(
   }
   int moved = 0;
   if (own) {
-    const float4 x0 = S.xref[j];
+    const float4 x0 = S.xref[j], xs = S.X[j];
     S.X[j] = x; S.V[j] = v; S.f[j] = fo;
     const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
                 dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
-    moved = dx * dx + dy * dy + dz * dz > S.half_skin2;
+    moved = (dx * dx + dy * dy + dz * dz > S.half_skin2 ? 1 : 0) | (step_moved2(S, x, xs) > hs2 ? 2 : 0);
+    atomicMax(&s_vmax, __float_as_uint(sqrtf(v.x * v.x + v.y * v.y + v.z * v.z)));
   }
-  moved = __syncthreads_or(moved);
-  if (tid == 0) *cl.map_shared_rank(sMoved + rank, 0) = moved;
+  moved = __syncthreads_or(moved & 1) | (__syncthreads_or(moved & 2) ? 2 : 0);
+  if (tid == 0) {
+    *cl.map_shared_rank(sMoved + rank, 0) = moved;
+    *cl.map_shared_rank(sVmax + rank, 0) = s_vmax;
+  }
   cl.sync();  // (also: no block leaves while another may still write its copies)
   if (rank == 0 && tid == 0) {
     int any = 0;
-    for (int b = 0; b < MDC; ++b) any |= sMoved[b];
-    *S.rebuild = any;
+    unsigned vm = 0u;
+    for (int b = 0; b < MDC; ++b) {
+      any |= sMoved[b];
+      vm = max(vm, sVmax[b]);
+    }
+    *S.rebuild = any & 1;
+    if (any & 2) *S.fast += 1;
+    *S.vmax = __uint_as_float(vm);
     *S.step += 1;
   }
 }
@@ -982,7 +1032,7 @@ T *salloc(mpcd_surrogate *s, size_t n) {
 
 constexpr size_t kMd1Smem = 2 * MAXC * sizeof(float4) + MAXC * MAXF * sizeof(uint16_t) + MAXC;
 constexpr int kMdBlockMax = 1024;  // colloids up to which the substeps run in one block, else in a cluster
-constexpr size_t kMdSmem = 2 * MAXC * sizeof(float4) + MD_MAXT * MAXF * sizeof(uint16_t) + MD_MAXT + MDC * sizeof(int);
+constexpr size_t kMdSmem = 2 * MAXC * sizeof(float4) + MD_MAXT * MAXF * sizeof(uint16_t) + MD_MAXT + 2 * MDC * sizeof(int);
 constexpr size_t kNetSmem = sizeof(NetSmem);
 
 int enqueue_step(mpcd_surrogate *s) {
@@ -1044,15 +1094,16 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   S.eps = (float)p->eps;
   S.fc = (float)(4.0 * p->eps * (12.0 * (std::pow(p->sig_colloid, 12) / std::pow(rc, 13)) -
                                  6.0 * (std::pow(p->sig_colloid, 6) / std::pow(rc, 7))));  // cpp/update.cpp:4
-  // force partners within the cutoff plus a skin of 1 (a colloid moves far less in one
-  // step), features within three radii; one all-pairs scan finds both
-  S.rforce2 = (float)((rc + 1.0) * (rc + 1.0));
-  S.rscan2 = S.rforce2 > S.ct_feat2 ? S.rforce2 : S.ct_feat2;
-  // candidate lists: within that distance plus a skin of 1, rebuilt once a colloid has
+  // force partners within the cutoff plus a skin of 0.5 to 2 (partner_skin; k_sur_md counts
+  // the steps in which a colloid moves more than half of it), features within three radii
+  S.rc = (float)rc;
+  const float rfmax2 = (float)((rc + 2.0) * (rc + 2.0));
+  S.rscan2 = rfmax2 > S.ct_feat2 ? rfmax2 : S.ct_feat2;
+  // candidate lists: within that distance plus a skin of 2, rebuilt once a colloid has
   // moved half the skin
-  const double rl = std::sqrt((double)S.rscan2) + 1.0;
+  const double rl = std::sqrt((double)S.rscan2) + 2.0;
   S.rlist2 = (float)(rl * rl);
-  S.half_skin2 = 0.25f;
+  S.half_skin2 = 1.0f;
   S.key = make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32));
   const size_t Nc = S.Nc;
   S.step = salloc<long long>(s, 1);
@@ -1065,6 +1116,8 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   if (S.rebuild) cudaMemset(S.rebuild, 1, sizeof(int));  // no candidate lists yet
   S.fpart = salloc<uint16_t>(s, Nc * MAXF); S.fpn = salloc<uint8_t>(s, Nc);
   S.err = salloc<int>(s, 1);
+  S.fast = salloc<long long>(s, 1);
+  S.vmax = salloc<float>(s, 1);
   s->wpk = salloc<uint4>(s, PACK_U4);
   S.wpk = s->wpk;
   s->outd = salloc<float>(s, Nc * NO);
@@ -1111,6 +1164,12 @@ extern "C" int mpcd_surrogate_set_state(mpcd_surrogate *s, const double *pos, co
         cudaStreamSynchronize(s->stream) != cudaSuccess)
       return sfail(s, MPCD_ERR_CUDA, "state upload");
   }
+  float vm = 0.f;  // the largest speed: the first step's partner skin
+  for (int j = 0; j < S.Nc; ++j)
+    vm = std::max(vm, (float)std::sqrt(vel[3 * j] * vel[3 * j] + vel[3 * j + 1] * vel[3 * j + 1] +
+                                       vel[3 * j + 2] * vel[3 * j + 2]));
+  if (cudaMemcpyAsync(S.vmax, &vm, sizeof vm, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+    return sfail(s, MPCD_ERR_CUDA, "set-up");
   k_sur_forces<<<(S.Nc + 127) / 128, 128, 0, s->stream>>>(S);
   k_sur_features<<<(S.Nc + 3) / 4, 128, 0, s->stream>>>(S);
   if (cudaMemsetAsync(S.rebuild, 1, sizeof(int), s->stream) != cudaSuccess) return sfail(s, MPCD_ERR_CUDA, "set-up");
@@ -1152,6 +1211,16 @@ extern "C" int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recomp
   return MPCD_OK;
 }
 
+extern "C" int mpcd_surrogate_fast_steps(mpcd_surrogate *s, int64_t *count) {
+  if (!s || !count) return MPCD_ERR_PARAM;
+  long long c = 0;
+  if (cudaMemcpyAsync(&c, s->S.fast, sizeof c, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+      cudaStreamSynchronize(s->stream) != cudaSuccess)
+    return sfail(s, MPCD_ERR_CUDA, "fast-step count");
+  *count = c;
+  return MPCD_OK;
+}
+
 // the network's outputs of the last step in physical units (n_colloid x 12, host)
 extern "C" int mpcd_surrogate_outputs(mpcd_surrogate *s, float *out) {
   if (!s || !out) return MPCD_ERR_PARAM;
@@ -1184,8 +1253,9 @@ extern "C" int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps) {
   if (cudaMemcpyAsync(&bits, s->S.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess)
     return sfail(s, MPCD_ERR_CUDA, std::string("step: ") + cudaGetErrorString(cudaGetLastError()));
-  if (bits) return sfail(s, MPCD_ERR_CAPACITY, "a colloid has more neighbours than its lists hold (64 within three "
-                                             "radii or the force cutoff plus the skin, 24 within the force cutoff "
-                                             "plus the skin)");
+  if (bits & 3)
+    return sfail(s, MPCD_ERR_CAPACITY, "a colloid has more neighbours than its lists hold (64 within three radii "
+                                       "or the force cutoff plus 4, 32 within the force cutoff plus 2)");
+  if (bits) return sfail(s, MPCD_ERR_CUDA, "a weight copy of the network kernel did not arrive");
   return MPCD_OK;
 }

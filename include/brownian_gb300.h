@@ -275,6 +275,11 @@ int mpcd_surrogate_features(mpcd_surrogate *s, float *out, int recompute);
 int mpcd_surrogate_outputs(mpcd_surrogate *s, float *out);
 /* nsteps MPCD steps; synchronises */
 int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps);
+/* Steps so far (since create) in which some colloid moved more than 1.0: the WCA force
+ * partners of a step are the pairs within the cutoff plus 2 at its start, so such a step
+ * may miss a collision.  Colloids of the trained closure move about 0.01 per step; the
+ * count rises for dynamics without drag (e.g. a network that predicts no exchange). */
+int mpcd_surrogate_fast_steps(mpcd_surrogate *s, int64_t *count);
 
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their

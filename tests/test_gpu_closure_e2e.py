@@ -31,4 +31,6 @@ def test_trained_closure_beats_no_closure():
     d_c = abs(res["rel_diff_vs_full"]["closure"]["msd"][1])
     d_n = abs(res["rel_diff_vs_full"]["no_closure"]["msd"][1])
     assert d_c < d_n, res["rel_diff_vs_full"]
+    # the trained closure's colloids never outrun the force-partner skin
+    assert res["fast_steps"]["closure"] == 0, res["fast_steps"]
     net.close()
