@@ -506,7 +506,7 @@ def run_ours(args, rank, world, dist):
     sim.close()
     stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
     ens = run_ensemble(args.ensemble, args.ensemble_steps, rank) if args.ensemble > 0 else None
-    clo = run_closure(args.closure_steps, 600) if (args.closure_steps > 0 and rank == 0) else None
+    clo = run_closure(args.closure_steps, 2000) if (args.closure_steps > 0 and rank == 0) else None
 
     if rank != 0:
         return None

@@ -392,3 +392,53 @@ def device_stats(obj, steps, L, **lags):
         return {k: v.tolist() for k, v in tr.analyse(**lags).items()}
     finally:
         tr.close()
+
+
+def demo(colloids=500, fraction=0.1, steps=30, seed=5):
+    """The colloid-only step with a random network (means and log-variances of order one,
+    exchange standard deviation 0.5) on randomly placed colloids of radius 2: a fixed
+    workload for timing and profiling the step's kernels.  Returns the state."""
+    import brownian_gb300 as bg
+    R = 2.0
+    L = int(round((colloids * 4.0 / 3.0 * np.pi * R ** 3 / fraction) ** (1.0 / 3.0)))
+    M = bg.displaced_mass(R, 10)
+    p = bg.make_params(L, 1, colloids, n_sub=10, mass_colloid=M, sig_colloid=4.0, sigma=4.0, I_colloid=0.4 * M * 4.0,
+                       v0=0.05, theta_deg=90.0, Dr=0.001, seed=seed)
+    rng = np.random.default_rng(seed)
+    pos = []
+    while len(pos) < colloids:  # random sequential placement, centre distance >= 4.3
+        x = rng.uniform(0, L, 3)
+        if pos:
+            d = np.array(pos) - x
+            d -= L * np.round(d / L)
+            if np.min(np.sum(d * d, axis=1)) < 4.3 ** 2:
+                continue
+        pos.append(x)
+    vel = rng.normal(0, 0.05, (colloids, 3))
+    w = rng.normal(0, 0.02, (colloids, 3))
+    ra = rng.normal(0, 1, (colloids, 3))
+    ra /= np.linalg.norm(ra, axis=1, keepdims=True)
+    net = Network(max_batch=max(colloids, 16), seed=seed)
+    net.set_params(rng.normal(0, 0.05, net.n_params).astype(np.float32))
+    net.set_normalisation(rng.normal(0, 0.1, IN).astype(np.float32), rng.uniform(0.5, 2, IN).astype(np.float32),
+                          np.zeros(NY, np.float32), np.full(NY, 0.5, np.float32))
+    sur = Surrogate(p, net)
+    try:
+        sur.set_state(np.array(pos), vel, w, ra)
+        sur.step(steps)
+        return sur.get_state()
+    finally:
+        sur.close()
+        net.close()
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description="colloid-only step with a random network (timing and profiling)")
+    ap.add_argument("what", choices=["demo"])
+    ap.add_argument("--colloids", type=int, default=500)
+    ap.add_argument("--fraction", type=float, default=0.1)
+    ap.add_argument("--steps", type=int, default=30)
+    a = ap.parse_args()
+    st = demo(a.colloids, a.fraction, a.steps)
+    print("ok", {k: float(np.abs(v).max()) for k, v in st.items()})
