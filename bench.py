@@ -370,6 +370,66 @@ def run_ensemble(nrep, steps, rank):
             "timing": "wall clock around mpcd_ensemble_step(K) (it ends with a device synchronisation)"}
 
 
+def run_large(steps, warmup=3):
+    """The large single system: 128^3 cells, density 10 (20,971,520 fluid particles), 2,000
+    colloids of radius 3 (mass of the displaced fluid, WCA sigma 6), v0 = 0.02, Dr = 0.0005,
+    SRD angle 130 degrees, 20 MD substeps, FP32 form with the FP64 diagnostics.  Particle-steps/s
+    from CUDA events around graph replays; per kernel its time per launch (profiled steps) and,
+    for the fluid passes, the fraction of the measured copy bandwidth their algorithmic bytes
+    reach."""
+    import numpy as np
+    import torch
+
+    import brownian_gb300 as bg
+    L3, NC3, R3, NSUB = 128, 2000, 3.0, 20
+    M = DENSITY * 4.0 / 3.0 * np.pi * R3 ** 3
+    N = L3 ** 3 * DENSITY
+    sim = bg.Simulation(L3, N, NC3, precision=bg.FP32C, n_sub=NSUB, ndt=0.1, kbt=1.0, kbt1=1.0, mass_fl=1.0,
+                        mass_colloid=M, sig_colloid=2 * R3, eps=1.0, sigma=2 * R3, I_colloid=0.4 * M * R3 ** 2,
+                        v0=0.02, theta_deg=130.0, Dr=0.0005, seed=0, init_gap=0.5)
+    st = torch.cuda.Stream()
+    sim.set_stream(st.cuda_stream)
+    sim.initialize(bg.INIT_PHYSICAL)
+    sim.setup()
+    sim.step(warmup)
+    d0 = sim.diag()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    sim.step(steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    d1 = sim.diag()
+    sim.profile(True)
+    sim.step(2)
+    prof = sim.profile_read()
+    sim.profile(False)
+    peak = measured_peak_hbm()[0]
+    per_particle = {"k_stream": 44, "k_rotate": 28, "k_rotate_sort": 64}  # algorithmic bytes, FP32 form
+    kernels = {}
+    for k, (n, tms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+        us = tms / max(n, 1) * 1e3
+        row = {"launches_per_step": n / 2, "us_per_launch": us, "share": tms / sum(v[1] for v in prof.values())}
+        if k in per_particle:
+            gbs = per_particle[k] * N / (us * 1e-6) / 1e9
+            row.update({"algorithmic_bytes_per_particle": per_particle[k], "achieved_gbs": gbs,
+                        "frac_of_measured_copy": gbs / peak})
+        kernels[k] = row
+    sim.close()
+    b_step = NSUB * 44 + 56
+    ps = N / (ms / 1e3)
+    return {"workload": "128^3 cells, density 10 (20,971,520 fluid particles), 2000 colloids r=3 (WCA sigma 6), "
+                        "v0 0.02, Dr 0.0005, SRD angle 130 deg, 20 substeps; FP32 form",
+            "steps": steps, "warmup": warmup, "ms_per_step": ms, "value": ps, "unit": "particle-steps/s",
+            "hbm_roofline_frac_step": b_step * ps / (peak * 1e9), "bytes_per_particle_step": b_step,
+            "peak_gbs": peak, "kernels": kernels,
+            "diag": {"temperature": d1["temperature_fluid"],
+                     # total momentum change over the timed steps, relative to sum |p_i| of a thermal fluid
+                     "momentum_drift_rel": float(np.max(np.abs(np.array(d1["momentum"]) - np.array(d0["momentum"])))
+                                                 / (N * np.sqrt(8.0 / np.pi)))}}
+
+
 def _speed_row(row, p, net, closure, bg, _t):
     """Time per MPCD step of full MPCD (FP64 and FP32 forms) and of the colloid-only step
     from the full run's colloid state, into row."""
@@ -506,6 +566,7 @@ def run_ours(args, rank, world, dist):
     sim.close()
     stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
     ens = run_ensemble(args.ensemble, args.ensemble_steps, rank) if args.ensemble > 0 else None
+    large = run_large(args.large_steps) if (args.large_steps > 0 and rank == 0) else None
     clo = run_closure(args.closure_steps, 2000) if (args.closure_steps > 0 and rank == 0) else None
 
     if rank != 0:
@@ -537,6 +598,8 @@ def run_ours(args, rank, world, dist):
         line["ensemble"] = ens
     if clo:
         line["closure"] = clo
+    if large is not None and rank == 0:
+        line["large"] = large
     return line
 
 
@@ -552,6 +615,8 @@ def main():
                     help="steps of the FP32c-vs-FP64 statistics run (MSD at lag 100; <=100: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="replicas of the batched-ensemble sub-object (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--large-steps", type=int, default=5,
+                    help="timed steps of the 128^3 / 2000-colloid FP32 system (0: skip)")
     ap.add_argument("--closure-steps", type=int, default=800,
                     help="steps per activity of the closure's training runs (500 colloids each; 0: skip)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
