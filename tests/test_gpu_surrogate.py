@@ -17,12 +17,15 @@ def _params(L, nc):
 
 def _state(L, nc, seed):
     rng = np.random.default_rng(seed)
-    pos = []
-    while len(pos) < nc:  # random sequential placement with centre distance >= 4.2
+    pos = np.empty((nc, 3))
+    n = 0
+    while n < nc:  # random sequential placement with centre distance >= 4.2
         x = rng.uniform(0, L, 3)
-        if all(np.linalg.norm((x - y) - L * np.round((x - y) / L)) >= 4.2 for y in pos):
-            pos.append(x)
-    pos = np.array(pos)
+        d = pos[:n] - x
+        d -= L * np.round(d / L)
+        if n == 0 or np.min(np.sum(d * d, axis=1)) >= 4.2 ** 2:
+            pos[n] = x
+            n += 1
     vel = rng.normal(0, 0.05, (nc, 3))
     w = rng.normal(0, 0.02, (nc, 3))
     ra = rng.normal(0, 1, (nc, 3))
@@ -94,5 +97,30 @@ def test_step_network_matches_mlp_forward(nc):
     ref = od.cpu().numpy()
     assert np.all(np.isfinite(got))
     assert np.array_equal(got, ref), np.max(np.abs(got - ref))
+    sur.close()
+    net.close()
+
+
+def test_cluster_substeps_above_1024_colloids():
+    """More than 1024 colloids: the substeps run in a cluster of 8 blocks.  The step stays finite,
+    the next step's network inputs are the features of the state it left (numpy restatement),
+    and the force partners cover every pair within the WCA cutoff."""
+    from brownian_gb300 import closure
+    L, nc = 60, 1200
+    net = closure.Network(max_batch=64, seed=2)
+    rng = np.random.default_rng(7)
+    net.set_params(rng.normal(0, 0.05, net.n_params).astype(np.float32))
+    net.set_normalisation(np.zeros(81), np.ones(81), np.zeros(6), np.full(6, 0.5))
+    sur = closure.Surrogate(_params(L, nc), net)
+    sur.set_state(*_state(L, nc, 11))
+    sur.step(20)
+    st = sur.get_state()
+    for k, v in st.items():
+        assert np.all(np.isfinite(v)), k
+    sur.step(1)
+    fused = sur.features(recompute=False)
+    ref = closure.features(st, L, 2.0)
+    assert np.allclose(fused, ref, atol=2e-5), np.max(np.abs(fused - ref))
+    assert sur.fast_steps() == 0
     sur.close()
     net.close()
