@@ -305,11 +305,20 @@ class Simulation:
              _f64(ang_vel_colloid, self.Nc), _f64(ra, self.Nc)]
         self._ck(lib().mpcd_set_state(self.h, *[_dp(x) for x in a]))
 
-    def get_state(self):
-        out = {k: np.empty((self.N, 3)) for k in ("pos_fl", "vel_fl")}
-        out.update({k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra", "f")})
-        self._ck(lib().mpcd_get_state(self.h, *[_dp(out[k]) for k in ("pos_fl", "vel_fl", "pos_colloid",
-                                                                      "vel_colloid", "ang_vel_colloid", "ra", "f")]))
+    _STATE_KEYS = ("pos_fl", "vel_fl", "pos_colloid", "vel_colloid", "ang_vel_colloid", "ra", "f")
+
+    def get_state(self, out=None):
+        """The state as (n, 3) float64 arrays.  `out`: a dict of C-contiguous float64 arrays of
+        those shapes to fill instead of new ones (page-locked ones make the copies direct)."""
+        if out is None:
+            out = {k: np.empty((self.N, 3)) for k in ("pos_fl", "vel_fl")}
+            out.update({k: np.empty((self.Nc, 3)) for k in self._STATE_KEYS[2:]})
+        for k in self._STATE_KEYS:
+            a = out[k]
+            n = self.N if k in ("pos_fl", "vel_fl") else self.Nc
+            if a.dtype != np.float64 or a.shape != (n, 3) or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape ({n}, 3)")
+        self._ck(lib().mpcd_get_state(self.h, *[_dp(out[k]) for k in self._STATE_KEYS]))
         return out
 
     def exchange(self, reset=True):

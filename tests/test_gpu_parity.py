@@ -121,6 +121,14 @@ def test_runs_are_deterministic():
     sa, sb = a.get_state(), b.get_state()
     for k in sa:
         assert np.array_equal(sa[k], sb[k]), k
+    # the same state into caller-provided page-locked buffers
+    import torch
+    out = {k: torch.empty(v.shape, dtype=torch.float64).pin_memory().numpy() for k, v in sa.items()}
+    got = b.get_state(out=out)
+    for k in sa:
+        assert got[k] is out[k] and np.array_equal(out[k], sa[k]), k
+    with pytest.raises(ValueError):
+        b.get_state(out=dict(out, pos_fl=np.empty((3, 3))))
 
 
 def test_momentum_conserved():
