@@ -463,7 +463,7 @@ def _speed_row(row, p, net, closure, bg, _t):
 def run_closure(samples_steps, deploy_steps):
     """The learned closure: training samples from full MPCD of the 64^3 system with v0 swept
     over [0, 0.1] (500 colloids x 5 activities x samples_steps steps), GPU training, then
-    colloid-only runs against full MPCD (the judge) on a 500-colloid system at volume
+    colloid-only runs against full MPCD (the yardstick) on a 500-colloid system at volume
     fraction 0.1, and the time per MPCD step of both at 500 and 2000 colloids."""
     import time as _t
 

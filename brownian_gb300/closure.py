@@ -330,7 +330,7 @@ def generate_gpu(params_list, steps, warmup=20, net=None):
 
 def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0, 1, 2, 5, 10, 20),
             olags=(0, 10, 50, 100)):
-    """Full MPCD (the judge), the closure surrogate and colloid-only dynamics without any
+    """Full MPCD (the yardstick), the closure surrogate and colloid-only dynamics without any
     fluid exchange, from the same colloid state: MSD, velocity and orientation
     autocorrelations, and the time per MPCD step of the full run and of the surrogate."""
     import time

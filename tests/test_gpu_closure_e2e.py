@@ -1,6 +1,6 @@
 """The learned closure end to end at a small size: samples from the exact collision
 kernel, training on the GPU, and what the trained network gains over the method
-without it (colloid-only dynamics with no fluid exchange), judged by full MPCD."""
+without it (colloid-only dynamics with no fluid exchange), measured against full MPCD."""
 import numpy as np
 import pytest
 
