@@ -429,16 +429,21 @@ __global__ void __launch_bounds__(256) k_cell_prep(const SysF64 S) {
     ab[9] = 0; ab[10] = 0; ab[11] = 0;
     return;
   }
-  const double inv = S.inv_n[n];
-  double ux = (double)a.sx * S.inv_sw * inv, uy = (double)a.sy * S.inv_sw * inv, uz = (double)a.sz * S.inv_sw * inv;
+  // (sx 2^-kw) / n in one product: the power-of-two scaling is exact, so this is the same
+  // rounding of the same exact product
+  const double insw = S.insw_n[n];
+  double ux = (double)a.sx * insw, uy = (double)a.sy * insw, uz = (double)a.sz * insw;
   double s2 = (double)a.s2 * S.inv_sw;
   double var = s2 - (double)n * (ux * ux + uy * uy + uz * uz);
-  double s = var > 0 ? sqrt(S.cs * (double)(n - 1) / var) : 1.0;
-  // rotation axis: rho = 2 ran - 1, phi = 4 asin(1) ran (cpp/rotation_mpcd.cpp:19-20)
+  // sqrt(cs (n - 1) / var) as sqrt(cs (n - 1)) (per n, from the host) times 1/sqrt(var): within
+  // a few ulp of the quotient's root, and no double division on the FP64 pipe
+  double s = var > 0 ? S.sqcs_n[n] * rsqrt(var) : 1.0;
+  // rotation axis: rho = 2 ran - 1, phi = 4 asin(1) ran (cpp/rotation_mpcd.cpp:19-20); the sine
+  // and cosine of phi = pi (2 ran) from sincospi (2 ran is exact), within an ulp of sincos(phi)
   uint4 r = draw4(S.key, DOM_AXIS, 0, (uint32_t)(c + 1), 0, (uint32_t)(S.ss->step + 1));
-  double rho = pm1(r.x), phi = S.two_pi * u01(r.y);
+  double rho = pm1(r.x);
   double sp, cp;
-  sincos(phi, &sp, &cp);
+  sincospi(2.0 * u01(r.y), &sp, &cp);
   double sq = sqrt(1.0 - rho * rho);
   double r1 = cp * sq, r2 = sp * sq, r3 = rho;
   double ct = S.ct, st = S.st, ict = S.ict;
