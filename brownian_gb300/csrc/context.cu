@@ -204,8 +204,8 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
 
 static void enq_fin_on(mpcd_ctx *c, cudaStream_t s, int mode, int l) {
   if (c->S.fin_table) {
-    // a block of four warps per colloid: warp 0 the colloid, all four its cell table
-    launch_on(c, s, "k_fin", k_fin, c->S.Nc > 0 ? c->S.Nc : 1, 128, c->S, mode, l);
+    // a block of eight warps per colloid: warp 0 the colloid, all eight its cell table
+    launch_on(c, s, "k_fin", k_fin, c->S.Nc > 0 ? c->S.Nc : 1, 256, c->S, mode, l);
     return;
   }
   // one warp per colloid (warp j / grid of block j % grid): each SM's FP64 unit
@@ -458,6 +458,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.sqrt_kt_m = sqrt(p.kbt / p.mass_fl);
   S.m_beta = p.mass_fl / p.kbt;
   S.inv_m_beta = p.kbt / p.mass_fl;
+  S.inv_mc = 1.0 / p.mass_colloid;
+  S.inv_ic = 1.0 / p.I_colloid;
   S.cs = 3.0 * p.kbt * dt2 / p.mass_fl;
   // run() gives each particle of a colloid's rear shell M v0 / (m cnt): with a shell of
   // one particle (a colloid whose rear is blocked by another) that is M v0 / m.  The

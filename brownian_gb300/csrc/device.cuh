@@ -540,11 +540,24 @@ static __device__ d3 activity_rot(const SysF64 &S, d3 ra, d3 sb, d3 cb, d3 xi) {
   return ra;
 }
 
+// sin x and cos x: for |x| < 2^-6 (the Euler angles Omega dt of a substep) by their
+// Maclaurin series in Horner form, whose first omitted terms x^9/9! and x^10/10! are below
+// 1e-21, so the results are within a few ulp; else sincos
+static __device__ __forceinline__ void sincos_small(double x, double *s, double *c) {
+  if (fabs(x) < 0.015625) {
+    const double x2 = x * x;
+    *s = x * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0) * (1.0 - x2 * (1.0 / 42.0))));
+    *c = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0) * (1.0 - x2 * (1.0 / 56.0))));
+  } else {
+    sincos(x, s, c);
+  }
+}
+
 static __device__ d3 activity(const SysF64 &S, d3 ra, d3 W, d3 xi) {
   d3 b = mul3s(W, S.dt), sb, cb;
-  sincos(b.x, &sb.x, &cb.x);
-  sincos(b.y, &sb.y, &cb.y);
-  sincos(b.z, &sb.z, &cb.z);
+  sincos_small(b.x, &sb.x, &cb.x);
+  sincos_small(b.y, &sb.y, &cb.y);
+  sincos_small(b.z, &sb.z, &cb.z);
   return activity_rot(S, ra, sb, cb, xi);
 }
 
@@ -682,7 +695,7 @@ static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, in
   // this step reads the orientation): lane k takes sin and cos of (Omega dt)_k
   if (act) {
     double s, co;
-    sincos(__dmul_rn(S.W[3 * j + k], S.dt), &s, &co);
+    sincos_small(__dmul_rn(S.W[3 * j + k], S.dt), &s, &co);
     const d3 sb = mk(__shfl_sync(grp, s, 0), __shfl_sync(grp, s, 1), __shfl_sync(grp, s, 2));
     const d3 cb = mk(__shfl_sync(grp, co, 0), __shfl_sync(grp, co, 1), __shfl_sync(grp, co, 2));
     const d3 rn = activity_rot(S, ldv(S.ra, j), sb, cb, ldv(S.xi, j));

@@ -717,7 +717,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
     e->lo[lane] = 0;
     const double dp = __dmul_rn(x, S.mass_fl);
     S.xacc[6 * j + lane] += dp;  // the exchange record (mpcd_exchange_read)
-    v = __dadd_rn(v, __ddiv_rn(dp, lin ? S.mass_colloid : S.I_colloid));
+    v = __dadd_rn(v, __dmul_rn(dp, lin ? S.inv_mc : S.inv_ic));  // (within an ulp of dp / M)
     if (lin) {
       // compute_force_md at X_g (done by the streaming pass) and update_velocity_colloid
       const double fn = S.fnew[3 * j + k];
@@ -731,7 +731,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
     // Omega moves to lanes 0-2, each takes one sine and cosine, all gather them
     const double w = __shfl_sync(grp, v, lin ? lane + 3 : lane);
     double s = 0, co = 0;
-    if (lin) sincos(__dmul_rn(w, S.dt), &s, &co);
+    if (lin) sincos_small(__dmul_rn(w, S.dt), &s, &co);
     const d3 sb = mk(__shfl_sync(grp, s, 0), __shfl_sync(grp, s, 1), __shfl_sync(grp, s, 2));
     const d3 cb = mk(__shfl_sync(grp, co, 0), __shfl_sync(grp, co, 1), __shfl_sync(grp, co, 2));
     const d3 r3 = mk(__shfl_sync(grp, ra, 0), __shfl_sync(grp, ra, 1), __shfl_sync(grp, ra, 2));
@@ -771,7 +771,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
   S.ra[3 * j + k] = ra;
 }
 
-__global__ void __launch_bounds__(128) k_fin(__grid_constant__ const SysF64 S, int mode, int l) {
+__global__ void __launch_bounds__(256) k_fin(__grid_constant__ const SysF64 S, int mode, int l) {
   k_fin_body(S, blockIdx.x, gridDim.x, mode, l);
 }
 

@@ -79,6 +79,7 @@ struct SysF64 {
   float rcf;           // FP32 prefilter radius of the WCA pair search
   double ddt;          // 0.5*dt*dt/mass_colloid         cpp/update.cpp:48
   double dtb2;         // dt/(mass_colloid*2)            cpp/update.cpp:63
+  double inv_mc, inv_ic;  // 1/mass_colloid, 1/I_colloid (the exchange's velocity changes)
   double v0, Dr, rotdiff_s;
   double ct, st, ict;  // cos, sin, 1-cos of the SRD angle
   double two_pi;       // 4.0*asin(1.0)

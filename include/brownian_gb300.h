@@ -149,7 +149,7 @@ int64_t mpcd_launch_count(const mpcd_ctx *c);
 /* ---- launch shapes (no counterpart in the reference: tuning of this implementation) -- */
 enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, multiple of 32) */
        MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32); the FP64
-                                  form runs one block of 128 per colloid (it also builds the
+                                  form runs one block of 256 per colloid (it also builds the
                                   cell tables) and ignores this shape */
        MPCD_LAUNCH_AUX = 2 };  /* colloid side work (forces, cell table, orientation; a kernel on a
                                   second stream beside the streaming and event passes): grid > 0
