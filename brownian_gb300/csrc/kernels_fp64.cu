@@ -590,7 +590,8 @@ __global__ void k_run_kick(const SysF64 S, int fb) {
     ShellRec rec = S.shell[i];
     if (!rec.pass) continue;
     int p = S.newpos[rec.p];
-    d3 v = mk(__ddiv_rn(F.wx[p], S.dt), __ddiv_rn(F.wy[p], S.dt), __ddiv_rn(F.wz[p], S.dt));
+    // v = w (1/dt): within an ulp of w / dt, without a double division per component
+    d3 v = mk(__dmul_rn(F.wx[p], S.inv_dt), __dmul_rn(F.wy[p], S.inv_dt), __dmul_rn(F.wz[p], S.inv_dt));
     for (int k = 0; k < rec.n; ++k) {
       if (!((rec.pass >> k) & 1)) continue;
       int j = rec.j[k];
