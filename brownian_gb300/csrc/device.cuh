@@ -249,14 +249,15 @@ static __device__ __forceinline__ double refl_gauss(const SysF64 &S, uint4 r1, u
       z = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
     }
   }
-  const double g = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(z)), z));
+  // -2 log(z) / z as -2 log(z) times 1/z (the reciprocal overlaps the logarithm; within an ulp)
+  const double g = __dsqrt_rn(__dmul_rn(__dmul_rn(-2.0, log(z)), __drcp_rn(z)));
   *v2 = __dmul_rn(__dmul_rn(x2, g), S.sqrt_kt_m);
   return __dmul_rn(__dmul_rn(x1, g), S.sqrt_kt_m);
 }
 
-// vector / |vector| as one reciprocal and three products (within an ulp of the
-// reference's three divisions)
-static __device__ __forceinline__ d3 refl_unit(d3 v) { return mul3s(v, __drcp_rn(__dsqrt_rn(norm2_ref(v.x, v.y, v.z)))); }
+// vector / |vector| as one reciprocal square root and three products (within a few ulp of
+// the reference's three divisions)
+static __device__ __forceinline__ d3 refl_unit(d3 v) { return mul3s(v, rsqrt(norm2_ref(v.x, v.y, v.z))); }
 
 // t = img(ran L - rf), the random point relative to the particle
 static __device__ __forceinline__ d3 refl_point(const SysF64 &S, uint4 r0, d3 rf) {
