@@ -345,7 +345,7 @@ static void enq_step(mpcd_ctx *c, bool sort) {
       enq_fin(c, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
     }
   }
-  launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+  launch(c, "k_end_step", k_end_step, 1, 256, c->S);
 }
 
 static int collect_profile(mpcd_ctx *c) {
@@ -912,7 +912,7 @@ extern "C" int mpcd_substep(mpcd_ctx *c, int l) {
   enq_fin(c, M_FINISH | M_ACT, l);
   c->next_sub = l + 1;
   if (l == n) {
-    launch(c, "k_end_step", k_end_step, 1, 32, c->S);
+    launch(c, "k_end_step", k_end_step, 1, 256, c->S);
     c->phase = 0;
     c->host_step += 1;
   }

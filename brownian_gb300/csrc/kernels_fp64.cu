@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
   // computed meanwhile) and the displacement bound as margin; pending particles
   // belong to the event passes and are skipped
   const int xb = (flags & F_PIPE) ? (int)((gs - 1) & 1) : buf;
-  const float mg = (flags & F_PIPE) ? S.cmarginf : 0.f;
+  const float mg = (flags & F_PIPE) ? S.ss->cm : 0.f;
 
   double x[U], y[U], z[U], wx[U], wy[U], wz[U];
   bool valid[U], ev[U];
@@ -761,7 +761,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
     const d3 Xn = mk(__shfl_sync(g3, xn, 0), __shfl_sync(g3, xn, 1), __shfl_sync(g3, xn, 2));
     S.X[nxt][3 * j + k] = xn;
     if (k == 0) {
-      if (d2 > S.cmargin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
+      if (d2 > S.ss->cm2) atomicOr(&S.ss->err, ERRB_DISPLACE);
       S.Xf[nxt][j] = make_float4((float)Xn.x, (float)Xn.y, (float)Xn.z, 0.f);
       S.cbox[nxt][j] = colloid_cell(S, Xn);
       colloid_q(S, nxt, j, Xn);
@@ -797,6 +797,8 @@ __global__ void __launch_bounds__(128) k_colloid_setup(const SysF64 S) {
     S.ss->nevents = 0;
     S.ss->nnew[0] = S.ss->nnew[1] = 0;
     S.ss->npend = 0;
+    S.ss->cm = S.cmarginf;  // the static bound until a step has measured the colloids
+    S.ss->cm2 = S.cmargin2;
   }
   if (j >= S.Nc) return;
   const int b = (int)((g0 - 1) & 1);
@@ -830,10 +832,49 @@ __global__ void __launch_bounds__(128) k_colloid_pot(const SysF64 S) {
 // completes a step: bumps the step counter
 static __device__ __forceinline__ void k_end_step_body(const SysF64 &S, const int VB, const int NVB) {
   if (VB != 0) return;
-  if (threadIdx.x == 0) S.ss->step += 1;
   // run()'s shell counts start from zero for the next step (its rear-shell test runs beside
   // the next step's cell pass, so the cell pass cannot clear them)
   for (int j = threadIdx.x; j < S.Nc; j += blockDim.x) S.shell_cnt[j] = 0;
+  if (S.precision == MPCD_FP64 && S.Nc > 0) {
+    // the next step's colloid margin: twice the largest displacement a substep gives at
+    // the colloids' present speeds, within [0.005, the static bound], and never below the
+    // move the next step's first streaming pass assumes (from the last substep's positions
+    // to the present ones, already checked against this step's margin; from the FP32
+    // copies of the positions, plus 2e-5 for their rounding).  A colloid that moves further
+    // in a substep fails the step (the finish checks every move).
+    __shared__ float s_vm[32], s_dm[32];
+    const long long g = (S.ss->step + 1) * S.n_sub;  // the substep the colloids are at
+    const float4 *Fc = S.Xf[g & 1], *Fp = S.Xf[(g - 1) & 1];
+    float vm = 0.f, dm = 0.f;
+    for (int j = threadIdx.x; j < S.Nc; j += blockDim.x) {
+      const float vx = (float)S.V[3 * j], vy = (float)S.V[3 * j + 1], vz = (float)S.V[3 * j + 2];
+      vm = fmaxf(vm, vx * vx + vy * vy + vz * vz);
+      const float4 a = Fc[j], b = Fp[j];
+      const float ex = wrapf(a.x - b.x, S.Lxf), ey = wrapf(a.y - b.y, S.Lyf), ez = wrapf(a.z - b.z, S.Lzf);
+      dm = fmaxf(dm, ex * ex + ey * ey + ez * ez);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      vm = fmaxf(vm, __shfl_xor_sync(0xFFFFFFFFu, vm, o));
+      dm = fmaxf(dm, __shfl_xor_sync(0xFFFFFFFFu, dm, o));
+    }
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      s_vm[w] = vm;
+      s_dm[w] = dm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < nw; ++k) {
+        vm = fmaxf(vm, s_vm[k]);
+        dm = fmaxf(dm, s_dm[k]);
+      }
+      float cm = fminf(fmaxf(2.f * (float)S.dt * sqrtf(vm), 0.005f), S.cmarginf);
+      cm = fmaxf(cm, sqrtf(dm) + 2e-5f);
+      S.ss->cm = cm;
+      S.ss->cm2 = (double)cm * (double)cm;
+    }
+  }
+  if (threadIdx.x == 0) S.ss->step += 1;
 }
 
 __global__ void k_end_step(__grid_constant__ const SysF64 S) {

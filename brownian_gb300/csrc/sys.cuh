@@ -61,6 +61,10 @@ struct StepState {
   long long ev_total;  // events summed over substeps (diagnostics)
   double rr[3];     // grid shift of the SRD binning the next streaming pass performs
   float rrf[3];     // the same, FP32
+  // FP64 form: the bound on a colloid's displacement in one substep the streaming pass's
+  // prefilter uses as margin this step and the colloid finish checks (cm2 = cm^2)
+  float cm;
+  double cm2;
 };
 
 struct SysF64 {
