@@ -315,9 +315,7 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32
 
 // the A fragment of K step kk (16 rows of the activations), one ldmatrix.x4: lane l
 // gives the address of row l % 16 at column kk + 8 (l / 16)
-__device__ __forceinline__ void a_frag(const bf16 (*A)[LDA], int kk, int gq, int q, uint32_t a[4]) {
-  (void)gq;
-  (void)q;
+__device__ __forceinline__ void a_frag(const bf16 (*A)[LDA], int kk, uint32_t a[4]) {
   const int lane = threadIdx.x & 31;
   const uint32_t addr = (uint32_t)__cvta_generic_to_shared(&A[lane & 15][kk + 8 * (lane >> 4)]);
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
@@ -625,17 +623,17 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
           for (int t = 0; t < TPW; ++t) b1[t] = B1[(TPW * warp + t) * 32 + lane];
         }
         uint32_t a[4];
-        a_frag(A, 32 * c, gq, q, a);
+        a_frag(A, 32 * c, a);
 #pragma unroll
         for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b0[t].x, b0[t].y);
-        a_frag(A, 32 * c + 16, gq, q, a);
+        a_frag(A, 32 * c + 16, a);
 #pragma unroll
         for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b0[t].z, b0[t].w);
         if (two) {
-          a_frag(A, 32 * c + 32, gq, q, a);
+          a_frag(A, 32 * c + 32, a);
 #pragma unroll
           for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b1[t].x, b1[t].y);
-          a_frag(A, 32 * c + 48, gq, q, a);
+          a_frag(A, 32 * c + 48, a);
 #pragma unroll
           for (int t = 0; t < TPW; ++t) mma_bf16(acc[t], a, b1[t].z, b1[t].w);
         }
@@ -671,9 +669,9 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
       for (int kp = 0; kp < H / 32; ++kp) {
         const uint4 b = B[(2 * kp + warp) * 32 + lane];
         uint32_t a[4];
-        a_frag(A, 32 * kp, gq, q, a);
+        a_frag(A, 32 * kp, a);
         mma_bf16(acc, a, b.x, b.y);
-        a_frag(A, 32 * kp + 16, gq, q, a);
+        a_frag(A, 32 * kp + 16, a);
         mma_bf16(acc, a, b.z, b.w);
       }
       const float *bias = sm.bias + 3 * H;
