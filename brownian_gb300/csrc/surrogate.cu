@@ -7,16 +7,18 @@
 // (cpp/update.cpp:34-46, plus rotational diffusion Dr), in FP32.
 //
 // Per step, two kernels (one CUDA graph):
-//   k_sur_net, one block per 16 colloids over the whole GPU: each colloid's
-//     neighbours (all pairs, one warp per four colloids), its 81 network inputs and
-//     its force partners for the step, the whole network (four layers, BF16
-//     mma.sync with FP32 accumulation, activations in shared memory, the weights
-//     streamed through a ring of shared-memory stages by cp.async while the block
-//     computes), the Gaussian draw of the exchange and the step's
-//     rotational-diffusion draws;
-//   k_sur_md, one cluster of 8 blocks: the active kick and the n_sub substeps (each
-//     needs every colloid's new position: distributed shared memory and one cluster
-//     barrier per substep).
+//   k_sur_net, one block per 16 colloids over the whole GPU (16 compute warps, one
+//     producer warp): each colloid's neighbours (from candidate lists kept with a
+//     skin, all pairs when they expire), its 81 network inputs and its force partners
+//     for the step, the whole network (four layers, BF16 mma.sync with FP32
+//     accumulation, activations in shared memory, the weights streamed through a
+//     ring of shared-memory stages by bulk copies while the block computes), the
+//     Gaussian draw of the exchange, the step's rotational-diffusion draws and the
+//     orientation through the substeps;
+//   the substeps, k_sur_md1 (one block, up to 1024 colloids) or k_sur_md (one cluster
+//     of 8 blocks): the active kick and the n_sub velocity-Verlet substeps (each needs
+//     every colloid's new position: a block barrier, or distributed shared memory and
+//     one cluster barrier, per substep).
 // The packed weights (the layout k_sur_net reads) are rebuilt from the network at
 // every mpcd_surrogate_step call.  k_sur_features computes the inputs of the
 // current state on request.
