@@ -69,7 +69,7 @@ struct mpcd_ctx {
   std::vector<cudaEvent_t> event_pool;
   std::map<std::string, std::pair<int64_t, double>> prof;
   StepState *ss_host = nullptr;  // pinned
-  double *inv_n = nullptr, *insw_n = nullptr, *sqcs_n = nullptr;
+  double *insw_n = nullptr, *sqcs_n = nullptr;
   double *part = nullptr;        // reduction partials
   int part_blocks = 256;
   double *staging = nullptr;     // AoS transfer buffer, allocated on first use
@@ -556,8 +556,6 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     S.pend = m.get<uint8_t>(S.N);
   }
   S.ss = m.get<StepState>(1);
-  c->inv_n = m.get<double>(S.max_per_cell + 1);
-  S.inv_n = c->inv_n;
   c->insw_n = m.get<double>(S.max_per_cell + 1);
   S.insw_n = c->insw_n;
   c->sqcs_n = m.get<double>(S.max_per_cell + 1);
@@ -569,13 +567,11 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     delete c;
     return m.err == cudaErrorMemoryAllocation ? MPCD_ERR_NOMEM : MPCD_ERR_CUDA;
   }
-  std::vector<double> inv(S.max_per_cell + 1, 0.0), insw(S.max_per_cell + 1, 0.0), sqcs(S.max_per_cell + 1, 0.0);
+  std::vector<double> insw(S.max_per_cell + 1, 0.0), sqcs(S.max_per_cell + 1, 0.0);
   for (int n = 1; n <= S.max_per_cell; ++n) {
-    inv[n] = 1.0 / n;
-    insw[n] = ldexp(inv[n], -S.kw);
+    insw[n] = ldexp(1.0 / n, -S.kw);
     sqcs[n] = sqrt(S.cs * (double)(n - 1));
   }
-  scopy(c, c->inv_n, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice);
   scopy(c, c->insw_n, insw.data(), sizeof(double) * insw.size(), cudaMemcpyHostToDevice);
   scopy(c, c->sqcs_n, sqcs.data(), sizeof(double) * sqcs.size(), cudaMemcpyHostToDevice);
   if (cudaMallocHost(&c->ss_host, sizeof(StepState)) != cudaSuccess) {

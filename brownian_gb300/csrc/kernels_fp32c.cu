@@ -475,11 +475,13 @@ static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const
     return;
   }
   // mean and thermostat factor in FP64 from the exact sums
-  const double inv = S.inv_n[n];
-  const double ux = (double)a.sx * S.inv_sw * inv, uy = (double)a.sy * S.inv_sw * inv, uz = (double)a.sz * S.inv_sw * inv;
+  // (2^-kw / n in one factor: the power-of-two scaling is exact)
+  const double insw = S.insw_n[n];
+  const double ux = (double)a.sx * insw, uy = (double)a.sy * insw, uz = (double)a.sz * insw;
   const double var = (double)a.s2 * S.inv_sw - (double)n * (ux * ux + uy * uy + uz * uz);
-  // S.cs is 3 kT dt^2 / m for the displacement sums of the FP64 form; these are velocity sums
-  const float s = var > 0 ? (float)sqrt(S.cs * S.inv_dt * S.inv_dt * (double)(n - 1) / var) : 1.f;
+  // S.cs is 3 kT dt^2 / m for the displacement sums of the FP64 form; these are velocity sums:
+  // sqrt(cs (n - 1)) / dt (per n) times 1/sqrt(var), no double division or square root
+  const float s = var > 0 ? (float)(S.sqcs_n[n] * S.inv_dt * rsqrt(var)) : 1.f;
   // rotation axis rho = 2 ran - 1, phi = 2 pi ran (cpp/rotation_mpcd.cpp:19-20)
   uint4 r = draw4(S.key, DOM_AXIS, 0, (uint32_t)(c + 1), 0, (uint32_t)(S.ss->step + 1));
   const float rho = 2.f * u01f(r.x) - 1.f;

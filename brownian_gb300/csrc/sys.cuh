@@ -113,8 +113,7 @@ struct SysF64 {
   // cells
   CellAcc *acc;        // [Cpad]
   double *cell_ab;     // [C][12]: A (row-major 3x3), b
-  const double *inv_n; // [max_per_cell+1]: 1/n
-  const double *insw_n;  // [max_per_cell+1]: 2^-kw / n (exact scaling of 1/n), the FP64 cell mean
+  const double *insw_n;  // [max_per_cell+1]: 2^-kw / n (exact scaling of 1/n), the cell mean of both forms
   const double *sqcs_n;  // [max_per_cell+1]: sqrt(cs (n - 1)), the FP64 thermostat's numerator
   // colloids
   double *X[2];        // [Nc][3] double-buffered by global substep parity
