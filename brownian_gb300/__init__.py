@@ -316,8 +316,9 @@ class Simulation:
         for k in self._STATE_KEYS:
             a = out[k]
             n = self.N if k in ("pos_fl", "vel_fl") else self.Nc
-            if a.dtype != np.float64 or a.shape != (n, 3) or not a.flags["C_CONTIGUOUS"]:
-                raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape ({n}, 3)")
+            if (a.dtype != np.float64 or a.shape != (n, 3) or not a.flags["C_CONTIGUOUS"]
+                    or not a.flags["WRITEABLE"]):
+                raise ValueError(f"out[{k!r}] must be a writeable C-contiguous float64 array of shape ({n}, 3)")
         self._ck(lib().mpcd_get_state(self.h, *[_dp(out[k]) for k in self._STATE_KEYS]))
         return out
 

@@ -331,7 +331,7 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
   cudaStreamWaitEvent(c->stream, c->ev_finp[n & 1], 0);
 }
 
-// one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:101-114)
+// one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:25-38)
 static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
   enq_rotation_run(c, sort);
@@ -851,7 +851,7 @@ extern "C" int mpcd_setup(mpcd_ctx *c) {
   const int zero = 0;
   CUDA_OK(c, cudaMemcpyAsync(&c->S.ss->err, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   // create_box + neighbour_list_md + compute_force_md: forces at the current positions,
-  // cell table around each colloid (cpp/active_brownian.cpp:93-96)
+  // cell table around each colloid (cpp/active_brownian.cpp:17-20)
   // no particle is pending between steps (a step cut short by an error may have left marks)
   if (c->S.pend) CUDA_OK(c, cudaMemsetAsync(c->S.pend, 0, (size_t)c->S.N, c->stream));
   if (c->S.Nc) CUDA_OK(c, cudaMemsetAsync(c->S.shell_cnt, 0, sizeof(int) * (size_t)c->S.Nc, c->stream));

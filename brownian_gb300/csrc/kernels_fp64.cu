@@ -784,7 +784,7 @@ __global__ void __launch_bounds__(128) k_fin_b(const SysF64 *Ss, const int *boff
   k_fin_body(sS, VB, NVB, mode, l);
 }
 
-// Set-up (the prologue of main, cpp/active_brownian.cpp:93-96): forces at the
+// Set-up (the prologue of main, cpp/active_brownian.cpp:17-20): forces at the
 // current positions (compute_force_md), the cell table for the run() candidates
 // of the first step (substep g0-1) and the table of the first substep g0.
 __global__ void __launch_bounds__(128) k_colloid_setup(const SysF64 S) {

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(kThreads) k_fluid_total(const double *__restri
 }
 
 // device address of g_partials, looked up once per device with that device current
-// (the host-side name of the array is not a device address)
+// (the host-side name of the array is not a device address); it stays valid while the
+// device's primary context lives, i.e. until a cudaDeviceReset of that device
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_lock;
 double *g_partials_dev[kMaxDevices] = {};
@@ -103,13 +104,30 @@ extern "C" int mpcd_fluid_sums_noalloc(const double *vel, int64_t n, double mass
             (long long)MPCD_NOALLOC_MAX_PARTICLES);
     return MPCD_ERR_CAPACITY;
   }
+  // An error an earlier, unrelated launch left on this thread belongs to its owner: report it
+  // without clearing it (cudaPeekAtLastError), and launch nothing.  With none pending, an
+  // error after a launch below is that launch's own, and is read (and cleared) here.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "mpcd_fluid_sums_noalloc: an earlier CUDA error is pending (%s); nothing launched\n",
+            cudaGetErrorString(e));
+    return MPCD_ERR_CUDA;
+  }
   double *part = nullptr;
   if (partials_for_current_device(&part) != cudaSuccess) return MPCD_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nblk = n > 0 ? (int)((n + kPerBlock - 1) / kPerBlock) : 1;
   k_fluid_partials<<<nblk, kThreads, 0, s>>>(vel, n, part);
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    fprintf(stderr, "mpcd_fluid_sums_noalloc: partial-sum launch: %s\n", cudaGetErrorString(e));
+    return MPCD_ERR_CUDA;
+  }
   k_fluid_total<<<1, kThreads, 0, s>>>(part, nblk, mass, out);
-  return cudaGetLastError() == cudaSuccess ? MPCD_OK : MPCD_ERR_CUDA;
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    fprintf(stderr, "mpcd_fluid_sums_noalloc: total launch: %s\n", cudaGetErrorString(e));
+    return MPCD_ERR_CUDA;
+  }
+  return MPCD_OK;
 }
 
 static_assert((long long)kMaxBlocks * kPerBlock == MPCD_NOALLOC_MAX_PARTICLES, "limit and scratch size agree");

@@ -163,7 +163,7 @@ void neighbour_list_md() {
   if (g_phase == IN_STEP) substep_routine(1);
 }
 
-// in the prologue: the set-up (create_box, neighbour lists and forces, cpp/active_brownian.cpp:93-96)
+// in the prologue: the set-up (create_box, neighbour lists and forces, cpp/active_brownian.cpp:17-20)
 void compute_force_md() {
   if (g_phase == INITIALISED) {
     upload_if_changed();

@@ -79,11 +79,11 @@ enum { MPCD_PHYSICS_REFERENCE = 0, MPCD_PHYSICS_FIXED = 1 };
 
 typedef struct {
   int64_t step;            /* completed MPCD steps                                        */
-  double ke_fluid;         /* cpp/active_brownian.cpp:131                                 */
-  double ke_colloid;       /* :128                                                        */
-  double ang_ke_colloid;   /* :129                                                        */
-  double potential_colloid;/* cpp/update.cpp:23                                           */
-  double energy_colloid;   /* :130                                                        */
+  double ke_fluid;         /* cpp/active_brownian.cpp:55                                  */
+  double ke_colloid;       /* :52                                                         */
+  double ang_ke_colloid;   /* :53                                                         */
+  double potential_colloid;/* cpp/update.cpp:16-24                                        */
+  double energy_colloid;   /* cpp/active_brownian.cpp:54                                  */
   double momentum[3];      /* fluid + colloid, this step (the reference never resets its sum) */
   double momentum_fluid[3];
   double temperature_fluid;/* 2 KE / (3 N kB) in units of kbt                             */
@@ -113,21 +113,21 @@ int64_t mpcd_get_step(const mpcd_ctx *c);
 /* initialize_colloid + initialize_fluid (cpp/initialize.cpp:31-83) and tumble (cpp/run.cpp:3-8) */
 int mpcd_initialize(mpcd_ctx *c, int style);
 /* create_box + neighbour_list_mpcd + neighbour_list_md + compute_force_md, the prologue of
- * main (cpp/active_brownian.cpp:93-96); required once after set_state/initialize */
+ * main (cpp/active_brownian.cpp:17-20); required once after set_state/initialize */
 int mpcd_setup(mpcd_ctx *c);
 /* rotation_mpcd (cpp/rotation_mpcd.cpp:3-50) for step counter+1 */
 int mpcd_rotation_mpcd(mpcd_ctx *c);
 /* run (cpp/run.cpp:10-26) */
 int mpcd_run(mpcd_ctx *c);
-/* one pass of the substep body l (1..n_sub) of cpp/active_brownian.cpp:104-113:
+/* one pass of the substep body l (1..n_sub) of cpp/active_brownian.cpp:28-37:
  * update_pos_md, neighbour_list_md, update_pos_mpcd, neighbour_list_mpcd,
  * fluid_colloid_collision, update_activity_direction, compute_force_md,
  * update_velocity_colloid */
 int mpcd_substep(mpcd_ctx *c, int l);
 /* nsteps complete MPCD steps (rotation_mpcd, run, n_sub substeps) — the loop of
- * cpp/active_brownian.cpp:99-132, replayed as one CUDA graph per step */
+ * cpp/active_brownian.cpp:23-56, replayed as one CUDA graph per step */
 int mpcd_step(mpcd_ctx *c, int nsteps);
-/* diagnostics of the state now (cpp/active_brownian.cpp:115-131) */
+/* diagnostics of the state now (cpp/active_brownian.cpp:39-55) */
 int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out);
 
 /* ---- observables for parity checks --------------------------------------------------- */
@@ -292,9 +292,12 @@ int mpcd_surrogate_fast_steps(mpcd_surrogate *s, int64_t *count);
  * as the fluid part of mpcd_diag, with no context.  Its per-block partial sums live in a
  * fixed 512 KiB array of the library that every GPU loading it holds until exit; nothing
  * is allocated.  The first call on a device looks up that array's device address (make it
- * before any stream capture).  All calls share the array: calls that overlap on the GPU
- * (other streams, other threads) race.  Returns MPCD_ERR_CAPACITY, with a message on
- * stderr, for n > MPCD_NOALLOC_MAX_PARTICLES. */
+ * before any stream capture); the address is kept for the life of the device's primary
+ * context, so after a cudaDeviceReset of that device the process must not call this
+ * function again.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race.  Returns MPCD_ERR_CAPACITY, with a message on stderr, for
+ * n > MPCD_NOALLOC_MAX_PARTICLES; returns MPCD_ERR_CUDA without launching (and without
+ * clearing that error) when an earlier CUDA error is pending on the calling thread. */
 #define MPCD_NOALLOC_MAX_PARTICLES 33554432LL
 int mpcd_fluid_sums_noalloc(const double *vel, int64_t n, double mass, double *out, void *stream);
 

@@ -719,7 +719,7 @@ int orc_update_velocity_colloid(orc_ctx *c) {
 
 /* ------------------------------------------------------------------ driver */
 
-/* cpp/active_brownian.cpp:93-96 */
+/* cpp/active_brownian.cpp:17-20 */
 int orc_setup(orc_ctx *c) {
   if (orc_create_box(c)) return -1;
   if (orc_neighbour_list_mpcd(c)) return -1;
@@ -727,7 +727,7 @@ int orc_setup(orc_ctx *c) {
   return orc_compute_force_md(c);
 }
 
-/* cpp/active_brownian.cpp:104-113 */
+/* cpp/active_brownian.cpp:28-37 */
 int orc_substep(orc_ctx *c, int l) {
   c->l = l;
   memcpy(c->old_force, c->f, sizeof(V3) * ((size_t)c->p.n_colloid + 2));
@@ -742,7 +742,7 @@ int orc_substep(orc_ctx *c, int l) {
   return orc_update_velocity_colloid(c);
 }
 
-/* cpp/active_brownian.cpp:99-114 */
+/* cpp/active_brownian.cpp:23-38 */
 int orc_step(orc_ctx *c) {
   c->nn += 1;
   if (orc_rotation_mpcd(c)) return -1;
@@ -758,7 +758,7 @@ int orc_run_steps(orc_ctx *c, int nsteps) {
   return 0;
 }
 
-/* cpp/active_brownian.cpp:115-131 with the momentum reset each call */
+/* cpp/active_brownian.cpp:39-55 with the momentum reset each call */
 void orc_diag(const orc_ctx *c, double *out) {
   double ke_colloid = 0, ke_fluid = 0, ang_ke_colloid = 0, abs_p = 0;
   V3 mom = v3(0, 0, 0);

@@ -99,7 +99,7 @@ int orc_run_steps(orc_ctx *c, int nsteps);
 int orc_get_step(const orc_ctx *c);
 void orc_set_step(orc_ctx *c, int nn);
 
-/* diagnostics of cpp/active_brownian.cpp:115-131, momentum reset per call:
+/* diagnostics of cpp/active_brownian.cpp:39-55, momentum reset per call:
  * out[0] ke_fluid, [1] ke_colloid, [2] ang_ke_colloid, [3] potential_colloid,
  * [4] energy_colloid, [5..7] total momentum (fluid + colloid), [8] sum |p_i| */
 void orc_diag(const orc_ctx *c, double *out);

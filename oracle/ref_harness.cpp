@@ -7,7 +7,7 @@
 // defines (cpp/active_brownian.cpp:3-7, names and types fixed by the
 // declarations in cpp/parameters.hpp:8-10,72), takes the parameters from the
 // command line instead of compile-time constants, and calls the routines in the
-// order of cpp/active_brownian.cpp:90-114, writing a record after each routine.
+// order of cpp/active_brownian.cpp:14-38, writing a record after each routine.
 //
 // Output: a stream of records  [char tag[48]][uint64 nbytes][bytes].
 // Modes:

@@ -2,7 +2,7 @@
 
 `replay(case)` drives the oracle through exactly the sequence that
 oracle/ref_harness.cpp drives the reference's own cpp/ routines through
-(cpp/active_brownian.cpp:90-114) and returns the same records (tag, bytes), so a
+(cpp/active_brownian.cpp:14-38) and returns the same records (tag, bytes), so a
 trace of the compiled reference and a trace of the oracle can be compared
 record by record.  `parse_records` reads the harness's binary record stream.
 """

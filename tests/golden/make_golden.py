@@ -7,7 +7,7 @@ occupancy of every binning, the candidate lists, the 342-cell neighbour table),
 plus the reference's ran() stream for two seeds.  Only needs the reference
 sources; run it in a checkout where they exist:
 
-    python tests/golden/make_golden.py [--ref /path/to/brownian]
+    python tests/golden/make_golden.py --ref /path/to/brownian
 
 The tests compare the oracle's own traces of the same cases against these
 hashes (tests/test_oracle_pin.py).
@@ -86,7 +86,7 @@ def run_case(case, tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="reference checkout (the directory holding cpp/)")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
     with tempfile.TemporaryDirectory() as tmp:

@@ -129,6 +129,10 @@ def test_runs_are_deterministic():
         assert got[k] is out[k] and np.array_equal(out[k], sa[k]), k
     with pytest.raises(ValueError):
         b.get_state(out=dict(out, pos_fl=np.empty((3, 3))))
+    ro = np.zeros_like(out["f"])
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        b.get_state(out=dict(out, f=ro))
 
 
 def test_momentum_conserved():

@@ -1,17 +1,18 @@
 """The reference's own driver (cpp/active_brownian.cpp) links against
 libbrownian_shim unchanged: every routine it calls is defined there.  Link only
-(running it needs a GPU); skipped where the reference sources are absent."""
+(running it needs a GPU); skipped unless BROWNIAN_REFERENCE names a reference
+checkout (the directory holding cpp/)."""
 import os
 import subprocess
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/cpp"
+REF = os.path.join(os.environ.get("BROWNIAN_REFERENCE", ""), "cpp")
 LIB = os.path.join(ROOT, "brownian_gb300", "lib")
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF, "active_brownian.cpp")), reason="reference sources absent")
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF, "active_brownian.cpp")), reason="BROWNIAN_REFERENCE unset or without cpp/")
 def test_reference_driver_links_against_the_shim(tmp_path):
     from brownian_gb300 import build
     build.build()

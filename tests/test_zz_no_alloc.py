@@ -51,6 +51,32 @@ def test_noalloc_sums_match_diag_on_two_calls():
     sim.close()
 
 
+@pytest.mark.parametrize("n", [0, 1, 2047, 2049, 600_000])
+def test_noalloc_sums_match_numpy(n):
+    """Sizes that leave the last block partial and, at 600,000 particles (293 blocks of
+    2,048), make the final reduction's strided loop over the block partials run more than
+    once; two calls in a row, the second on other velocities."""
+    import torch
+
+    import brownian_gb300 as bg
+    rng = np.random.default_rng(n + 1)
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for call in range(2):
+        vel = rng.normal(0.0, 1.0 + call, size=(max(n, 1), 3))[:n]
+        v = torch.from_numpy(np.ascontiguousarray(vel)).cuda() if n else torch.zeros(3, dtype=torch.float64,
+                                                                                      device="cuda")
+        out.fill_(float("nan"))
+        assert _sums(v.data_ptr(), n, 2.0, out.data_ptr(), stream.cuda_stream) == bg.OK
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        mom = 2.0 * vel.sum(axis=0) if n else np.zeros(3)
+        ke = 0.5 * 2.0 * float((vel * vel).sum()) if n else 0.0
+        scale = 2.0 * np.abs(vel).sum() if n else 1.0
+        assert np.all(np.abs(got[:3] - mom) <= RTOL * scale), (n, call, got, mom)
+        assert abs(got[3] - ke) <= RTOL * max(ke, 1e-300), (n, call, got[3], ke)
+
+
 def test_noalloc_rejects_more_than_its_maximum():
     import torch
 
