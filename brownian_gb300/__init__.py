@@ -23,7 +23,10 @@ INIT_REFERENCE, INIT_PHYSICAL = 0, 1
 # every symbol include/brownian_gb300.h declares
 EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", "mpcd_set_state", "mpcd_get_state",
            "mpcd_set_step", "mpcd_get_step", "mpcd_initialize", "mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run",
-           "mpcd_substep", "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
+           "mpcd_substep", "mpcd_update_pos_md", "mpcd_neighbour_list_md", "mpcd_update_pos_mpcd",
+           "mpcd_neighbour_list_mpcd", "mpcd_fluid_colloid_collision", "mpcd_update_activity_direction",
+           "mpcd_compute_force_md", "mpcd_update_velocity_colloid", "mpcd_get_neighbour_md", "mpcd_get_box_binning",
+           "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
@@ -34,6 +37,10 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_surrogate_features", "mpcd_surrogate_outputs", "mpcd_surrogate_fast_steps", "mpcd_surrogate_step", "mpcd_updown_velocity", "mpcd_traj_create",
            "mpcd_traj_destroy", "mpcd_traj_last_error", "mpcd_traj_frames", "mpcd_traj_reset", "mpcd_traj_record",
            "mpcd_traj_record_surrogate", "mpcd_traj_analyse", "mpcd_traj_read", "mpcd_traj_write"]
+# the routines of the substep body, in the reference's order (cpp/active_brownian.cpp:28-37)
+SUBSTEP_ROUTINES = ("update_pos_md", "neighbour_list_md", "update_pos_mpcd", "neighbour_list_mpcd",
+                    "fluid_colloid_collision", "update_activity_direction", "compute_force_md",
+                    "update_velocity_colloid")
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
 NOALLOC_MAX_PARTICLES = 33554432
 PHYSICS_REFERENCE, PHYSICS_FIXED = 0, 1
@@ -96,6 +103,10 @@ def lib():
         for n in ["mpcd_setup", "mpcd_rotation_mpcd", "mpcd_run"]:
             getattr(L, n).argtypes = [vp]
         L.mpcd_substep.argtypes = [vp, C.c_int]
+        for n in SUBSTEP_ROUTINES:
+            getattr(L, "mpcd_" + n).argtypes = [vp]
+        L.mpcd_get_neighbour_md.argtypes = [vp, ip, ip, C.c_int]
+        L.mpcd_get_box_binning.argtypes = [vp, ip, ip, ip]
         L.mpcd_step.argtypes = [vp, C.c_int]
         L.mpcd_diag.argtypes = [vp, C.POINTER(Diag)]
         L.mpcd_get_rotation_binning.argtypes = [vp, ip, ip, dp]
@@ -383,6 +394,52 @@ class Simulation:
 
     def substep(self, l):
         self._ck(lib().mpcd_substep(self.h, l))
+
+    def update_pos_md(self):
+        self._ck(lib().mpcd_update_pos_md(self.h))
+
+    def neighbour_list_md(self):
+        self._ck(lib().mpcd_neighbour_list_md(self.h))
+
+    def update_pos_mpcd(self):
+        self._ck(lib().mpcd_update_pos_mpcd(self.h))
+
+    def neighbour_list_mpcd(self):
+        self._ck(lib().mpcd_neighbour_list_mpcd(self.h))
+
+    def fluid_colloid_collision(self):
+        self._ck(lib().mpcd_fluid_colloid_collision(self.h))
+
+    def update_activity_direction(self):
+        self._ck(lib().mpcd_update_activity_direction(self.h))
+
+    def compute_force_md(self):
+        self._ck(lib().mpcd_compute_force_md(self.h))
+
+    def update_velocity_colloid(self):
+        self._ck(lib().mpcd_update_velocity_colloid(self.h))
+
+    def substep_routines(self):
+        """one substep as the eight routine calls, in the reference's order"""
+        for n in SUBSTEP_ROUTINES:
+            getattr(self, n)()
+
+    def neighbour_md(self, cap=256):
+        """the pair list of the last neighbour_list_md: per colloid its partners j > i (0-based)"""
+        cnt = np.zeros(self.Nc, np.int32)
+        lst = np.zeros((max(self.Nc, 1), cap), np.int32)
+        self._ck(lib().mpcd_get_neighbour_md(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             lst.ctypes.data_as(C.POINTER(C.c_int32)), cap))
+        return [lst[i, :min(cnt[i], cap)].copy() for i in range(self.Nc)]
+
+    def box_binning(self):
+        """the last neighbour_list_mpcd's box of each particle (1-based), occupancy of each box,
+        candidate count of each colloid"""
+        cell_of = np.empty(self.N, np.int32)
+        occ = np.empty(self.C, np.int32)
+        nn = np.empty(max(self.Nc, 1), np.int32)
+        self._ck(lib().mpcd_get_box_binning(self.h, *[a.ctypes.data_as(C.POINTER(C.c_int32)) for a in (cell_of, occ, nn)]))
+        return cell_of, occ, nn[:self.Nc]
 
     def step(self, nsteps=1):
         self._ck(lib().mpcd_step(self.h, nsteps))

@@ -24,7 +24,7 @@ LIB = os.path.join(OUT, "libbrownian_gb300.so")
 SHIM = os.path.join(OUT, "libbrownian_shim.so")
 
 SOURCES = ["kernels_fp64.cu", "kernels_fp32c.cu", "init_fp64.cu", "context.cu", "noalloc.cu", "mlp.cu", "surrogate.cu",
-           "diag.cu", "traj.cu"]
+           "diag.cu", "traj.cu", "routines.cu"]
 SHIM_SOURCES = ["shim.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "--extended-lambda", "-lineinfo",
               "-Xcompiler", "-fPIC,-ffp-contract=off"]

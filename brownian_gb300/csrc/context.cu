@@ -86,6 +86,12 @@ struct mpcd_ctx {
   ExchAcc *ud_acc = nullptr;
   long long ud_epoch = -1;
   int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
+  // routine-by-routine substep: the next routine of the substep body (0: update_pos_md)
+  int rseq = 0;
+  // neighbour_list_mpcd observables (allocated on first use): box of each particle,
+  // occupancy of each box, candidates of each colloid
+  int *box_cell = nullptr, *box_occ = nullptr, *box_nn = nullptr;
+  bool box_valid = false;
 };
 
 static int fail(mpcd_ctx *c, int code, const std::string &m) {
@@ -373,6 +379,7 @@ static const char *err_text(int bits) {
   if (bits & ERRB_SHELLSLOTS) return "a particle lies in more rear shells than a record holds";
   if (bits & ERRB_DELTA) return "a colloid momentum exchange left the range of the exact sums";
   if (bits & ERRB_EVENTS) return "the wall-collision event lists overflowed";
+  if (bits & ERRB_NBR) return "a colloid has more pair-list partners than the list holds";
   return "device error";
 }
 
@@ -541,6 +548,12 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.xacc = m.get<double>(6 * Nc);
   S.shell_cnt = m.get<int>(Nc);
   S.pot_part = m.get<double>(Nc);
+  S.fold = m.get<double>(3 * Nc);
+  S.nbr_n = m.get<int>(Nc);
+  S.nbr = m.get<uint16_t>(Nc * NBR_CAP);
+  S.bkt_start = m.get<int>((size_t)NBK_MAX * NBK_MAX * NBK_MAX + 1);
+  S.bkt_cur = m.get<int>((size_t)NBK_MAX * NBK_MAX * NBK_MAX);
+  S.bkt_list = m.get<int>(Nc);
   // run() candidates: particles within sigma/2 + 1/2 of a colloid, with room to spare
   const double rsh = p.sigma * 0.5 + 0.5, density = (double)S.N / (double)S.C;
   double est = (double)S.Nc * (4.0 / 3.0 * M_PI * rsh * rsh * rsh * density * 2.0 + 64.0);
@@ -626,7 +639,8 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   if (c->evs) cudaStreamDestroy(c->evs);
-  for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc})
+  for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc, (void *)c->box_cell,
+                  (void *)c->box_occ, (void *)c->box_nn})
     if (q) cudaFree(q);
   for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
@@ -653,8 +667,15 @@ extern "C" int mpcd_set_stream(mpcd_ctx *c, void *stream) {
 
 // ---------------------------------------------------------------- state
 
+// the colloid position buffer holding the present positions: that of the last substep
+// of the last completed step, or inside a step begun routine by routine, that of the
+// substep the routines have reached
 static int cur_buf(const mpcd_ctx *c) {
   long long g = c->ss_host->step * c->S.n_sub - 1;
+  if (c->phase == 1 && (c->next_sub > 1 || c->rseq > 0)) {
+    const int l = c->rseq > 0 ? c->next_sub : c->next_sub - 1;
+    g = c->host_step * c->S.n_sub + (l - 1);
+  }
   return (int)(g & 1);
 }
 
@@ -728,6 +749,8 @@ static int invalidate_tables(mpcd_ctx *c) {
   c->setup_done = false;
   c->phase = 0;
   c->next_sub = 1;
+  c->rseq = 0;
+  c->box_valid = false;
   return MPCD_OK;
 }
 
@@ -900,6 +923,8 @@ extern "C" int mpcd_substep(mpcd_ctx *c, int l) {
   if (l < 1 || l > n) return fail(c, MPCD_ERR_PARAM, "substep out of range");
   if (c->phase != 1 || c->next_sub != l)
     return fail(c, MPCD_ERR_STATE, "substeps follow rotation_mpcd and run, in order 1..n_sub");
+  if (c->rseq != 0)
+    return fail(c, MPCD_ERR_STATE, "a substep begun routine by routine is unfinished (update_velocity_colloid closes it)");
   enq_fin(c, M_ADVANCE, l - 1);   // update_pos_md, neighbour_list_md
   // update_pos_mpcd, neighbour_list_mpcd, fluid_colloid_collision (fluid side), and
   // compute_force_md at the new colloid positions
@@ -960,7 +985,7 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   if ((r = need_setup(c))) return r;
   const SysF64 &S = c->S;
   launch(c, "k_diag_fluid", k_diag_fluid, c->part_blocks, 256, S, c->part);
-  if (S.Nc) launch(c, "k_colloid_pot", k_colloid_pot, colloid_grid(c), 128, S);
+  if (S.Nc) launch(c, "k_colloid_pot", k_colloid_pot, colloid_grid(c), 128, S, cur_buf(c));
   if ((r = check_device(c))) return r;
   std::vector<double> part((size_t)c->part_blocks * 5);
   CUDA_OK(c, scopy(c, part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
@@ -1062,6 +1087,9 @@ extern "C" int64_t mpcd_launch_count(const mpcd_ctx *c) { return c ? c->launches
 
 // initialisation lives in init.cu; it needs the context internals
 #include "init_host.inc"
+
+// the substep body routine by routine
+#include "routines_host.inc"
 
 extern "C" int mpcd_exchange_read(mpcd_ctx *c, double *out, int reset) {
   if (!c) return MPCD_ERR_PARAM;

@@ -566,6 +566,43 @@ static __device__ __forceinline__ float wrapf(float d, float L) { return d - L *
 // the same with a reciprocal of L (for prefilters that carry a margin)
 static __device__ __forceinline__ float wrapf_r(float d, float L, float iL) { return d - L * rintf(d * iL); }
 
+// One pair term of compute_force_md (cpp/update.cpp:21-28) in the reference's FP64
+// expression order: with temp = img(X_j - X_k) and r = |temp| < r_cutoff, the force
+// on j from k (ff) and, with want_pot, the pair's potential (pt).  Returns whether
+// the pair is inside the cutoff.
+static __device__ __forceinline__ bool wca_pair(const SysF64 &S, d3 Xj, const double *Xc, int k, bool want_pot,
+                                                d3 &ff, double &pt) {
+  d3 temp = mk(ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
+               ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz));
+  double r = __dsqrt_rn(norm2_ref(temp.x, temp.y, temp.z));
+  if (!(r < S.r_cutoff)) return false;
+  double p13 = r, p7 = r;
+  for (int i = 1; i < 13; ++i) { p13 = __dmul_rn(p13, r); if (i == 6) p7 = p13; }
+  double t1 = __ddiv_rn(S.sig12, p13), t2 = __ddiv_rn(S.sig6, p7);
+  double mag = __dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(__dmul_rn(12.0, t1), __dmul_rn(6.0, t2))), S.fc);
+  ff = div3s(mul3s(temp, mag), r);
+  if (want_pot) {
+    double q = __ddiv_rn(S.sig_colloid, r);
+    pt = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(pow(q, 12.0), pow(q, 6.0))), S.ufc),
+                   __dmul_rn(S.fc, r));
+  }
+  return true;
+}
+
+// Adds the pair terms of the lanes that hit, in lane order, to f and pot (every
+// lane ends with the same sums).
+static __device__ __forceinline__ void wca_gather(bool hit, d3 ff, double pt, d3 &f, double &pot) {
+  unsigned hm = __ballot_sync(FULL, hit);
+  while (hm) {
+    int src = __ffs(hm) - 1;
+    hm &= hm - 1;
+    double fx = __shfl_sync(FULL, ff.x, src), fy = __shfl_sync(FULL, ff.y, src), fz = __shfl_sync(FULL, ff.z, src);
+    double pp = __shfl_sync(FULL, pt, src);
+    f = add3(f, mk(fx, fy, fz));
+    pot = __dadd_rn(pot, pp);
+  }
+}
+
 // WCA force on colloid j at positions Xc (compute_force_md, cpp/update.cpp:14-32):
 // partners with r < r_cutoff summed in ascending partner order, which is the
 // order the reference's pair loop adds them to f[j].  FP32 prefilter over all
@@ -602,35 +639,31 @@ static __device__ d3 wca_force(const SysF64 &S, const double *Xc, const float4 *
       if (!m) continue;
       d3 ff = mk(0, 0, 0);
       double pt = 0;
-      bool hit = false;
-      if (cand) {
-        d3 temp = mk(ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
-                     ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz));
-        double r = __dsqrt_rn(norm2_ref(temp.x, temp.y, temp.z));
-        if (r < S.r_cutoff) {
-          hit = true;
-          double p13 = r, p7 = r;
-          for (int i = 1; i < 13; ++i) { p13 = __dmul_rn(p13, r); if (i == 6) p7 = p13; }
-          double t1 = __ddiv_rn(S.sig12, p13), t2 = __ddiv_rn(S.sig6, p7);
-          double mag = __dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(__dmul_rn(12.0, t1), __dmul_rn(6.0, t2))), S.fc);
-          ff = div3s(mul3s(temp, mag), r);
-          if (want_pot && k > j) {
-            double q = __ddiv_rn(S.sig_colloid, r);
-            pt = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(4.0, S.eps), __dsub_rn(pow(q, 12.0), pow(q, 6.0))), S.ufc),
-                           __dmul_rn(S.fc, r));
-          }
-        }
-      }
-      unsigned hm = __ballot_sync(FULL, hit);
-      while (hm) {
-        int src = __ffs(hm) - 1;
-        hm &= hm - 1;
-        double fx = __shfl_sync(FULL, ff.x, src), fy = __shfl_sync(FULL, ff.y, src), fz = __shfl_sync(FULL, ff.z, src);
-        double pp = __shfl_sync(FULL, pt, src);
-        f = add3(f, mk(fx, fy, fz));
-        pot = __dadd_rn(pot, pp);
-      }
+      const bool hit = cand && wca_pair(S, Xj, Xc, k, want_pot && k > j, ff, pt);
+      wca_gather(hit, ff, pt, f, pot);
     }
+  }
+  return f;
+}
+
+// The same sum over colloid j's pair list (neighbour_list_md: its partners within the
+// list radius, both below and above j, in ascending order), one partner per lane.
+static __device__ d3 wca_force_list(const SysF64 &S, const double *Xc, int j, int lane, bool want_pot, double &pot) {
+  d3 f = mk(0, 0, 0);
+  pot = 0;
+  const d3 Xj = ldv(Xc, j);
+  const int n = min(S.nbr_n[j], NBR_CAP);
+  const uint16_t *lst = S.nbr + (size_t)j * NBR_CAP;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + lane;
+    d3 ff = mk(0, 0, 0);
+    double pt = 0;
+    bool hit = false;
+    if (i < n) {
+      const int k = lst[i];
+      hit = wca_pair(S, Xj, Xc, k, want_pot && k > j, ff, pt);
+    }
+    wca_gather(hit, ff, pt, f, pot);
   }
   return f;
 }
@@ -664,6 +697,34 @@ static __device__ __forceinline__ float table_reach(const SysF64 &S, long long e
   return (e % S.n_sub) == S.n_sub - 1 ? S.rT_shell : S.rT_coll;
 }
 
+// update_activity_direction (cpp/update.cpp:34-46) of colloid j on lanes k = 0-2 of
+// group grp: lane k takes sin and cos of (Omega dt)_k, all three gather them, lane 0
+// stores the turned orientation (with the rotational-diffusion normals S.xi[j])
+static __device__ __forceinline__ void activity_apply(const SysF64 &S, int j, int k, unsigned grp) {
+  double s, co;
+  sincos_small(__dmul_rn(S.W[3 * j + k], S.dt), &s, &co);
+  const d3 sb = mk(__shfl_sync(grp, s, 0), __shfl_sync(grp, s, 1), __shfl_sync(grp, s, 2));
+  const d3 cb = mk(__shfl_sync(grp, co, 0), __shfl_sync(grp, co, 1), __shfl_sync(grp, co, 2));
+  const d3 rn = activity_rot(S, ldv(S.ra, j), sb, cb, ldv(S.xi, j));
+  if (k == 0) stv(S.ra, j, rn);
+}
+
+// the three standard normals of substep g's rotational diffusion of colloid j
+// (Box-Muller) into S.xi[j], on lanes k = 0-2 of group grp: lane 0 the pair (r0, t0)
+// giving xi_x and xi_y, lane 1 the pair (r1, t1) giving xi_z
+static __device__ __forceinline__ void rotdiff_draw(const SysF64 &S, long long g, int j, int k, unsigned grp) {
+  uint4 r = draw4(S.key, DOM_ROTDIFF, 0, (uint32_t)(j + 1), 0, (uint32_t)g);
+  const uint32_t ur = k == 0 ? r.x : r.z, ut = k == 0 ? r.y : r.w;
+  double rr = 0, sn = 0, cs = 0;
+  if (k < 2) {
+    rr = sqrt(-2.0 * log(u01(ur)));
+    sincos(__dmul_rn(S.two_pi, u01(ut)), &sn, &cs);
+  }
+  const double r0 = __shfl_sync(grp, rr, 0), s0 = __shfl_sync(grp, sn, 0), c0 = __shfl_sync(grp, cs, 0);
+  const double r1 = __shfl_sync(grp, rr, 1), c1 = __shfl_sync(grp, cs, 1);
+  if (k == 0) stv(S.xi, j, mk(__dmul_rn(r0, c0), __dmul_rn(r0, s0), __dmul_rn(r1, c1)));
+}
+
 // Colloid work that the next substep needs and nothing in this substep changes
 // (k_aux, on a second stream beside the streaming and event passes of this
 // substep): the WCA forces at the positions X_g (compute_force_md) and the cell
@@ -691,31 +752,12 @@ static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, in
   }
   if (w != 1 || lane >= 3) return;
   const unsigned grp = 0x7u;
-  const int k = lane;
   // update_activity_direction of the previous substep (nothing before the end of
-  // this step reads the orientation): lane k takes sin and cos of (Omega dt)_k
-  if (act) {
-    double s, co;
-    sincos_small(__dmul_rn(S.W[3 * j + k], S.dt), &s, &co);
-    const d3 sb = mk(__shfl_sync(grp, s, 0), __shfl_sync(grp, s, 1), __shfl_sync(grp, s, 2));
-    const d3 cb = mk(__shfl_sync(grp, co, 0), __shfl_sync(grp, co, 1), __shfl_sync(grp, co, 2));
-    const d3 rn = activity_rot(S, ldv(S.ra, j), sb, cb, ldv(S.xi, j));
-    if (k == 0) stv(S.ra, j, rn);
-  }
+  // this step reads the orientation), with the normals that substep drew
+  if (act) activity_apply(S, j, lane, grp);
   if (S.Dr > 0) {
-    // the three standard normals of this substep's rotational diffusion (Box-Muller):
-    // lane 0 the pair (r0, t0) giving xi_x and xi_y, lane 1 the pair (r1, t1) giving xi_z
     __syncwarp(grp);
-    uint4 r = draw4(S.key, DOM_ROTDIFF, 0, (uint32_t)(j + 1), 0, (uint32_t)g);
-    const uint32_t ur = k == 0 ? r.x : r.z, ut = k == 0 ? r.y : r.w;
-    double rr = 0, sn = 0, cs = 0;
-    if (k < 2) {
-      rr = sqrt(-2.0 * log(u01(ur)));
-      sincos(__dmul_rn(S.two_pi, u01(ut)), &sn, &cs);
-    }
-    const double r0 = __shfl_sync(grp, rr, 0), s0 = __shfl_sync(grp, sn, 0), c0 = __shfl_sync(grp, cs, 0);
-    const double r1 = __shfl_sync(grp, rr, 1), c1 = __shfl_sync(grp, cs, 1);
-    if (k == 0) stv(S.xi, j, mk(__dmul_rn(r0, c0), __dmul_rn(r0, s0), __dmul_rn(r1, c1)));
+    rotdiff_draw(S, g, j, lane, grp);
   }
 }
 

@@ -5,7 +5,7 @@
 namespace bgb {
 
 enum : int { F_STREAM = 1, F_COLLIDE = 2, F_SHELL = 4, F_BINROT = 8, F_PIPE = 16 };
-enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8 };
+enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8, M_COLL = 16 };
 
 // k_stream<FLAGS> instantiations, by flag set (nullptr for a set not built)
 using StreamKernel = void (*)(const SysF64, int, int);
@@ -52,7 +52,17 @@ __global__ void k_run_kick(const SysF64 S, int fb);
 __global__ void k_fin(__grid_constant__ const SysF64 S, int mode, int l);
 __global__ void k_aux(__grid_constant__ const SysF64 S, int l, int act);
 __global__ void k_colloid_setup(const SysF64 S);
-__global__ void k_colloid_pot(const SysF64 S);
+__global__ void k_colloid_pot(const SysF64 S, int b);
+// routine-by-routine substeps (routines.cu)
+__global__ void k_cbucket(const SysF64 S, const double *Xc, NListGeo geo);
+__global__ void k_nlist(const SysF64 S, const double *Xc, NListGeo geo);
+__global__ void k_force_list(const SysF64 S, const double *Xc);
+__global__ void k_act_now(const SysF64 S, int l);
+__global__ void k_vel_colloid(const SysF64 S);
+__global__ void k_unpend(const SysF64 S);
+__global__ void k_table(const SysF64 S, int l);
+__global__ void k_box_bin(const SysF64 S, int fb, int *cell_of, int *occ);
+__global__ void k_no_neigh(const SysF64 S, int b, const int *occ, int *no_neigh);
 __global__ void k_end_step(__grid_constant__ const SysF64 S);
 __global__ void k_diag_fluid(const SysF64 S, double *part);
 

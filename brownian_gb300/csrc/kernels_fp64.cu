@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
     wx[u] = wy[u] = wz[u] = 0;
     if (valid[u]) {
       x[u] = F.x[p]; y[u] = F.y[p]; z[u] = F.z[p];
-      if (flags & (F_STREAM | F_BINROT)) { wx[u] = F.wx[p]; wy[u] = F.wy[p]; wz[u] = F.wz[p]; }
+      if (flags & (F_STREAM | F_BINROT | F_COLLIDE)) { wx[u] = F.wx[p]; wy[u] = F.wy[p]; wz[u] = F.wz[p]; }
       if (flags & F_PIPE) pd[u] = S.pend[p];
     }
   }
@@ -345,12 +345,15 @@ __global__ void __launch_bounds__(256) k_bin(const SysF64 S, int fb) {
 
 StreamKernel stream_kernel(int flags) {
   // substeps run overlapped (F_PIPE; the last one's binning is k_bin); the set-up
-  // pass stands alone
+  // pass stands alone; the routine-by-routine substep streams (F_STREAM) and tests
+  // for wall collisions (F_COLLIDE) in passes of their own
   switch (flags) {
     case F_STREAM | F_COLLIDE | F_PIPE: return k_stream<F_STREAM | F_COLLIDE | F_PIPE>;
     case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE:
       return k_stream<F_STREAM | F_COLLIDE | F_SHELL | F_PIPE>;
     case F_SHELL | F_BINROT: return k_stream<F_SHELL | F_BINROT>;
+    case F_STREAM: return k_stream<F_STREAM>;
+    case F_COLLIDE: return k_stream<F_COLLIDE>;
   }
   return nullptr;
 }
@@ -380,6 +383,7 @@ EventKernel event_kernel(int flags) {
     case F_STREAM | F_COLLIDE | F_PIPE: return k_events<F_COLLIDE | F_PIPE>;
     case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE: return k_events<F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
     case F_SHELL | F_BINROT: return k_events<F_SHELL | F_BINROT>;
+    case F_COLLIDE: return k_events<F_COLLIDE>;
   }
   return nullptr;
 }
@@ -710,7 +714,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
   double v = lin ? S.V[3 * j + k] : S.W[3 * j + k];
   double f = lin ? S.f[3 * j + k] : 0.0;
 
-  if (mode & M_FINISH) {
+  if (mode & (M_FINISH | M_COLL)) {
     // end of fluid_colloid_collision: V += vc m/M, Omega += omega m/I (cpp/fluid_colloid_collision.cpp:46-47)
     ExchAcc *e = S.exch + j;
     const double x = __dadd_rn((double)e->hi[lane] * 0x1p-20, (double)e->lo[lane] * 0x1p-72);
@@ -719,7 +723,7 @@ static __device__ __forceinline__ void k_fin_colloid(const SysF64 &S, int j, int
     const double dp = __dmul_rn(x, S.mass_fl);
     S.xacc[6 * j + lane] += dp;  // the exchange record (mpcd_exchange_read)
     v = __dadd_rn(v, __dmul_rn(dp, lin ? S.inv_mc : S.inv_ic));  // (within an ulp of dp / M)
-    if (lin) {
+    if (lin && (mode & M_FINISH)) {
       // compute_force_md at X_g (done by the streaming pass) and update_velocity_colloid
       const double fn = S.fnew[3 * j + k];
       v = __dadd_rn(v, __dmul_rn(__dadd_rn(f, fn), S.dtb2));
@@ -817,13 +821,12 @@ __global__ void __launch_bounds__(128) k_colloid_setup(const SysF64 S) {
                   [&](int cell) { tappend(S.Tcnt[b ^ 1], S.Tlist[b ^ 1], cell, g0, j, err); });
 }
 
-// WCA potential of the current configuration, per colloid (pairs k > j), for the
-// diagnostics (cpp/update.cpp:23)
-__global__ void __launch_bounds__(128) k_colloid_pot(const SysF64 S) {
+// WCA potential of the configuration in position buffer b, per colloid (pairs k > j),
+// for the diagnostics (cpp/update.cpp:24)
+__global__ void __launch_bounds__(128) k_colloid_pot(const SysF64 S, int b) {
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (j >= S.Nc) return;
-  const int b = (int)((S.ss->step * S.n_sub - 1) & 1);
   double pot;
   wca_force(S, S.X[b], S.Xf[b], j, lane, true, pot);
   if (lane == 0) S.pot_part[j] = pot;

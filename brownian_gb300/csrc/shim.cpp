@@ -9,14 +9,17 @@
 //   step rotation_mpcd, run and n substeps of update_pos_md, neighbour_list_md,
 //   update_pos_mpcd, neighbour_list_mpcd, [updown_velocity], fluid_colloid_collision,
 //   update_activity_direction, compute_force_md, update_velocity_colloid.
-// The GPU runs a substep as one fused pass: update_pos_md starts substep l and
-// the next routines of the substep only advance the position in the sequence;
-// update_velocity_colloid ends it and copies the colloid arrays (and, after the
-// last substep of a step, the fluid arrays) into the reference's globals.  The
-// state lives on the GPU; edits the caller makes to the global arrays between
-// initialize_fluid and the set-up's compute_force_md are uploaded.  Random
-// numbers are the library's keyed Philox draws (key = the global `seed`), not the
-// reference's ran() stream, so a run is statistically, not bitwise, the reference's.
+// Each routine of a substep runs its own entry point (mpcd_update_pos_md ...
+// mpcd_update_velocity_colloid) and then copies the arrays it writes into the
+// reference's globals (pos_colloid; pos_fl; pos_fl, vel_fl, vel_colloid and
+// ang_vel_colloid; ra; f and potential_colloid; vel_colloid), so the globals hold the
+// GPU's state after every routine; rotation_mpcd and run copy the fluid and colloid
+// velocities.  The state lives on the GPU; edits the caller makes to the global arrays
+// between steps (or between initialize_fluid and the set-up's compute_force_md) are
+// uploaded at the next rotation_mpcd (or the set-up), and the set-up then runs again:
+// forces and cell tables at the edited positions.  Random numbers are the library's
+// keyed Philox draws (key = the global `seed`), not the reference's ran() stream, so a
+// run is statistically, not bitwise, the reference's.
 // updown_velocity is a no-op: the reference discards its results, and the counts it leaves in
 // the globals are overwritten by run() before anything reads them (the diagnostic itself is
 // mpcd_updown_velocity).
@@ -46,10 +49,10 @@ namespace {
 mpcd_ctx *g_ctx = nullptr;
 enum Phase { NONE, ALLOCATED, INITIALISED, READY, IN_STEP };
 Phase g_phase = NONE;
-int g_sub = 0;          // substep in progress (0: none)
-int g_seq = 0;          // position within the substep's routine sequence
-std::vector<double> g_seen_fl;  // fluid state as last copied to the globals (pos then vel)
-std::vector<double> g_seen_c;   // colloid state as last copied (pos, vel, ang_vel, ra)
+// the arrays as last copied to or from the GPU, so that edits by the caller show
+enum { A_POS_FL, A_VEL_FL, A_POS_C, A_VEL_C, A_ANG_C, A_RA, A_COUNT };
+std::vector<double> g_seen[A_COUNT];
+int g_sub = 0;  // substeps opened in the present step
 
 [[noreturn]] void die(const char *what) {
   fprintf(stderr, "brownian_shim: %s%s%s\n", what, g_ctx ? ": " : "", g_ctx ? mpcd_last_error(g_ctx) : "");
@@ -62,42 +65,52 @@ void check(int r, const char *what) {
 
 double *flat(shim_point *a) { return &a[1].x; }  // the reference's arrays are 1-based
 
-void download(bool fluid) {
-  double *pf = nullptr, *vf = nullptr;
-  if (fluid) {
-    pf = flat(pos_fl);
-    vf = flat(vel_fl);
-  }
-  check(mpcd_get_state(g_ctx, pf, vf, flat(pos_colloid), flat(vel_colloid), flat(ang_vel_colloid), flat(ra), flat(f)),
-        "copying the state to the reference's arrays");
-  const size_t N3 = 3 * (size_t)no_of_fluid, C3 = 3 * (size_t)no_of_colloid;
-  if (fluid) {
-    g_seen_fl.resize(2 * N3);
-    memcpy(g_seen_fl.data(), pf, 8 * N3);
-    memcpy(g_seen_fl.data() + N3, vf, 8 * N3);
-  }
-  g_seen_c.resize(4 * C3);
-  memcpy(g_seen_c.data(), flat(pos_colloid), 8 * C3);
-  memcpy(g_seen_c.data() + C3, flat(vel_colloid), 8 * C3);
-  memcpy(g_seen_c.data() + 2 * C3, flat(ang_vel_colloid), 8 * C3);
-  memcpy(g_seen_c.data() + 3 * C3, flat(ra), 8 * C3);
-  mpcd_diag_t d;
-  if (mpcd_diag(g_ctx, &d) == MPCD_OK) potential_colloid = d.potential_colloid;
+shim_point *global_of(int a) {
+  shim_point *const g[A_COUNT] = {pos_fl, vel_fl, pos_colloid, vel_colloid, ang_vel_colloid, ra};
+  return g[a];
 }
 
-// upload the globals if the caller changed them since they were last copied
-void upload_if_changed() {
-  const size_t N3 = 3 * (size_t)no_of_fluid, C3 = 3 * (size_t)no_of_colloid;
-  const bool fl_changed = g_seen_fl.size() != 2 * N3 || memcmp(g_seen_fl.data(), flat(pos_fl), 8 * N3) ||
-                          memcmp(g_seen_fl.data() + N3, flat(vel_fl), 8 * N3);
-  const bool c_changed = g_seen_c.size() != 4 * C3 || memcmp(g_seen_c.data(), flat(pos_colloid), 8 * C3) ||
-                         memcmp(g_seen_c.data() + C3, flat(vel_colloid), 8 * C3) ||
-                         memcmp(g_seen_c.data() + 2 * C3, flat(ang_vel_colloid), 8 * C3) ||
-                         memcmp(g_seen_c.data() + 3 * C3, flat(ra), 8 * C3);
-  if (fl_changed || c_changed)
-    check(mpcd_set_state(g_ctx, fl_changed ? flat(pos_fl) : nullptr, fl_changed ? flat(vel_fl) : nullptr,
-                         flat(pos_colloid), flat(vel_colloid), flat(ang_vel_colloid), flat(ra)),
-          "copying the reference's arrays to the GPU");
+size_t count_of(int a) { return 3 * (size_t)(a <= A_VEL_FL ? no_of_fluid : no_of_colloid); }
+
+void remember(int a) {
+  g_seen[a].resize(count_of(a));
+  memcpy(g_seen[a].data(), flat(global_of(a)), 8 * count_of(a));
+}
+
+// copy the named arrays (bits of 1 << A_*), and f and the potential when `forces`, from
+// the GPU into the reference's globals
+void pull(unsigned which, bool forces = false) {
+  double *p[A_COUNT];
+  for (int a = 0; a < A_COUNT; ++a) p[a] = (which >> a) & 1u ? flat(global_of(a)) : nullptr;
+  check(mpcd_get_state(g_ctx, p[A_POS_FL], p[A_VEL_FL], p[A_POS_C], p[A_VEL_C], p[A_ANG_C], p[A_RA],
+                       forces ? flat(f) : nullptr),
+        "copying the state to the reference's arrays");
+  for (int a = 0; a < A_COUNT; ++a)
+    if ((which >> a) & 1u) remember(a);
+  if (forces) {
+    mpcd_diag_t d;
+    check(mpcd_diag(g_ctx, &d), "diagnostics");
+    potential_colloid = d.potential_colloid;
+  }
+}
+
+const unsigned ALL = (1u << A_COUNT) - 1u;
+
+// upload the globals if the caller changed them since they were last copied; the set-up
+// then runs again (forces and tables at the edited state).  Returns whether it uploaded.
+bool upload_if_changed() {
+  bool changed[A_COUNT], fl = false, any = false;
+  for (int a = 0; a < A_COUNT; ++a) {
+    changed[a] = g_seen[a].size() != count_of(a) || memcmp(g_seen[a].data(), flat(global_of(a)), 8 * count_of(a));
+    any = any || changed[a];
+  }
+  fl = changed[A_POS_FL] || changed[A_VEL_FL];
+  if (!any) return false;
+  check(mpcd_set_state(g_ctx, fl ? flat(pos_fl) : nullptr, fl ? flat(vel_fl) : nullptr, flat(pos_colloid),
+                       flat(vel_colloid), flat(ang_vel_colloid), flat(ra)),
+        "copying the reference's arrays to the GPU");
+  for (int a = 0; a < A_COUNT; ++a) remember(a);
+  return true;
 }
 
 shim_point *alloc_points(int count) {
@@ -106,10 +119,11 @@ shim_point *alloc_points(int count) {
   return p;
 }
 
-// the eight routines of a substep, in the reference's order; update_pos_md opens it
-void substep_routine(int seq) {
-  if (g_phase != IN_STEP || g_sub < 1 || g_seq != seq) die("substep routines called out of the reference's order");
-  g_seq = seq + 1;
+// a routine of the substep body: its entry point, then its arrays to the globals
+void substep_routine(int (*fn)(mpcd_ctx *), const char *name, unsigned writes, bool forces = false) {
+  if (g_phase != IN_STEP) die("substep routines run inside a step (after rotation_mpcd and run)");
+  check(fn(g_ctx), name);
+  if (writes || forces) pull(writes, forces);
 }
 
 }  // namespace
@@ -143,7 +157,7 @@ void initialize_fluid() {
   if (g_phase != ALLOCATED) die("initialize_fluid before initialize");
   check(mpcd_initialize(g_ctx, MPCD_INIT_REFERENCE), "initialisation");
   check(mpcd_set_step(g_ctx, 0), "initialisation");
-  download(true);
+  pull(ALL);
   g_phase = INITIALISED;
 }
 
@@ -155,56 +169,65 @@ void tumble() {
 void create_box() {}
 void updown_velocity() {}
 
+// the set-up (create_box, neighbour lists and forces, cpp/active_brownian.cpp:17-20)
+static void setup() {
+  check(mpcd_setup(g_ctx), "set-up");
+  pull(0, true);
+  g_phase = READY;
+}
+
 void neighbour_list_mpcd() {
-  if (g_phase == IN_STEP) substep_routine(3);
+  if (g_phase == INITIALISED || g_phase == READY) return;  // the prologue: part of the set-up
+  substep_routine(mpcd_neighbour_list_mpcd, "neighbour_list_mpcd", 0);
 }
 
 void neighbour_list_md() {
-  if (g_phase == IN_STEP) substep_routine(1);
+  if (g_phase == INITIALISED || g_phase == READY) return;  // the prologue: part of the set-up
+  substep_routine(mpcd_neighbour_list_md, "neighbour_list_md", 0);
 }
 
-// in the prologue: the set-up (create_box, neighbour lists and forces, cpp/active_brownian.cpp:17-20)
+// in the prologue the set-up; inside a step the routine
 void compute_force_md() {
   if (g_phase == INITIALISED) {
     upload_if_changed();
-    check(mpcd_setup(g_ctx), "set-up");
-    download(false);
-    g_phase = READY;
+    setup();
     return;
   }
-  substep_routine(6);
+  substep_routine(mpcd_compute_force_md, "compute_force_md", 0, true);
 }
 
 void rotation_mpcd() {
   if (g_phase == INITIALISED) die("rotation_mpcd before the set-up");
   if (g_phase != READY) die("rotation_mpcd inside a step");
-  upload_if_changed();
+  if (upload_if_changed()) setup();
   check(mpcd_rotation_mpcd(g_ctx), "rotation_mpcd");
   g_phase = IN_STEP;
   g_sub = 0;
+  pull(1u << A_VEL_FL);
 }
 
 void run() {
-  if (g_phase != IN_STEP || g_sub != 0) die("run out of order");
+  if (g_phase != IN_STEP) die("run out of order");
   check(mpcd_run(g_ctx), "run");
+  pull((1u << A_VEL_FL) | (1u << A_VEL_C));
 }
 
 void update_pos_md() {
-  if (g_phase != IN_STEP || g_sub >= n || (g_sub > 0 && g_seq != 8)) die("update_pos_md out of order");
+  substep_routine(mpcd_update_pos_md, "update_pos_md", 1u << A_POS_C);
   g_sub += 1;
-  check(mpcd_substep(g_ctx, g_sub), "substep");
-  g_seq = 1;
+}
+void update_pos_mpcd() { substep_routine(mpcd_update_pos_mpcd, "update_pos_mpcd", 1u << A_POS_FL); }
+void fluid_colloid_collision() {
+  substep_routine(mpcd_fluid_colloid_collision, "fluid_colloid_collision",
+                  (1u << A_POS_FL) | (1u << A_VEL_FL) | (1u << A_VEL_C) | (1u << A_ANG_C));
+}
+void update_activity_direction() {
+  substep_routine(mpcd_update_activity_direction, "update_activity_direction", 1u << A_RA);
 }
 
-void update_pos_mpcd() { substep_routine(2); }
-void fluid_colloid_collision() { substep_routine(4); }
-void update_activity_direction() { substep_routine(5); }
-
 void update_velocity_colloid() {
-  substep_routine(7);
-  const bool last = g_sub == n;
-  download(last);
-  if (last) {
+  substep_routine(mpcd_update_velocity_colloid, "update_velocity_colloid", 1u << A_VEL_C);
+  if (g_sub == n) {  // the last substep closed the step
     g_phase = READY;
     g_sub = 0;
   }

@@ -15,11 +15,14 @@ enum : int {
   ERRB_DISPLACE = 16,   // a wall collision moved a particle further than the cell-table margin
   ERRB_SHELLSLOTS = 32, // a particle sits in the rear shells of more colloids than a record holds
   ERRB_DELTA = 64,      // a colloid momentum exchange left the range of the exact sums
-  ERRB_EVENTS = 128     // the wall-collision event (or pending-particle) lists overflowed
+  ERRB_EVENTS = 128,    // the wall-collision event (or pending-particle) lists overflowed
+  ERRB_NBR = 256        // a colloid has more pair-list partners than the list holds
 };
 
 constexpr int TCAP = 16;     // colloids per cell in the fluid-to-colloid table
 constexpr int SHELL_J = 8;   // colloids per run() candidate record
+constexpr int NBR_CAP = 256; // partners per colloid in the colloid pair list (the reference holds 200)
+constexpr int NBK_MAX = 32;  // buckets per axis of the colloid pair-list grid
 
 // one run() candidate: a particle whose binned cell is in the 342-cell block of
 // each listed colloid and which lies within sigma/2 + 1/2 of it
@@ -165,6 +168,21 @@ struct SysF64 {
   // step state
   StepState *ss;
   double *pot_part;    // [Nc] per-colloid share of the WCA potential
+  // routine-by-routine substeps (mpcd_update_pos_md ... mpcd_update_velocity_colloid)
+  double *fold;        // [Nc][3] old_force: the force before this substep's compute_force_md
+  int *nbr_n;          // [Nc] partners in the colloid pair list
+  uint16_t *nbr;       // [Nc][NBR_CAP] partners of each colloid, ascending (both sides of j)
+  int *bkt_start;      // [NBK_MAX^3 + 1] first slot of each bucket of the pair-list grid
+  int *bkt_cur;        // [NBK_MAX^3] fill cursor of each bucket
+  int *bkt_list;       // [Nc] colloids by bucket
+};
+
+// the bucket grid of a colloid pair list: per axis nb buckets of width bs >= the list
+// radius (every partner within it is in a neighbouring bucket), r2 = radius^2
+struct NListGeo {
+  int nb[3];
+  double bs[3];
+  double r2;
 };
 
 // view of one fluid buffer

@@ -124,6 +124,43 @@ int mpcd_run(mpcd_ctx *c);
  * fluid_colloid_collision, update_activity_direction, compute_force_md,
  * update_velocity_colloid */
 int mpcd_substep(mpcd_ctx *c, int l);
+
+/* The same substep routine by routine: one entry point per reference routine of the body of
+ * cpp/active_brownian.cpp:28-37, each its own launches and its own effect on the state, for a
+ * caller that drives them one at a time as main() does.  Called in the reference's order
+ * after rotation_mpcd and run (MPCD_ERR_STATE otherwise), the n_sub passes give mpcd_substep's
+ * bits.  update_pos_md opens substep l (the next one) and update_velocity_colloid closes it;
+ * after the last substep it also bins the fluid for the next rotation_mpcd and records the
+ * next run()'s rear-shell candidates (what the fused step's last streaming pass does).  The
+ * FP64 form only (MPCD_ERR_STATE for MPCD_FP32C). */
+/* update_pos_md (cpp/update.cpp:48-54), after old_force = f (cpp/active_brownian.cpp:28) */
+int mpcd_update_pos_md(mpcd_ctx *c);
+/* neighbour_list_md (cpp/neighbour_list.cpp:27-39): the colloid pair list within 3 sig_colloid,
+ * built from a grid of buckets at least that wide (mpcd_get_neighbour_md reads it) */
+int mpcd_neighbour_list_md(mpcd_ctx *c);
+/* update_pos_mpcd (cpp/update.cpp:56-60) */
+int mpcd_update_pos_mpcd(mpcd_ctx *c);
+/* neighbour_list_mpcd (cpp/neighbour_list.cpp:41-58): the per-cell colloid table the collision
+ * scans, rebuilt at the present colloid positions, and the reference's box binning and
+ * per-colloid candidate counts (mpcd_get_box_binning reads them) */
+int mpcd_neighbour_list_mpcd(mpcd_ctx *c);
+/* fluid_colloid_collision (cpp/fluid_colloid_collision.cpp:26-49): the reflections and the
+ * colloids' velocity and angular-velocity changes */
+int mpcd_fluid_colloid_collision(mpcd_ctx *c);
+/* update_activity_direction (cpp/update.cpp:34-46), with the rotational diffusion Dr */
+int mpcd_update_activity_direction(mpcd_ctx *c);
+/* compute_force_md (cpp/update.cpp:14-32) over the pair list of the last neighbour_list_md */
+int mpcd_compute_force_md(mpcd_ctx *c);
+/* update_velocity_colloid (cpp/update.cpp:62-67) */
+int mpcd_update_velocity_colloid(mpcd_ctx *c);
+/* the pair list of the last mpcd_neighbour_list_md as the reference keeps it
+ * (neighbour[k][i], cpp/neighbour_list.cpp:35): per colloid i (0-based) count[i] partners
+ * j > i, ascending, 0-based, in partners[i * cap + k] (up to cap per colloid) */
+int mpcd_get_neighbour_md(mpcd_ctx *c, int32_t *count, int32_t *partners, int cap);
+/* the last mpcd_neighbour_list_mpcd's binning (cpp/neighbour_list.cpp:44-47): per particle its
+ * 1-based box number 1 + cell(pos) (cell_of[N]), per box 1..C its occupancy fluid_no
+ * (occupancy[C]), per colloid its candidate count no_neigh (no_neigh[Nc]); NULL skips */
+int mpcd_get_box_binning(mpcd_ctx *c, int32_t *cell_of, int32_t *occupancy, int32_t *no_neigh);
 /* nsteps complete MPCD steps (rotation_mpcd, run, n_sub substeps) — the loop of
  * cpp/active_brownian.cpp:23-56, replayed as one CUDA graph per step */
 int mpcd_step(mpcd_ctx *c, int nsteps);

@@ -727,10 +727,17 @@ int orc_setup(orc_ctx *c) {
   return orc_compute_force_md(c);
 }
 
-/* cpp/active_brownian.cpp:28-37 */
-int orc_substep(orc_ctx *c, int l) {
+/* the start of substep l of the main loop (cpp/active_brownian.cpp:27-28): the substep
+ * counter the keyed draws use, and old_force = f */
+int orc_begin_substep(orc_ctx *c, int l) {
   c->l = l;
   memcpy(c->old_force, c->f, sizeof(V3) * ((size_t)c->p.n_colloid + 2));
+  return 0;
+}
+
+/* cpp/active_brownian.cpp:28-37 */
+int orc_substep(orc_ctx *c, int l) {
+  orc_begin_substep(c, l);
   if (orc_update_pos_md(c)) return -1;
   if (orc_neighbour_list_md(c)) return -1;
   if (orc_update_pos_mpcd(c)) return -1;
@@ -825,6 +832,13 @@ int orc_get_binning(const orc_ctx *c, int kind, int32_t *cell_of, int32_t *occup
 }
 
 void orc_get_shift(const orc_ctx *c, double *rr3) { rr3[0] = c->last_rr.x; rr3[1] = c->last_rr.y; rr3[2] = c->last_rr.z; }
+
+int orc_get_neighbour_md(const orc_ctx *c, int i, int32_t *out, int cap) {
+  if (i < 1 || i > c->p.n_colloid) return -1;
+  const ilist *l = &c->neighbour[i];
+  for (int k = 0; k < l->n && k < cap; ++k) out[k] = l->v[k];
+  return l->n;
+}
 
 int orc_get_neigh_fl(const orc_ctx *c, int j, int32_t *out, int cap) {
   if (j < 1 || j > c->p.n_colloid) return -1;

@@ -90,9 +90,11 @@ int orc_updown_velocity(orc_ctx *c, double *vel_out /* 3*Nc */, double *up_vel_o
 int orc_updown_sums(orc_ctx *c, int *cnt, int *up_cnt, double *vel_sum, double *up_vel_sum);
 
 /* driver pieces (cpp/active_brownian.cpp) */
-int orc_setup(orc_ctx *c);       /* create_box, neighbour_list_mpcd, neighbour_list_md, compute_force_md (:93-96) */
-int orc_substep(orc_ctx *c, int l); /* one pass of the inner loop body (:104-113); sets substep counter l */
-int orc_step(orc_ctx *c);        /* nn += 1; rotation_mpcd, run, n_sub substeps (:99-114) */
+int orc_setup(orc_ctx *c);       /* create_box, neighbour_list_mpcd, neighbour_list_md, compute_force_md (:17-20) */
+int orc_substep(orc_ctx *c, int l); /* one pass of the inner loop body (:28-37); sets substep counter l */
+int orc_begin_substep(orc_ctx *c, int l); /* what the loop does before update_pos_md (:27-28): substep
+                                             counter l, old_force = f */
+int orc_step(orc_ctx *c);        /* nn += 1; rotation_mpcd, run, n_sub substeps (:23-38) */
 int orc_run_steps(orc_ctx *c, int nsteps);
 
 /* step counter nn (the reference's global, 1-based inside a step) */
@@ -118,6 +120,9 @@ double orc_potential(const orc_ctx *c);
 int orc_get_binning(const orc_ctx *c, int kind, int32_t *cell_of, int32_t *occupancy);
 /* the last grid shift used by rotation_mpcd */
 void orc_get_shift(const orc_ctx *c, double *rr3);
+/* the colloid pair list of the last neighbour_list_md: partners (1-based, ascending, all > i)
+ * of colloid i (1-based); returns the count, writes up to cap */
+int orc_get_neighbour_md(const orc_ctx *c, int i, int32_t *out, int cap);
 /* neigh_fl of colloid j (1-based): returns count, writes up to cap particle ids (1-based) */
 int orc_get_neigh_fl(const orc_ctx *c, int j, int32_t *out, int cap);
 /* the 342-cell neighbour table of box b (1-based) in reference order; returns count */

@@ -58,6 +58,8 @@ def lib():
             getattr(L, name).argtypes = [vp]
             getattr(L, name).restype = C.c_int
         L.orc_substep.argtypes = [vp, C.c_int]
+        L.orc_begin_substep.argtypes = [vp, C.c_int]
+        L.orc_get_neighbour_md.argtypes = [vp, C.c_int, C.POINTER(C.c_int32), C.c_int]
         L.orc_run_steps.argtypes = [vp, C.c_int]
         L.orc_get_step.argtypes = [vp]
         L.orc_set_step.argtypes = [vp, C.c_int]
@@ -145,6 +147,19 @@ class Oracle:
 
     def substep(self, l):
         self._call("substep", l)
+
+    def begin_substep(self, l):
+        """substep counter l and old_force = f, what main does before update_pos_md"""
+        self._call("begin_substep", l)
+
+    def neighbour_md(self):
+        """per colloid (0-based), its partners j > i of the last neighbour_list_md, 0-based"""
+        out = []
+        buf = np.zeros(max(self.Nc, 1), dtype=np.int32)
+        for i in range(1, self.Nc + 1):
+            n = lib().orc_get_neighbour_md(self.h, i, _ip(buf), buf.size)
+            out.append(buf[:n].copy() - 1)
+        return out
 
     def run_steps(self, n):
         self._call("run_steps", n)
