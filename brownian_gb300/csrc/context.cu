@@ -70,6 +70,7 @@ struct mpcd_ctx {
   std::map<std::string, std::pair<int64_t, double>> prof;
   StepState *ss_host = nullptr;  // pinned
   double *insw_n = nullptr, *sqcs_n = nullptr;
+  float *sq3kt_n32 = nullptr;
   double *part = nullptr;        // reduction partials
   int part_blocks = 256;
   double *staging = nullptr;     // AoS transfer buffer, allocated on first use
@@ -196,7 +197,7 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
     cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
   }
   launch(c, name, f32 ? stream_kernel32(flags) : stream_kernel(flags),
-         blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread() : stream64_per_thread(flags))), 256, c->S, l, fb);
+         blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread(flags) : stream64_per_thread(flags))), 256, c->S, l, fb);
   if (!f32 && (flags & F_PIPE) && (flags & F_BINROT)) launch(c, "k_bin", k_bin, c->n_sm * 8, 256, c->S, fb);
   if (fork) {
     launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act);
@@ -573,6 +574,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.insw_n = c->insw_n;
   c->sqcs_n = m.get<double>(S.max_per_cell + 1);
   S.sqcs_n = c->sqcs_n;
+  c->sq3kt_n32 = m.get<float>(S.max_per_cell + 1);
+  S.sq3kt_n32 = c->sq3kt_n32;
   c->part = m.get<double>((size_t)c->part_blocks * 8);
   if (m.err != cudaSuccess) {
     std::string e = cudaGetErrorString(m.err);
@@ -581,12 +584,15 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     return m.err == cudaErrorMemoryAllocation ? MPCD_ERR_NOMEM : MPCD_ERR_CUDA;
   }
   std::vector<double> insw(S.max_per_cell + 1, 0.0), sqcs(S.max_per_cell + 1, 0.0);
+  std::vector<float> sq32(S.max_per_cell + 1, 0.f);
   for (int n = 1; n <= S.max_per_cell; ++n) {
     insw[n] = ldexp(1.0 / n, -S.kw);
     sqcs[n] = sqrt(S.cs * (double)(n - 1));
+    sq32[n] = (float)sqrt(3.0 * p.kbt * (double)(n - 1) / p.mass_fl);
   }
   scopy(c, c->insw_n, insw.data(), sizeof(double) * insw.size(), cudaMemcpyHostToDevice);
   scopy(c, c->sqcs_n, sqcs.data(), sizeof(double) * sqcs.size(), cudaMemcpyHostToDevice);
+  scopy(c, c->sq3kt_n32, sq32.data(), sizeof(float) * sq32.size(), cudaMemcpyHostToDevice);
   if (cudaMallocHost(&c->ss_host, sizeof(StepState)) != cudaSuccess) {
     m.release();
     delete c;

@@ -50,16 +50,20 @@ static __device__ __forceinline__ int cell_of_pos(const SysF64 &S, double x, dou
 // global atomic per block (the whole block must call it): for the run() records
 // of a last substep, about one particle in sixteen, too many for one atomic per
 // warp on a single counter.
-static __device__ __forceinline__ int block_base(int *counter, unsigned m, int lane) {
+static __device__ __forceinline__ int block_base_n(int *counter, int warp_count, int lane) {
   __shared__ int s_tot, s_base;
   if (threadIdx.x == 0) s_tot = 0;
   __syncthreads();
   int off = 0;
-  if (lane == 0 && m) off = atomicAdd(&s_tot, __popc(m));
+  if (lane == 0 && warp_count) off = atomicAdd(&s_tot, warp_count);
   __syncthreads();
   if (threadIdx.x == 0) s_base = s_tot ? atomicAdd(counter, s_tot) : 0;
   __syncthreads();
   return s_base + __shfl_sync(FULL, off, 0);
+}
+
+static __device__ __forceinline__ int block_base(int *counter, unsigned m, int lane) {
+  return block_base_n(counter, __popc(m), lane);
 }
 
 // Batched launches: block b of a launch over nrep systems belongs to the system r
@@ -107,6 +111,47 @@ static __device__ __forceinline__ void tappend(unsigned long long *Tc, uint16_t 
   const int slot = (int)(unsigned)atomicAdd(&Tc[cell], 1ull);
   if (slot < TCAP) Tl[(size_t)cell * TCAP + slot] = (uint16_t)j;
   else atomicOr(err, ERRB_TTABLE);
+}
+
+// --------------------------------------------------------------- exact cell sums
+
+// one particle's terms of the exact cell sums (count, fixed-point w or v, |w|^2)
+static __device__ __forceinline__ void bin_add(CellAcc *a, int n, long long fx, long long fy, long long fz,
+                                               long long f2) {
+  atomicAdd(&a->n, n);
+  atomicAdd((unsigned long long *)&a->sx, (unsigned long long)fx);
+  atomicAdd((unsigned long long *)&a->sy, (unsigned long long)fy);
+  atomicAdd((unsigned long long *)&a->sz, (unsigned long long)fz);
+  atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
+}
+
+// The same for one particle per lane (cell c < 0: none), the whole warp calling: lanes of
+// equal cell (__match_any_sync) gather their terms onto the group's first lane, which
+// adds them with one set of atomics.  The gathering jumps pointers along the group
+// (each lane's next higher lane of its cell): after round r a lane holds the sum of
+// itself and its next 2^r - 1 group members, so ceil(log2(size)) rounds leave the total
+// on the first lane.  The sums are integers, so the result does not depend on the order.
+static __device__ __forceinline__ void bin_add_warp(CellAcc *acc, int c, long long fx, long long fy, long long fz,
+                                                    long long f2) {
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
+  const unsigned above = peers & ~((2u << lane) - 1u);
+  int nxt = above ? __ffs(above) - 1 : -1;
+  unsigned long long sx = (unsigned long long)fx, sy = (unsigned long long)fy, sz = (unsigned long long)fz,
+                     s2 = (unsigned long long)f2;
+  int n = c >= 0 ? 1 : 0;
+  while (__any_sync(0xFFFFFFFFu, nxt >= 0)) {
+    const int src = nxt >= 0 ? nxt : lane;
+    const unsigned long long ax = __shfl_sync(0xFFFFFFFFu, sx, src), ay = __shfl_sync(0xFFFFFFFFu, sy, src),
+                             az = __shfl_sync(0xFFFFFFFFu, sz, src), a2 = __shfl_sync(0xFFFFFFFFu, s2, src);
+    const int an = __shfl_sync(0xFFFFFFFFu, n, src), anx = __shfl_sync(0xFFFFFFFFu, nxt, src);
+    if (nxt >= 0) {
+      sx += ax; sy += ay; sz += az; s2 += a2;
+      n += an;
+      nxt = anx;
+    }
+  }
+  if (c >= 0 && lane == __ffs(peers) - 1) bin_add(acc + c, n, (long long)sx, (long long)sy, (long long)sz, (long long)s2);
 }
 
 // FP32 copy of a double by truncating the mantissa (integer pipe); relative

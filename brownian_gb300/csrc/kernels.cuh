@@ -29,7 +29,7 @@ __global__ void k_scan_blocks_b(const SysF64 *Ss, const int *boff, int nrep, int
 __global__ void k_gather_err(const SysF64 *Ss, int nrep, int *out);
 // FP32-compensated form (kernels_fp32c.cu)
 StreamKernel stream_kernel32(int flags);
-int stream32_per_thread();  // particles per thread of the FP32 streaming pass
+int stream32_per_thread(int flags);  // particles per thread of the FP32 streaming pass
 int stream64_per_thread(int flags);  // particles per thread of the FP64 streaming pass
 __global__ void k_bin(const SysF64 S, int fb);
 __global__ void k_updown_table(const SysF64 S, unsigned long long *Tc, uint16_t *Tl, long long epoch, float reach);

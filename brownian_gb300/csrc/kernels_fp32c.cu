@@ -73,11 +73,35 @@ __device__ __forceinline__ long long to_fix_f(float v, int k) {
   return (b >> 31) ? -r : r;
 }
 
-// the exact sums of the SRD binning for the next step (rotation_mpcd bins by the
-// shifted position: cell + floor(offset + rr) per axis)
-__device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, int cz, float ox, float oy, float oz,
-                                      float vx, float vy, float vz) {
-  const float *rr = S.ss->rrf;
+// one particle's part of the SRD binning for the next step (rotation_mpcd bins by the
+// shifted position: cell + floor(offset + rr) per axis): its cell (recorded in rotcell)
+// and the fixed-point v and |v|^2 the exact cell sums add up
+struct BinTerm32 {
+  int c;
+  long long fx, fy, fz, f2;
+};
+
+// round(v^2 2^k) from the significand m of v (24 bits, so m^2 is exact in 64 bits):
+// v^2 2^k = m^2 2^(2 (e - 150) + k); the same value as sq_fix of to_fix_f(v, k) whenever
+// v 2^k is an integer (every |v| >= 2^(23 - k)), and within one unit below that
+__device__ __forceinline__ long long sq_fix_f(float v, int k) {
+  const unsigned b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xFF);
+  if (e == 0) return 0;
+  const unsigned m = (b & 0x7FFFFFu) | 0x800000u;
+  const unsigned long long q = (unsigned long long)m * m;
+  const int sh = 2 * (e - 150) + k;
+  if (sh >= 0) return (long long)(q << (sh < 16 ? sh : 16));
+  if (sh <= -63) return 0;
+  const int s = -sh;
+  unsigned long long r = q >> s;
+  const unsigned long long rem = q & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+  if (rem > half || (rem == half && (r & 1ull))) r += 1ull;
+  return (long long)r;
+}
+
+__device__ __forceinline__ BinTerm32 bin32_term(const SysF64 &S, const float *rr, int p, int cx, int cy, int cz,
+                                                float ox, float oy, float oz, float vx, float vy, float vz) {
   float tx = ox + rr[0], ty = oy + rr[1], tz = oz + rr[2];
   int bx = cx + (tx < 0.f ? -1 : (tx >= 1.f ? 1 : 0));
   int by = cy + (ty < 0.f ? -1 : (ty >= 1.f ? 1 : 0));
@@ -88,141 +112,18 @@ __device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, in
   const int c = bx + S.Lx * (by + S.Ly * bz);
   S.rotcell[p] = c;
   if (!(fabsf(vx) <= S.vmaxf && fabsf(vy) <= S.vmaxf && fabsf(vz) <= S.vmaxf)) atomicOr(&S.ss->err, ERRB_VRANGE);
-  long long fx = to_fix_f(vx, S.kw), fy = to_fix_f(vy, S.kw), fz = to_fix_f(vz, S.kw);
-  long long f2 = sq_fix(fx, S.kw) + sq_fix(fy, S.kw) + sq_fix(fz, S.kw);
-  CellAcc *a = S.acc + c;
-  atomicAdd(&a->n, 1);
-  atomicAdd((unsigned long long *)&a->sx, (unsigned long long)fx);
-  atomicAdd((unsigned long long *)&a->sy, (unsigned long long)fy);
-  atomicAdd((unsigned long long *)&a->sz, (unsigned long long)fz);
-  atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
+  BinTerm32 t;
+  t.c = c;
+  t.fx = to_fix_f(vx, S.kw); t.fy = to_fix_f(vy, S.kw); t.fz = to_fix_f(vz, S.kw);
+  t.f2 = sq_fix_f(vx, S.kw) + sq_fix_f(vy, S.kw) + sq_fix_f(vz, S.kw);
+  return t;
 }
 
-// STREAM32_U particles per thread (thread t of block b: particles b * 256 U + t +
-// 256 u), their loads issued together so more memory requests are in flight
-#ifndef STREAM32_U
-#define STREAM32_U 2
-#endif
-template <int FLAGS>
-static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
-  constexpr int flags = FLAGS;
-  constexpr int U = STREAM32_U;
-  const long long step = S.ss->step;
-  const long long gs = step * S.n_sub + (l - 1);
-  const Fluid32 F = fluid32_at(S, fb);
-  const int p0 = VB * (256 * U) + threadIdx.x;
-  const int buf = (int)(gs & 1);
-  int cx[U], cy[U], cz[U];
-  float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
-  bool valid[U], ev[U];
-  unsigned members[U];
-  int cnt[U], lin[U];
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
-    valid[u] = p < S.N;
-    ev[u] = false;
-    members[u] = 0;
-    cnt[u] = 0;
-    lin[u] = 0;
-    if (valid[u]) {
-      unpack(F.q[p], cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
-      vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    if (!valid[u]) continue;
-    if (flags & F_STREAM) {
-      ox[u] = fmaf(vx[u], S.dtf, ox[u]); oy[u] = fmaf(vy[u], S.dtf, oy[u]); oz[u] = fmaf(vz[u], S.dtf, oz[u]);
-      carry(cx[u], ox[u], S.Lx); carry(cy[u], oy[u], S.Ly); carry(cz[u], oz[u], S.Lz);
-    }
-    lin[u] = cx[u] + S.Lx * (cy[u] + S.Ly * cz[u]);
-    if (flags & (F_COLLIDE | F_SHELL)) cnt[u] = tcount(S.Tcnt[buf][lin[u]], gs);
-  }
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    if (!valid[u]) continue;
-    if ((flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
-      cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
-      const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
-      const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
-      const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
-      for (int k = 0; k < cnt[u]; ++k) {
-        const int j = lst[k];
-        const float4 cq = Xq[j], co = Xo[j];
-        const float dx = rel(cx[u], ox[u], cq.x, co.x, S.Lx), dy = rel(cy[u], oy[u], cq.y, co.y, S.Ly),
-                    dz = rel(cz[u], oz[u], cq.z, co.z, S.Lz);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (flags & F_COLLIDE) ev[u] |= d2 <= rc2;
-        if ((flags & F_SHELL) && d2 <= rs2) members[u] |= 1u << k;
-      }
-    }
-    const int p = p0 + 256 * u;
-    if (!ev[u] && (flags & F_BINROT)) bin32(S, p, cx[u], cy[u], cz[u], ox[u], oy[u], oz[u], vx[u], vy[u], vz[u]);
-    if (flags & F_STREAM) F.q[p] = pack(cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
-  }
-  // appends: events one atomic per warp (no block barrier), run() candidate
-  // records (last substep) one atomic per block
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
-    const bool has_rec = (flags & F_SHELL) && valid[u] && !ev[u] && members[u] != 0;
-    const unsigned mev = __ballot_sync(FULL, ev[u]), mrec = __ballot_sync(FULL, has_rec);
-    int bev = 0, brec = 0;
-    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
-    bev = __shfl_sync(FULL, bev, 0);
-    if (flags & F_SHELL) brec = block_base(&S.ss->nshell, mrec, lane);
-    if (ev[u]) {
-      const int i = bev + __popc(mev & lt);
-      if (i < S.events_cap) S.events[i] = p;
-      else atomicOr(&S.ss->err, ERRB_EVENTS);
-    }
-    if (has_rec) {
-      const int i = brec + __popc(mrec & lt);
-      if (i < S.shell_cap) {
-        // colloids in ascending index, the order run() visits them
-        const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
-        ShellRec *r = S.shell + i;
-        r->p = F.id[p];
-        r->pass = 0;
-        int n = 0, last = -1;
-        for (int it = 0; it < cnt[u] && n < SHELL_J; ++it) {
-          int best = 0x7FFFFFFF;
-          for (int k = 0; k < cnt[u]; ++k) {
-            const int j = lst[k];
-            if (((members[u] >> k) & 1u) && j > last && j < best) best = j;
-          }
-          if (best == 0x7FFFFFFF) break;
-          r->j[n++] = (uint16_t)best;
-          last = best;
-        }
-        if (__popc(members[u]) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
-        r->n = (uint8_t)n;
-      } else {
-        atomicOr(&S.ss->err, ERRB_SHELL);
-      }
-    }
-  }
+__device__ __forceinline__ void bin32(const SysF64 &S, int p, int cx, int cy, int cz, float ox, float oy, float oz,
+                                      float vx, float vy, float vz) {
+  const BinTerm32 t = bin32_term(S, S.ss->rrf, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+  bin_add(S.acc + t.c, 1, t.fx, t.fy, t.fz, t.f2);
 }
-
-template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream32(__grid_constant__ const SysF64 S, int l, int fb) {
-  k_stream32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
-}
-
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
-template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
-  __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_stream32_body<FLAGS>(sS, VB, NVB, l, fb);
-}
-
-int stream32_per_thread() { return STREAM32_U; }
 
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 fm(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
@@ -268,6 +169,250 @@ __device__ f3 reflect32(const SysF64 &S, uint32_t a, uint32_t b, uint32_t t, f3 
   return res;
 }
 
+// One warp's wall collisions (cpp/fluid_colloid_collision.cpp:26-49) of the particles its
+// lanes hold (act: the lane has one): each lane takes its colloids in ascending order, the
+// ones whose sphere holds the particle, and the body of a collision (back half a substep,
+// the FP32 stochastic reflection, the exact exchange sums, forward half a substep) runs
+// once for all lanes that hit a colloid at that rank.  The whole warp calls it.
+template <int FLAGS>
+__device__ __forceinline__ void collide32_warp(const SysF64 &S, long long gs, int buf, bool act, int id, int cnt,
+                                               const uint16_t *lst, int &cx, int &cy, int &cz, float &ox, float &oy,
+                                               float &oz, float &vx, float &vy, float &vz) {
+  const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+  const float rc2 = S.r_coll * S.r_coll;
+  const f3 vdump = fm(vx, vy, vz);
+  bool more = act;
+  int last = -1;
+  while (__any_sync(FULL, more)) {
+    int j = 0x7FFFFFFF;
+    float4 cq = make_float4(0.f, 0.f, 0.f, 0.f), co = cq;
+    if (more) {
+      for (;;) {
+        j = 0x7FFFFFFF;
+        for (int k = 0; k < cnt; ++k) {
+          int c = lst[k];
+          if (c > last && c < j) j = c;
+        }
+        if (j == 0x7FFFFFFF) break;
+        last = j;
+        cq = Xq[j]; co = Xo[j];
+        f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+        if (r.x * r.x + r.y * r.y + r.z * r.z <= rc2) break;
+      }
+      more = j != 0x7FFFFFFF;
+    }
+    __syncwarp();
+    if (j == 0x7FFFFFFF) continue;
+    // back half a substep, reflect, forward half a substep
+    ox -= 0.5f * vx * S.dtf; oy -= 0.5f * vy * S.dtf; oz -= 0.5f * vz * S.dtf;
+    carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+    f3 rs = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
+    f3 rf = fm((float)cx + ox, (float)cy + oy, (float)cz + oz);
+    f3 u = reflect32(S, (uint32_t)(id + 1), (uint32_t)(j + 1), (uint32_t)gs, rf, rs);
+    f3 V = fm((float)S.V[3 * j], (float)S.V[3 * j + 1], (float)S.V[3 * j + 2]);
+    f3 W = fm((float)S.W[3 * j], (float)S.W[3 * j + 1], (float)S.W[3 * j + 2]);
+    f3 wr = fcross(W, rs);
+    vx = u.x + V.x + wr.x; vy = u.y + V.y + wr.y; vz = u.z + V.z + wr.z;
+    f3 dv = fm(vdump.x - vx, vdump.y - vy, vdump.z - vz);
+    f3 dl = fcross(rs, dv);
+    exch_add6(S.exch + j, mk(dv.x, dv.y, dv.z), mk(dl.x, dl.y, dl.z), &S.ss->err);
+    ox += 0.5f * vx * S.dtf; oy += 0.5f * vy * S.dtf; oz += 0.5f * vz * S.dtf;
+    carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+  }
+}
+
+// A particle after its wall collisions: the displacement check against the cell-table
+// margin, on the last substep its run() record and its binning (from its state after
+// the collisions), and its state written back.
+template <int FLAGS>
+__device__ __forceinline__ void finish32(const SysF64 &S, const Fluid32 &F, int p, int id, int buf, int cnt,
+                                         const uint16_t *lst, int cx0, int cy0, int cz0, float ox0, float oy0,
+                                         float oz0, int cx, int cy, int cz, float ox, float oy, float oz, float vx,
+                                         float vy, float vz) {
+  constexpr int flags = FLAGS;
+  {
+    // the cell table is built with a margin; a move beyond it could hide a colloid
+    const float ex = rel(cx, ox, (float)cx0, ox0, S.Lx), ey = rel(cy, oy, (float)cy0, oy0, S.Ly),
+                ez = rel(cz, oz, (float)cz0, oz0, S.Lz);
+    if (ex * ex + ey * ey + ez * ez > (float)S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
+  }
+  if (flags & F_SHELL) {
+    const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+    const float rs2 = S.r_shell * S.r_shell;
+    ShellRec rec;
+    rec.p = id;
+    rec.n = 0;
+    rec.pass = 0;
+    for (int last = -1; rec.n < SHELL_J;) {
+      int j = 0x7FFFFFFF;
+      for (int k = 0; k < cnt; ++k) {
+        int c = lst[k];
+        if (c > last && c < j) j = c;
+      }
+      if (j == 0x7FFFFFFF) break;
+      last = j;
+      float4 cq = Xq[j], co = Xo[j];
+      float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly), dz = rel(cz, oz, cq.z, co.z, S.Lz);
+      if (dx * dx + dy * dy + dz * dz <= rs2) rec.j[rec.n++] = (uint16_t)j;
+    }
+    if (rec.n) {
+      int idx = atomicAdd(&S.ss->nshell, 1);
+      if (idx < S.shell_cap) S.shell[idx] = rec;
+      else atomicOr(&S.ss->err, ERRB_SHELL);
+    }
+  }
+  if (flags & F_BINROT) bin32(S, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+  F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+  F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+}
+
+// STREAM32_U particles per thread (thread t of block b: particles b * 256 U + t +
+// 256 u), their loads issued together so more memory requests are in flight
+#ifndef STREAM32_U
+#define STREAM32_U 2
+#endif
+// the pass that also records run() candidates and bins keeps one particle per thread
+// (its register count, and so its occupancy)
+#ifndef STREAM32_U_SHELL
+#define STREAM32_U_SHELL 1
+#endif
+static constexpr __host__ __device__ int stream32_u(int flags) { return (flags & F_SHELL) ? STREAM32_U_SHELL : STREAM32_U; }
+template <int FLAGS>
+static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
+  constexpr int flags = FLAGS;
+  constexpr int U = stream32_u(FLAGS);
+  const long long step = S.ss->step;
+  const long long gs = step * S.n_sub + (l - 1);
+  const Fluid32 F = fluid32_at(S, fb);
+  const int p0 = VB * (256 * U) + threadIdx.x;
+  const int buf = (int)(gs & 1);
+  int cx[U], cy[U], cz[U];
+  float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
+  bool valid[U], ev[U];
+  unsigned members[U];
+  int cnt[U], lin[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    valid[u] = p < S.N;
+    ev[u] = false;
+    members[u] = 0;
+    cnt[u] = 0;
+    lin[u] = 0;
+    if (valid[u]) {
+      unpack(F.q[p], cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
+      vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
+    if (flags & F_STREAM) {
+      ox[u] = fmaf(vx[u], S.dtf, ox[u]); oy[u] = fmaf(vy[u], S.dtf, oy[u]); oz[u] = fmaf(vz[u], S.dtf, oz[u]);
+      carry(cx[u], ox[u], S.Lx); carry(cy[u], oy[u], S.Ly); carry(cz[u], oz[u], S.Lz);
+    }
+    lin[u] = cx[u] + S.Lx * (cy[u] + S.Ly * cz[u]);
+    if (flags & (F_COLLIDE | F_SHELL)) cnt[u] = tcount(S.Tcnt[buf][lin[u]], gs);
+  }
+  float rr[3] = {0.f, 0.f, 0.f};
+  if (flags & F_BINROT)
+    for (int k = 0; k < 3; ++k) rr[k] = S.ss->rrf[k];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    BinTerm32 bt{-1, 0, 0, 0, 0};
+    if (valid[u] && (flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
+      cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
+      const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+      const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+      const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
+      for (int k = 0; k < cnt[u]; ++k) {
+        const int j = lst[k];
+        const float4 cq = Xq[j], co = Xo[j];
+        const float dx = rel(cx[u], ox[u], cq.x, co.x, S.Lx), dy = rel(cy[u], oy[u], cq.y, co.y, S.Ly),
+                    dz = rel(cz[u], oz[u], cq.z, co.z, S.Lz);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (flags & F_COLLIDE) ev[u] |= d2 <= rc2;
+        if ((flags & F_SHELL) && d2 <= rs2) members[u] |= 1u << k;
+      }
+    }
+    const int p = p0 + 256 * u;
+    if (valid[u] && !ev[u] && (flags & F_BINROT))
+      bt = bin32_term(S, rr, p, cx[u], cy[u], cz[u], ox[u], oy[u], oz[u], vx[u], vy[u], vz[u]);
+    if (flags & F_BINROT) bin_add_warp(S.acc, bt.c, bt.fx, bt.fy, bt.fz, bt.f2);  // the whole warp
+    if (valid[u] && (flags & F_STREAM)) F.q[p] = pack(cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
+  }
+  // appends: events one atomic per warp (no block barrier), run() candidate
+  // records (last substep) one atomic per block for all U rounds
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned mrecs[U];
+  int nrec = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    mrecs[u] = __ballot_sync(FULL, (flags & F_SHELL) && valid[u] && !ev[u] && members[u] != 0);
+    nrec += __popc(mrecs[u]);
+  }
+  int brec = 0;
+  if (flags & F_SHELL) brec = block_base_n(&S.ss->nshell, nrec, lane);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int p = p0 + 256 * u;
+    const unsigned mrec = mrecs[u];
+    const bool has_rec = (mrec >> lane) & 1u;
+    const unsigned mev = __ballot_sync(FULL, ev[u]);
+    int bev = 0;
+    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
+    bev = __shfl_sync(FULL, bev, 0);
+    if (ev[u]) {
+      const int i = bev + __popc(mev & lt);
+      if (i < S.events_cap) S.events[i] = p;
+      else atomicOr(&S.ss->err, ERRB_EVENTS);
+    }
+    if (has_rec) {
+      const int i = brec + __popc(mrec & lt);
+      if (i < S.shell_cap) {
+        // colloids in ascending index, the order run() visits them
+        const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
+        ShellRec *r = S.shell + i;
+        r->p = F.id[p];
+        r->pass = 0;
+        int n = 0, last = -1;
+        for (int it = 0; it < cnt[u] && n < SHELL_J; ++it) {
+          int best = 0x7FFFFFFF;
+          for (int k = 0; k < cnt[u]; ++k) {
+            const int j = lst[k];
+            if (((members[u] >> k) & 1u) && j > last && j < best) best = j;
+          }
+          if (best == 0x7FFFFFFF) break;
+          r->j[n++] = (uint16_t)best;
+          last = best;
+        }
+        if (__popc(members[u]) > SHELL_J) atomicOr(&S.ss->err, ERRB_SHELLSLOTS);
+        r->n = (uint8_t)n;
+      } else {
+        atomicOr(&S.ss->err, ERRB_SHELL);
+      }
+    }
+    brec += __popc(mrec);
+  }
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32(__grid_constant__ const SysF64 S, int l, int fb) {
+  k_stream32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
+}
+
+// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
+  __shared__ SysF64 sS;
+  int VB, NVB;
+  batch_locate(Ss, boff, nrep, sS, VB, NVB);
+  k_stream32_body<FLAGS>(sS, VB, NVB, l, fb);
+}
+
+int stream32_per_thread(int flags) { return stream32_u(flags); }
+
 // wall collisions of the listed particles in colloid order, then (last substep)
 // their run() record and binning; one particle per lane
 template <int FLAGS>
@@ -277,14 +422,7 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
   const long long gs = step * S.n_sub + (l - 1);
   const int buf = (int)(gs & 1);
   const Fluid32 F = fluid32_at(S, fb);
-  const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
   const int n = min(S.ss->nevents, S.events_cap);
-  const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
-  // event i goes to block i % NVB and, within it, to warp (i / NVB) % warps: the
-  // few hundred to few thousand events of a substep spread over all SMs and over
-  // each SM's four schedulers instead of filling the first few
-  // (a warp-uniform trip count and collision loop, as the FP64 form: the body of a
-  // collision runs once for all lanes of a warp that hit a colloid at that rank)
   const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   for (int base = 0;; base += blockDim.x) {
     const int i = VB + NVB * (k0 + base);
@@ -305,84 +443,11 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
       cnt = cnt < TCAP ? cnt : TCAP;
     }
     const uint16_t *lst = S.Tlist[buf] + (size_t)lin * TCAP;
-    const f3 vdump = fm(vx, vy, vz);
     const int cx0 = cx, cy0 = cy, cz0 = cz;
     const float ox0 = ox, oy0 = oy, oz0 = oz;
-    if (flags & F_COLLIDE) {
-      bool more = valid;
-      int last = -1;
-      while (__any_sync(FULL, more)) {
-        // each lane's next colloid, in ascending order, whose sphere holds the
-        // particle; then all lanes meet before the collision body
-        int j = 0x7FFFFFFF;
-        float4 cq = make_float4(0.f, 0.f, 0.f, 0.f), co = cq;
-        if (more) {
-          for (;;) {
-            j = 0x7FFFFFFF;
-            for (int k = 0; k < cnt; ++k) {
-              int c = lst[k];
-              if (c > last && c < j) j = c;
-            }
-            if (j == 0x7FFFFFFF) break;
-            last = j;
-            cq = Xq[j]; co = Xo[j];
-            f3 r = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
-            if (r.x * r.x + r.y * r.y + r.z * r.z <= rc2) break;
-          }
-          more = j != 0x7FFFFFFF;
-        }
-        __syncwarp();
-        if (j == 0x7FFFFFFF) continue;
-        // back half a substep, reflect, forward half a substep
-        ox -= 0.5f * vx * S.dtf; oy -= 0.5f * vy * S.dtf; oz -= 0.5f * vz * S.dtf;
-        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
-        f3 rs = fm(rel(cx, ox, cq.x, co.x, S.Lx), rel(cy, oy, cq.y, co.y, S.Ly), rel(cz, oz, cq.z, co.z, S.Lz));
-        f3 rf = fm((float)cx + ox, (float)cy + oy, (float)cz + oz);
-        f3 u = reflect32(S, (uint32_t)(id + 1), (uint32_t)(j + 1), (uint32_t)gs, rf, rs);
-        f3 V = fm((float)S.V[3 * j], (float)S.V[3 * j + 1], (float)S.V[3 * j + 2]);
-        f3 W = fm((float)S.W[3 * j], (float)S.W[3 * j + 1], (float)S.W[3 * j + 2]);
-        f3 wr = fcross(W, rs);
-        vx = u.x + V.x + wr.x; vy = u.y + V.y + wr.y; vz = u.z + V.z + wr.z;
-        f3 dv = fm(vdump.x - vx, vdump.y - vy, vdump.z - vz);
-        f3 dl = fcross(rs, dv);
-        exch_add6(S.exch + j, mk(dv.x, dv.y, dv.z), mk(dl.x, dl.y, dl.z), &S.ss->err);
-        ox += 0.5f * vx * S.dtf; oy += 0.5f * vy * S.dtf; oz += 0.5f * vz * S.dtf;
-        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
-      }
-    }
+    if (flags & F_COLLIDE) collide32_warp<FLAGS>(S, gs, buf, valid, id, cnt, lst, cx, cy, cz, ox, oy, oz, vx, vy, vz);
     if (!valid) continue;
-    {
-      // the cell table is built with a margin; a move beyond it could hide a colloid
-      const float ex = rel(cx, ox, (float)cx0, ox0, S.Lx), ey = rel(cy, oy, (float)cy0, oy0, S.Ly),
-                  ez = rel(cz, oz, (float)cz0, oz0, S.Lz);
-      if (ex * ex + ey * ey + ez * ez > (float)S.disp_margin2) atomicOr(&S.ss->err, ERRB_DISPLACE);
-    }
-    if (flags & F_SHELL) {
-      ShellRec rec;
-      rec.p = id;
-      rec.n = 0;
-      rec.pass = 0;
-      for (int last = -1; rec.n < SHELL_J;) {
-        int j = 0x7FFFFFFF;
-        for (int k = 0; k < cnt; ++k) {
-          int c = lst[k];
-          if (c > last && c < j) j = c;
-        }
-        if (j == 0x7FFFFFFF) break;
-        last = j;
-        float4 cq = Xq[j], co = Xo[j];
-        float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly), dz = rel(cz, oz, cq.z, co.z, S.Lz);
-        if (dx * dx + dy * dy + dz * dz <= rs2) rec.j[rec.n++] = (uint16_t)j;
-      }
-      if (rec.n) {
-        int idx = atomicAdd(&S.ss->nshell, 1);
-        if (idx < S.shell_cap) S.shell[idx] = rec;
-        else atomicOr(&S.ss->err, ERRB_SHELL);
-      }
-    }
-    if (flags & F_BINROT) bin32(S, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
-    F.q[p] = pack(cx, cy, cz, ox, oy, oz);
-    F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+    finish32<FLAGS>(S, F, p, id, buf, cnt, lst, cx0, cy0, cz0, ox0, oy0, oz0, cx, cy, cz, ox, oy, oz, vx, vy, vz);
   }
 }
 
@@ -466,12 +531,13 @@ static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const
     if (threadIdx.x == 0) S.blk_off[VB] = total;
   }
   if (c >= S.C) return;
-  float *ab = S.cell_ab32 + (size_t)c * 12;
+  float4 *ab4 = reinterpret_cast<float4 *>(S.cell_ab32 + (size_t)c * 12);
   const int n = a.n;
   if (n > S.max_per_cell) atomicOr(&S.ss->err, ERRB_OCCUPANCY);
   if (n <= 1 || n > S.max_per_cell) {
-    ab[0] = 1; ab[1] = 0; ab[2] = 0; ab[3] = 0; ab[4] = 1; ab[5] = 0; ab[6] = 0; ab[7] = 0; ab[8] = 1;
-    ab[9] = 0; ab[10] = 0; ab[11] = 0;
+    ab4[0] = make_float4(1.f, 0.f, 0.f, 0.f);
+    ab4[1] = make_float4(1.f, 0.f, 0.f, 0.f);
+    ab4[2] = make_float4(1.f, 0.f, 0.f, 0.f);
     return;
   }
   // mean and thermostat factor in FP64 from the exact sums
@@ -479,9 +545,10 @@ static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const
   const double insw = S.insw_n[n];
   const double ux = (double)a.sx * insw, uy = (double)a.sy * insw, uz = (double)a.sz * insw;
   const double var = (double)a.s2 * S.inv_sw - (double)n * (ux * ux + uy * uy + uz * uz);
-  // S.cs is 3 kT dt^2 / m for the displacement sums of the FP64 form; these are velocity sums:
-  // sqrt(cs (n - 1)) / dt (per n) times 1/sqrt(var), no double division or square root
-  const float s = var > 0 ? (float)(S.sqcs_n[n] * S.inv_dt * rsqrt(var)) : 1.f;
+  // The factor sqrt(3 kT (n - 1) / (m var)) scales FP32 velocities, so it is needed to FP32
+  // precision only: the variance in FP64 (from the exact sums, where the cancellation
+  // happens), its reciprocal root in FP32 times sqrt(3 kT (n - 1) / m) (per n, from the host)
+  const float s = var > 0 ? S.sq3kt_n32[n] * rsqrtf((float)var) : 1.f;
   // rotation axis rho = 2 ran - 1, phi = 2 pi ran (cpp/rotation_mpcd.cpp:19-20)
   uint4 r = draw4(S.key, DOM_AXIS, 0, (uint32_t)(c + 1), 0, (uint32_t)(S.ss->step + 1));
   const float rho = 2.f * u01f(r.x) - 1.f;
@@ -495,11 +562,15 @@ static __device__ __forceinline__ void k_cell_prep32_body(const SysF64 &S, const
                       i2 * r1 + st * r3, i2 * r2 + ct, i2 * r3 - st * r1,
                       i3 * r1 - st * r2, i3 * r2 + st * r1, i3 * r3 + ct};
   const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+  float A[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) ab[k] = s * R[k];
-  ab[9] = fx - (ab[0] * fx + ab[1] * fy + ab[2] * fz);
-  ab[10] = fy - (ab[3] * fx + ab[4] * fy + ab[5] * fz);
-  ab[11] = fz - (ab[6] * fx + ab[7] * fy + ab[8] * fz);
+  for (int k = 0; k < 9; ++k) A[k] = s * R[k];
+  const float b0 = fx - (A[0] * fx + A[1] * fy + A[2] * fz);
+  const float b1 = fy - (A[3] * fx + A[4] * fy + A[5] * fz);
+  const float b2 = fz - (A[6] * fx + A[7] * fy + A[8] * fz);
+  ab4[0] = make_float4(A[0], A[1], A[2], A[3]);
+  ab4[1] = make_float4(A[4], A[5], A[6], A[7]);
+  ab4[2] = make_float4(A[8], b0, b1, b2);
 }
 
 __global__ void __launch_bounds__(256) k_cell_prep32(__grid_constant__ const SysF64 S) {

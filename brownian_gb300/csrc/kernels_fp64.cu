@@ -48,14 +48,6 @@ __device__ __forceinline__ BinTerm bin_term(const SysF64 &S, int p, double x, do
   return t;
 }
 
-__device__ __forceinline__ void bin_add(CellAcc *a, int n, long long fx, long long fy, long long fz, long long f2) {
-  atomicAdd(&a->n, n);
-  atomicAdd((unsigned long long *)&a->sx, (unsigned long long)fx);
-  atomicAdd((unsigned long long *)&a->sy, (unsigned long long)fy);
-  atomicAdd((unsigned long long *)&a->sz, (unsigned long long)fz);
-  atomicAdd((unsigned long long *)&a->s2, (unsigned long long)f2);
-}
-
 // the exact sums of the SRD binning for the next step: cell number, count, w, |w|^2
 __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double x, double y, double z, double wx,
                                                  double wy, double wz) {
@@ -335,11 +327,16 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
 // (the pending ones are binned by the event pass): a pass of its own, so that
 // its atomics run beside that substep's event pass and colloid finish.  Pending
 // marks stay set until the next step's rotation clears them.
+// Particles sit in cell order (sorted every sort_every steps), so a warp's particles
+// fall into a few cells of the shifted grid: their terms are summed per cell across the
+// warp first (bin_add_warp), one set of atomics per cell and warp.
 __global__ void __launch_bounds__(256) k_bin(const SysF64 S, int fb) {
   const Fluid F = fluid_at(S, fb);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.N; p += gridDim.x * blockDim.x) {
-    if (S.pend[p]) continue;
-    bin_for_rotation(S, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
+  for (int base = blockIdx.x * blockDim.x; base < S.N; base += gridDim.x * blockDim.x) {
+    const int p = base + threadIdx.x;
+    BinTerm t{-1, 0, 0, 0, 0};
+    if (p < S.N && !S.pend[p]) t = bin_term(S, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
+    bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);
   }
 }
 

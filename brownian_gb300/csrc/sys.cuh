@@ -118,6 +118,7 @@ struct SysF64 {
   double *cell_ab;     // [C][12]: A (row-major 3x3), b
   const double *insw_n;  // [max_per_cell+1]: 2^-kw / n (exact scaling of 1/n), the cell mean of both forms
   const double *sqcs_n;  // [max_per_cell+1]: sqrt(cs (n - 1)), the FP64 thermostat's numerator
+  const float *sq3kt_n32;  // [max_per_cell+1]: sqrt(3 kT (n - 1) / m), the FP32 thermostat's numerator
   // colloids
   double *X[2];        // [Nc][3] double-buffered by global substep parity
   float4 *Xf[2];       // FP32 copies for prefilters
