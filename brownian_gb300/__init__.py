@@ -34,7 +34,8 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
            "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
            "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
-           "mpcd_surrogate_features", "mpcd_surrogate_outputs", "mpcd_surrogate_fast_steps", "mpcd_surrogate_step", "mpcd_updown_velocity", "mpcd_traj_create",
+           "mpcd_surrogate_features", "mpcd_surrogate_outputs", "mpcd_surrogate_fast_steps", "mpcd_surrogate_step",
+           "mpcd_surrogate_set_fault", "mpcd_updown_velocity", "mpcd_traj_create",
            "mpcd_traj_destroy", "mpcd_traj_last_error", "mpcd_traj_frames", "mpcd_traj_reset", "mpcd_traj_record",
            "mpcd_traj_record_surrogate", "mpcd_traj_analyse", "mpcd_traj_read", "mpcd_traj_write"]
 # the routines of the substep body, in the reference's order (cpp/active_brownian.cpp:28-37)

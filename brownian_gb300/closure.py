@@ -214,6 +214,7 @@ class Surrogate:
         L.mpcd_surrogate_get_state.argtypes = [vp, dp, dp, dp, dp]
         L.mpcd_surrogate_features.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
         L.mpcd_surrogate_step.argtypes = [vp, C.c_int]
+        L.mpcd_surrogate_set_fault.argtypes = [vp, C.c_int]
         self.params, self.net = params, net
         self.Nc = params.n_colloid
         h = vp()
@@ -233,6 +234,10 @@ class Surrogate:
     def set_state(self, pos, vel, ang_vel, ra):
         a = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.Nc, 3) for x in (pos, vel, ang_vel, ra)]
         self._ck(lib().mpcd_surrogate_set_state(self.h, *[self._dp(x) for x in a]))
+
+    def set_fault(self, drop_chunk=-1):
+        """test hook: the network kernel's producer skips weight chunk drop_chunk (-1: none)"""
+        self._ck(lib().mpcd_surrogate_set_fault(self.h, int(drop_chunk)))
 
     def get_state(self):
         out = {k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra")}

@@ -60,7 +60,8 @@ struct Sur {
   float4 *X, *V, *W, *ra, *f;
   float *feat;      // the last step's network inputs [Nc][81]
   float *out;       // the last step's normalised network outputs [Nc][16]
-  float4 *imp;      // per-substep linear impulse of the drawn exchange [Nc], orientation at the step's start [Nc]
+  float4 *imp;      // per-substep linear impulse of the drawn exchange [Nc], orientation at the step's start [Nc],
+                    // Omega and orientation at the step's end [Nc] [Nc] (stored by the substep kernel)
   uint16_t *fpart;  // force partners [Nc][MAXF], ascending index
   uint8_t *fpn;     // their count
   uint16_t *nbl;    // candidate neighbours [Nc][CAND] (within rlist at the last rebuild), ascending index
@@ -68,6 +69,7 @@ struct Sur {
   float4 *xref;     // positions at the last rebuild
   int *rebuild;     // a colloid moved more than half the skin since (or no lists yet)
   int *err;
+  int drop_chunk;   // fault injection for tests: the producer does not issue this weight chunk (-1: none)
   const uint4 *wpk;                   // the packed BF16 weights (k_sur_pack)
   const float *bias;                  // the network's biases [256][256][256][16]
   const float *xmean, *xistd;         // input normalisation
@@ -350,6 +352,7 @@ __device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __
 __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
   extern __shared__ __align__(128) unsigned char net_smem[];
   NetSmem &sm = *reinterpret_cast<NetSmem *>(net_smem);
+  if (*S.err & 4) return;  // a weight copy of an earlier step of this call did not arrive: no more steps
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gq = lane >> 2, q = lane & 3;
   const unsigned lt = (1u << lane) - 1u;
@@ -590,13 +593,14 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
           *ab = 1;
           break;
         }
+        if (g == S.drop_chunk) continue;  // injected fault: the consumers' bounded waits give up
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         issue_chunk(S, sm, g);
         issued = g + 1;
       }
       // every copy issued (the last one into each stage) lands before the block exits
       for (int c = issued > NSTAGE ? issued - NSTAGE : 0; c < issued; ++c)
-        mbar_wait_bounded(&sm.full[c % NSTAGE], (uint32_t)((c / NSTAGE) & 1));
+        if (c != S.drop_chunk) mbar_wait_bounded(&sm.full[c % NSTAGE], (uint32_t)((c / NSTAGE) & 1));
     }
   } else {
     // three hidden layers: compute warp w takes columns 8 TPW w .. 8 TPW (w + 1) - 1, two
@@ -745,8 +749,10 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
       const float in = rsqrtf(ax * ax + ay * ay + az * az);
       a = make_float4(ax * in, ay * in, az * in, 0.f);
     }
-    S.W[j] = w;
-    S.ra[j] = a;
+    // the step's end state of Omega and ra, which the substep kernel stores (so a step
+    // whose network failed leaves them as they were)
+    S.imp[2 * S.Nc + j] = w;
+    S.imp[3 * S.Nc + j] = a;
   }
 }
 
@@ -796,6 +802,7 @@ __device__ __forceinline__ float3 partner_forces(const Sur &S, float4 x, const f
 template <int PER>
 __global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
   extern __shared__ float4 smem[];
+  if (*S.err & 4) return;  // the network's outputs of this step are incomplete: the state stays as it was
   __shared__ unsigned s_vmax;  // the largest speed at the end (float bits, non-negative)
   const float hs = 0.5f * partner_skin(S), hs2 = hs * hs;
   uint16_t *sF = reinterpret_cast<uint16_t *>(smem + 2 * MAXC);  // [MAXC][MAXF] force partners
@@ -860,6 +867,7 @@ __global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
     if (j >= S.Nc) continue;
     const float4 x0 = S.xref[j], xs = S.X[j];
     S.X[j] = x[u]; S.V[j] = v[u]; S.f[j] = fo[u];
+    S.W[j] = S.imp[2 * S.Nc + j]; S.ra[j] = S.imp[3 * S.Nc + j];
     const float dx = wrapd(x[u].x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x[u].y - x0.y, S.L[1], S.iL[1]),
                 dz = wrapd(x[u].z - x0.z, S.L[2], S.iL[2]);
     moved |= dx * dx + dy * dy + dz * dz > S.half_skin2;
@@ -888,6 +896,7 @@ __global__ void __launch_bounds__(1024) k_sur_md1(const Sur S) {
 constexpr int MDC = 8, MD_MAXT = MAXC / MDC;
 
 __global__ void __cluster_dims__(MDC, 1, 1) __launch_bounds__(MD_MAXT) k_sur_md(const Sur S) {
+  if (*S.err & 4) return;  // the network's outputs of this step are incomplete: the state stays as it was
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ float4 smem[];
@@ -942,6 +951,7 @@ __global__ void __cluster_dims__(MDC, 1, 1) __launch_bounds__(MD_MAXT) k_sur_md(
   if (own) {
     const float4 x0 = S.xref[j], xs = S.X[j];
     S.X[j] = x; S.V[j] = v; S.f[j] = fo;
+    S.W[j] = S.imp[2 * S.Nc + j]; S.ra[j] = S.imp[3 * S.Nc + j];
     const float dx = wrapd(x.x - x0.x, S.L[0], S.iL[0]), dy = wrapd(x.y - x0.y, S.L[1], S.iL[1]),
                 dz = wrapd(x.z - x0.z, S.L[2], S.iL[2]);
     moved = (dx * dx + dy * dy + dz * dz > S.half_skin2 ? 1 : 0) | (step_moved2(S, x, xs) > hs2 ? 2 : 0);
@@ -1110,12 +1120,13 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   S.X = salloc<float4>(s, Nc); S.V = salloc<float4>(s, Nc); S.W = salloc<float4>(s, Nc);
   S.ra = salloc<float4>(s, Nc); S.f = salloc<float4>(s, Nc);
   S.feat = salloc<float>(s, Nc * NF); S.out = salloc<float>(s, Nc * OUTP);
-  S.imp = salloc<float4>(s, 2 * Nc);
+  S.imp = salloc<float4>(s, 4 * Nc);
   S.nbl = salloc<uint16_t>(s, Nc * CAND); S.nbn = salloc<int>(s, Nc);
   S.xref = salloc<float4>(s, Nc); S.rebuild = salloc<int>(s, 1);
   if (S.rebuild) cudaMemset(S.rebuild, 1, sizeof(int));  // no candidate lists yet
   S.fpart = salloc<uint16_t>(s, Nc * MAXF); S.fpn = salloc<uint8_t>(s, Nc);
   S.err = salloc<int>(s, 1);
+  S.drop_chunk = -1;
   S.fast = salloc<long long>(s, 1);
   S.vmax = salloc<float>(s, 1);
   s->wpk = salloc<uint4>(s, PACK_U4);
@@ -1232,8 +1243,22 @@ extern "C" int mpcd_surrogate_outputs(mpcd_surrogate *s, float *out) {
   return MPCD_OK;
 }
 
+extern "C" int mpcd_surrogate_set_fault(mpcd_surrogate *s, int drop_chunk) {
+  if (!s || drop_chunk < -1 || drop_chunk >= NCHUNK || (drop_chunk >= 0 && drop_chunk < NSTAGE))
+    return sfail(s, MPCD_ERR_PARAM, "drop_chunk: -1, or a weight chunk the producer loop issues");
+  s->S.drop_chunk = drop_chunk;
+  if (s->exec) {  // the kernels take the parameters by value: capture again
+    cudaGraphExecDestroy(s->exec);
+    s->exec = nullptr;
+  }
+  return MPCD_OK;
+}
+
 extern "C" int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps) {
   if (!s || nsteps < 0) return MPCD_ERR_PARAM;
+  // each call starts with the error bits clear: a failed call leaves the state as it was
+  // before its failing step, and the next call may go on from there
+  if (cudaMemsetAsync(s->S.err, 0, sizeof(int), s->stream) != cudaSuccess) return sfail(s, MPCD_ERR_CUDA, "step");
   if (nsteps > 0 && pack_weights(s) != MPCD_OK) return MPCD_ERR_CUDA;
   if (!s->exec) {
     cudaGraph_t g;

@@ -317,6 +317,13 @@ int mpcd_surrogate_step(mpcd_surrogate *s, int nsteps);
  * may miss a collision.  Colloids of the trained closure move about 0.01 per step; the
  * count rises for dynamics without drag (e.g. a network that predicts no exchange). */
 int mpcd_surrogate_fast_steps(mpcd_surrogate *s, int64_t *count);
+/* Every wait of the network kernel on its weight copies is bounded (100 ms); a copy that
+ * does not arrive makes the step fail with MPCD_ERR_CUDA ("a weight copy of the network
+ * kernel did not arrive"), the call's remaining steps are skipped and the colloid state stays
+ * as it was before the failing step; the next mpcd_surrogate_step starts afresh.  For tests of
+ * that path this hook makes the kernel's producer skip weight chunk `drop_chunk` (6..19; -1:
+ * none) so that the waits run out; the copies it does issue all land before the kernel ends. */
+int mpcd_surrogate_set_fault(mpcd_surrogate *s, int drop_chunk);
 
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their
