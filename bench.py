@@ -266,42 +266,57 @@ def measure_resident(sim, stream, precision, args, world, dist, with_clocks=True
                 step_frac=value / world * STEP_BYTES[precision] / (peak * 1e9))
 
 
-def form_statistics(steps, lag):
-    """Both precision forms from the same initial state: momentum drift, fluid
-    temperature and colloid MSD at `lag` steps (unwrapped, averaged over colloids
-    and time origins every 10 steps)."""
+def form_statistics(replicas, steps, lag=100, every=10):
+    """Both precision forms on the 64^3 workload, `replicas` independent systems each (seeds
+    100 + r, the same initial state for both forms), `steps` steps per system: per system the
+    colloid MSD at `lag` steps (unwrapped positions in a device trajectory, a frame every
+    `every` steps, averaged over colloids and time origins), the mean fluid temperature and
+    the largest momentum change relative to sum |p|.  The forms are compared through the
+    means over systems, with standard errors from the spread between systems (independent)."""
     import numpy as np
-    out = {}
+
+    import brownian_gb300 as bg
+    per = {}
     for prec in ("fp64", "fp32c"):
-        sim, _ = make_sim(prec, 0)
-        d0 = sim.diag()
-        X = [sim.get_colloids()["pos_colloid"]]
-        temps = []
-        for s in range(steps):
-            sim.step(1)
-            X.append(sim.get_colloids()["pos_colloid"])
-            if (s + 1) % 10 == 0:
-                temps.append(sim.diag()["temperature_fluid"])
-        d1 = sim.diag()
-        sim.close()
-        X = np.array(X)
-        dX = np.diff(X, axis=0)
-        dX -= L * np.round(dX / L)
-        U = np.concatenate([X[:1], X[:1] + np.cumsum(dX, axis=0)])
-        origins = range(0, steps - lag + 1, 10)
-        per_colloid = np.mean([np.sum((U[o + lag] - U[o]) ** 2, axis=1) for o in origins], axis=0)
-        scale = sim.N * np.sqrt(8.0 / np.pi)  # sum |p_i| of a thermal fluid (m = kT = 1)
-        out[prec] = {"msd": float(np.mean(per_colloid)),
-                     "msd_stderr": float(np.std(per_colloid) / np.sqrt(len(per_colloid))),
-                     "temperature": float(np.mean(temps)),
-                     "momentum_drift_rel": float(np.max(np.abs(np.array(d1["momentum"]) - np.array(d0["momentum"])))
-                                                 / scale)}
-    a, b = out["fp64"], out["fp32c"]
-    return {"steps": steps, "msd_lag": lag, "fp64": a, "fp32c": b,
+        rows = []
+        for r in range(replicas):
+            w = workload(seed=100 + r)
+            sim = bg.Simulation(w["L"], w["n_fluid"], w["n_colloid"],
+                                precision=bg.FP64 if prec == "fp64" else bg.FP32C, **w["kw"])
+            sim.initialize(bg.INIT_PHYSICAL)
+            sim.setup()
+            d0 = sim.diag()
+            tr = bg.Trajectory(sim.Nc, steps // every + 1, L)
+            tr.record(sim)
+            temps, drift = [], 0.0
+            for s in range(steps // every):
+                sim.step(every)
+                tr.record(sim)
+                if (s + 1) % 10 == 0:
+                    d = sim.diag()
+                    temps.append(d["temperature_fluid"])
+                    drift = max(drift, float(np.max(np.abs(np.array(d["momentum"]) - np.array(d0["momentum"])))))
+            msd = float(tr.analyse(msd_lags=(lag // every,), vacf_lags=(0,), oacf_lags=(0,))["msd"][0])
+            tr.close()
+            scale = sim.N * np.sqrt(8.0 / np.pi)  # sum |p_i| of a thermal fluid (m = kT = 1)
+            rows.append((msd, float(np.mean(temps)), drift / scale))
+            sim.close()
+        a = np.array(rows)
+        n = len(a)
+        per[prec] = {"msd": float(a[:, 0].mean()), "msd_stderr": float(a[:, 0].std(ddof=1) / np.sqrt(n)),
+                     "temperature": float(a[:, 1].mean()), "temperature_stderr": float(a[:, 1].std(ddof=1) / np.sqrt(n)),
+                     "momentum_drift_rel_mean": float(a[:, 2].mean()), "momentum_drift_rel_max": float(a[:, 2].max())}
+    a, b = per["fp64"], per["fp32c"]
+    return {"replicas": replicas, "steps": steps, "msd_lag_steps": lag, "frame_every": every,
+            "workload": "64^3, 2,621,440 fluid particles, 500 colloids; replica r from the library initialiser, seed "
+                        "100 + r, the same initial state for both forms",
+            "fp64": a, "fp32c": b,
             "msd_rel_diff": (b["msd"] - a["msd"]) / a["msd"],
-            "msd_rel_stderr_fp64": a["msd_stderr"] / a["msd"],
+            "msd_rel_diff_stderr": float(np.hypot(a["msd_stderr"], b["msd_stderr"]) / a["msd"]),
             "temperature_diff": b["temperature"] - a["temperature"],
-            "momentum_drift_rel_fp32c": b["momentum_drift_rel"]}
+            "temperature_diff_stderr": float(np.hypot(a["temperature_stderr"], b["temperature_stderr"])),
+            "momentum_drift_rel_fp64": a["momentum_drift_rel_max"],
+            "momentum_drift_rel_fp32c": b["momentum_drift_rel_max"]}
 
 
 def ensemble_params(nrep, seed=0):
@@ -345,7 +360,9 @@ def run_ensemble(nrep, steps, rank):
     l0 = ens.launch_count
     ens.step(1)
     launches_per_step = ens.launch_count - l0 - 1  # minus the error read-back
-    # the same replicas, each stepped by its own single-system call, one after the other
+    # the same replicas, each stepped by its own single-system call, one after the other:
+    # each replica's step graph enqueued back to back on one stream, one synchronisation
+    # per sweep over the replicas (a replica's next step needs its previous one only)
     st = torch.cuda.Stream()
     for s in ens:
         s.set_stream(st.cuda_stream)
@@ -353,7 +370,10 @@ def run_ensemble(nrep, steps, rank):
     t0 = time.perf_counter()
     for _ in range(steps):
         for s in ens:
-            s.step(1)
+            s.step_async(1)
+        ens[0].sync()
+    for s in ens:
+        s.sync()  # every replica's device checks
     looped_s = time.perf_counter() - t0
     n_particles = sum(p.n_fluid for p in P)
     ens.close()
@@ -362,7 +382,8 @@ def run_ensemble(nrep, steps, rank):
             "value": nrep * steps / batched_s, "unit": "replica-steps/s",
             "particle_steps_per_s": n_particles * steps / batched_s,
             "looped": {"value": nrep * steps / looped_s, "unit": "replica-steps/s",
-                       "how": "mpcd_step(1) of each replica in turn on one stream (each call synchronises)"},
+                       "how": "mpcd_step_async(1) of each replica in turn on one stream, one "
+                              "synchronisation per sweep over the replicas"},
             "speedup_vs_looped": looped_s / batched_s,
             "launches_per_step": launches_per_step,
             "autotune": {"choice": tuned["choice"], "ms_per_step": tuned["ms_per_step"],
@@ -514,7 +535,8 @@ def run_closure(samples_steps, deploy_steps):
             "heldout_nll": held, "heldout_nll_without_network": free,
             "speed": table,
             "speedup_500_vs_fp32c_in_comparison_run": res["speedup"],
-            "deploy_steps": deploy_steps, "lags": res["lags"], "rel_diff_vs_full": res["rel_diff_vs_full"],
+            "deploy_steps": deploy_steps, "blocks": res["blocks"], "lags": res["lags"],
+            "rel_diff_vs_full": res["rel_diff_vs_full"], "rel_diff_stderr": res["rel_diff_stderr"],
             "fast_steps": res["fast_steps"],
             "stats": res["stats"],
             "timing": "wall clock around step calls (each ends with a synchronisation); full MPCD 10 steps after 3, "
@@ -562,7 +584,8 @@ def run_ours(args, rank, world, dist):
            "timed": "set_state + setup + K x (step + diag) + get_state, host pinned buffers"}
     d = sim.diag()
     sim.close()
-    stats = form_statistics(args.stat_steps, 100) if (args.both and args.stat_steps > 100 and rank == 0) else None
+    stats = (form_statistics(args.stat_replicas, args.stat_steps)
+             if (args.both and args.stat_steps > 100 and args.stat_replicas > 1 and rank == 0) else None)
     ens = run_ensemble(args.ensemble, args.ensemble_steps, rank) if args.ensemble > 0 else None
     large = run_large(args.large_steps) if (args.large_steps > 0 and rank == 0) else None
     clo = run_closure(args.closure_steps, 2000) if (args.closure_steps > 0 and rank == 0) else None
@@ -609,10 +632,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"], help="form of the headline line")
     ap.add_argument("--both", type=int, default=1, help="also time the other precision form (sub-object)")
-    ap.add_argument("--stat-steps", type=int, default=200,
-                    help="steps of the FP32c-vs-FP64 statistics run (MSD at lag 100; <=100: skip)")
+    ap.add_argument("--stat-steps", type=int, default=2000,
+                    help="steps per system of the FP32c-vs-FP64 statistics (MSD at lag 100; <=100: skip)")
+    ap.add_argument("--stat-replicas", type=int, default=16,
+                    help="independent systems per form of the FP32c-vs-FP64 statistics (<2: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="replicas of the batched-ensemble sub-object (0: skip)")
-    ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--ensemble-steps", type=int, default=50)
     ap.add_argument("--large-steps", type=int, default=5,
                     help="timed steps of the 128^3 / 2000-colloid FP32 system (0: skip)")
     ap.add_argument("--closure-steps", type=int, default=800,

@@ -26,7 +26,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_substep", "mpcd_update_pos_md", "mpcd_neighbour_list_md", "mpcd_update_pos_mpcd",
            "mpcd_neighbour_list_mpcd", "mpcd_fluid_colloid_collision", "mpcd_update_activity_direction",
            "mpcd_compute_force_md", "mpcd_update_velocity_colloid", "mpcd_get_neighbour_md", "mpcd_get_box_binning",
-           "mpcd_step", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
+           "mpcd_step", "mpcd_step_async", "mpcd_sync", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
@@ -35,7 +35,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
            "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
            "mpcd_surrogate_features", "mpcd_surrogate_outputs", "mpcd_surrogate_fast_steps", "mpcd_surrogate_step",
-           "mpcd_surrogate_set_fault", "mpcd_updown_velocity", "mpcd_traj_create",
+           "mpcd_surrogate_set_fault", "mpcd_surrogate_set_noise", "mpcd_updown_velocity", "mpcd_traj_create",
            "mpcd_traj_destroy", "mpcd_traj_last_error", "mpcd_traj_frames", "mpcd_traj_reset", "mpcd_traj_record",
            "mpcd_traj_record_surrogate", "mpcd_traj_analyse", "mpcd_traj_read", "mpcd_traj_write"]
 # the routines of the substep body, in the reference's order (cpp/active_brownian.cpp:28-37)
@@ -109,6 +109,8 @@ def lib():
         L.mpcd_get_neighbour_md.argtypes = [vp, ip, ip, C.c_int]
         L.mpcd_get_box_binning.argtypes = [vp, ip, ip, ip]
         L.mpcd_step.argtypes = [vp, C.c_int]
+        L.mpcd_step_async.argtypes = [vp, C.c_int]
+        L.mpcd_sync.argtypes = [vp]
         L.mpcd_diag.argtypes = [vp, C.POINTER(Diag)]
         L.mpcd_get_rotation_binning.argtypes = [vp, ip, ip, dp]
         L.mpcd_get_shell_count.argtypes = [vp, ip]
@@ -444,6 +446,13 @@ class Simulation:
 
     def step(self, nsteps=1):
         self._ck(lib().mpcd_step(self.h, nsteps))
+
+    def step_async(self, nsteps=1):
+        """enqueue nsteps steps without waiting; sync() waits and reports device errors"""
+        self._ck(lib().mpcd_step_async(self.h, nsteps))
+
+    def sync(self):
+        self._ck(lib().mpcd_sync(self.h))
 
     def diag(self):
         d = Diag()

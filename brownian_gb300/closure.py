@@ -215,6 +215,7 @@ class Surrogate:
         L.mpcd_surrogate_features.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
         L.mpcd_surrogate_step.argtypes = [vp, C.c_int]
         L.mpcd_surrogate_set_fault.argtypes = [vp, C.c_int]
+        L.mpcd_surrogate_set_noise.argtypes = [vp, C.c_double]
         self.params, self.net = params, net
         self.Nc = params.n_colloid
         h = vp()
@@ -238,6 +239,10 @@ class Surrogate:
     def set_fault(self, drop_chunk=-1):
         """test hook: the network kernel's producer skips weight chunk drop_chunk (-1: none)"""
         self._ck(lib().mpcd_surrogate_set_fault(self.h, int(drop_chunk)))
+
+    def set_noise(self, scale=1.0):
+        """fluctuation of the drawn exchange: 1 the network's variance, 0 the mean only"""
+        self._ck(lib().mpcd_surrogate_set_noise(self.h, float(scale)))
 
     def get_state(self):
         out = {k: np.empty((self.Nc, 3)) for k in ("pos_colloid", "vel_colloid", "ang_vel_colloid", "ra")}
@@ -334,10 +339,14 @@ def generate_gpu(params_list, steps, warmup=20, net=None):
 
 
 def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0, 1, 2, 5, 10, 20),
-            olags=(0, 10, 50, 100)):
-    """Full MPCD (the yardstick), the closure surrogate and colloid-only dynamics without any
-    fluid exchange, from the same colloid state: MSD, velocity and orientation
-    autocorrelations, and the time per MPCD step of the full run and of the surrogate."""
+            olags=(0, 10, 50, 100), blocks=4):
+    """Full MPCD (the yardstick) against colloid-only dynamics from the same colloid state:
+    the closure (the network's mean and variance), the closure's mean only (the drag without
+    the fluctuations), and no fluid exchange at all.  Each run is `blocks` consecutive
+    stretches of `steps` / `blocks` steps; per stretch the MSD, velocity and orientation
+    autocorrelations on the GPU; reported as the mean over stretches with its standard error
+    (stretches longer than the largest lag are close to independent).  Also the time per MPCD
+    step of the full run and of the closure."""
     import time
     full = _sim(p)
     full.initialize(INIT_PHYSICAL)
@@ -350,7 +359,8 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     t_full = (time.perf_counter() - t0) / 20
     L = float(p.Lx)
     lag_kw = dict(msd_lags=lags, vacf_lags=vlags, oacf_lags=olags)
-    stats = {"full": device_stats(full, steps, L, **lag_kw)}
+    per = steps // blocks
+    stats = {"full": block_stats(full, per, blocks, L, **lag_kw)}
     full.close()
     sur = Surrogate(p, net)
     sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
@@ -359,15 +369,18 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     sur.step(100)
     t_sur = (time.perf_counter() - t0) / 100
     sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
-    stats["closure"] = device_stats(sur, steps, L, **lag_kw)
+    stats["closure"] = block_stats(sur, per, blocks, L, **lag_kw)
     fast = {"closure": sur.fast_steps()}
+    sur.set_noise(0.0)
+    sur.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
+    stats["mean_only"] = block_stats(sur, per, blocks, L, **lag_kw)
     sur.close()
     none_net = Network(max_batch=p.n_colloid)
     none_net.set_normalisation(np.zeros(IN), np.ones(IN), np.zeros(NY), np.full(NY, 1e-20))
     none_net.set_params(np.zeros(none_net.n_params))
     bare = Surrogate(p, none_net)
     bare.set_state(c0["pos_colloid"], c0["vel_colloid"], c0["ang_vel_colloid"], c0["ra"])
-    stats["no_closure"] = device_stats(bare, steps, L, **lag_kw)
+    stats["no_closure"] = block_stats(bare, per, blocks, L, **lag_kw)
     fast["no_closure"] = bare.fast_steps()
     bare.close()
     none_net.close()
@@ -375,11 +388,31 @@ def compare(p, net, steps, warmup=20, lags=(1, 2, 5, 10, 20, 50, 100), vlags=(0,
     out["stats"] = stats
     out["fast_steps"] = fast  # steps in which a colloid outran half its force-partner skin
     out["lags"] = {"msd": list(lags), "vacf": list(vlags), "oacf": list(olags)}
-    rel = {}
-    for name in ("closure", "no_closure"):
-        rel[name] = {k: (np.array(stats[name][k]) / np.array(stats["full"][k]) - 1.0).tolist()
-                     for k in ("msd", "vacf", "oacf")}
+    out["blocks"] = blocks
+    rel, err = {}, {}
+    f = stats["full"]
+    for name in ("closure", "mean_only", "no_closure"):
+        rel[name], err[name] = {}, {}
+        for k in ("msd", "vacf", "oacf"):
+            m, e = np.array(stats[name][k]), np.array(stats[name][k + "_stderr"])
+            mf, ef = np.array(f[k]), np.array(f[k + "_stderr"])
+            with np.errstate(divide="ignore", invalid="ignore"):
+                rel[name][k] = (m / mf - 1.0).tolist()
+                err[name][k] = np.sqrt((e / np.abs(mf)) ** 2 + (m * ef / mf ** 2) ** 2).tolist()
     out["rel_diff_vs_full"] = rel
+    out["rel_diff_stderr"] = err
+    return out
+
+
+def block_stats(obj, steps, blocks, L, **lags):
+    """device_stats of `blocks` consecutive stretches of `steps` steps: per quantity the mean
+    over the stretches and (key + "_stderr") its standard error."""
+    per = [device_stats(obj, steps, L, **lags) for _ in range(blocks)]
+    out = {}
+    for k in ("msd", "vacf", "oacf"):
+        a = np.array([q[k] for q in per])
+        out[k] = a.mean(0).tolist()
+        out[k + "_stderr"] = (a.std(0, ddof=1) / np.sqrt(blocks)).tolist() if blocks > 1 else [float("nan")] * a.shape[1]
     return out
 
 

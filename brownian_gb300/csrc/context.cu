@@ -946,7 +946,8 @@ extern "C" int mpcd_substep(mpcd_ctx *c, int l) {
   return check_device(c);
 }
 
-extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
+// nsteps steps enqueued on the context's stream (graph replays), nothing waited for
+static int enq_steps(mpcd_ctx *c, int nsteps) {
   int r;
   if ((r = need_setup(c))) return r;
   if (nsteps < 0) return MPCD_ERR_PARAM;
@@ -956,7 +957,7 @@ extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
       enq_step(c, sorts_at(c, c->host_step));
       c->host_step += 1;
     }
-    return check_device(c);
+    return MPCD_OK;
   }
   for (int s = 0; s < nsteps; ++s) {
     // one graph per (sorts this step, fluid buffer): the kernels' buffer arguments
@@ -980,6 +981,19 @@ extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
     if (sort) c->fbuf = 1 - b;
     c->host_step += 1;
   }
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_step(mpcd_ctx *c, int nsteps) {
+  int r;
+  if ((r = enq_steps(c, nsteps))) return r;
+  return check_device(c);
+}
+
+extern "C" int mpcd_step_async(mpcd_ctx *c, int nsteps) { return enq_steps(c, nsteps); }
+
+extern "C" int mpcd_sync(mpcd_ctx *c) {
+  if (!c) return MPCD_ERR_PARAM;
   return check_device(c);
 }
 

@@ -70,6 +70,7 @@ struct Sur {
   int *rebuild;     // a colloid moved more than half the skin since (or no lists yet)
   int *err;
   int drop_chunk;   // fault injection for tests: the producer does not issue this weight chunk (-1: none)
+  float noise;      // scale of the drawn exchange's fluctuation (1: the network's variance, 0: its mean only)
   const uint4 *wpk;                   // the packed BF16 weights (k_sur_pack)
   const float *bias;                  // the network's biases [256][256][256][16]
   const float *xmean, *xistd;         // input normalisation
@@ -699,7 +700,7 @@ __global__ void __launch_bounds__(NET_THREADS) k_sur_net(const Sur S) {
     const int r = tid / (NO / 2), k = tid % (NO / 2);
     const float *o = sm.out[r];
     const float lv = fminf(fmaxf(o[6 + k], -MLP_LOGVAR_CLAMP), MLP_LOGVAR_CLAMP);
-    sm.dp[r][k] = (o[k] + __expf(0.5f * lv) * sm.xi[r][k]) / sm.ys[k] + sm.ym[k];
+    sm.dp[r][k] = (o[k] + S.noise * __expf(0.5f * lv) * sm.xi[r][k]) / sm.ys[k] + sm.ym[k];
   }
   __syncthreads();
   // per (row, substep): Omega after the substep's share of the angular exchange (spread
@@ -1127,6 +1128,7 @@ extern "C" int mpcd_surrogate_create(const mpcd_params *p, mpcd_mlp *net, mpcd_s
   S.fpart = salloc<uint16_t>(s, Nc * MAXF); S.fpn = salloc<uint8_t>(s, Nc);
   S.err = salloc<int>(s, 1);
   S.drop_chunk = -1;
+  S.noise = 1.f;
   S.fast = salloc<long long>(s, 1);
   S.vmax = salloc<float>(s, 1);
   s->wpk = salloc<uint4>(s, PACK_U4);
@@ -1247,6 +1249,16 @@ extern "C" int mpcd_surrogate_set_fault(mpcd_surrogate *s, int drop_chunk) {
   if (!s || drop_chunk < -1 || drop_chunk >= NCHUNK || (drop_chunk >= 0 && drop_chunk < NSTAGE))
     return sfail(s, MPCD_ERR_PARAM, "drop_chunk: -1, or a weight chunk the producer loop issues");
   s->S.drop_chunk = drop_chunk;
+  if (s->exec) {  // the kernels take the parameters by value: capture again
+    cudaGraphExecDestroy(s->exec);
+    s->exec = nullptr;
+  }
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_surrogate_set_noise(mpcd_surrogate *s, double scale) {
+  if (!s || !(scale >= 0.0) || !(scale <= 1e3)) return sfail(s, MPCD_ERR_PARAM, "noise scale: 0 .. 1000");
+  s->S.noise = (float)scale;
   if (s->exec) {  // the kernels take the parameters by value: capture again
     cudaGraphExecDestroy(s->exec);
     s->exec = nullptr;

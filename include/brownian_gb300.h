@@ -164,6 +164,13 @@ int mpcd_get_box_binning(mpcd_ctx *c, int32_t *cell_of, int32_t *occupancy, int3
 /* nsteps complete MPCD steps (rotation_mpcd, run, n_sub substeps) — the loop of
  * cpp/active_brownian.cpp:23-56, replayed as one CUDA graph per step */
 int mpcd_step(mpcd_ctx *c, int nsteps);
+/* The same steps enqueued on the context's stream without waiting for them (no host
+ * synchronisation), for callers that step many contexts on one stream or overlap the steps
+ * with their own work; mpcd_sync waits for them and reports what went wrong on the device
+ * (as mpcd_step does before returning).  Other calls read the state only after the work
+ * enqueued before them (they synchronise). */
+int mpcd_step_async(mpcd_ctx *c, int nsteps);
+int mpcd_sync(mpcd_ctx *c);
 /* diagnostics of the state now (cpp/active_brownian.cpp:39-55) */
 int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out);
 
@@ -324,6 +331,10 @@ int mpcd_surrogate_fast_steps(mpcd_surrogate *s, int64_t *count);
  * that path this hook makes the kernel's producer skip weight chunk `drop_chunk` (6..19; -1:
  * none) so that the waits run out; the copies it does issue all land before the kernel ends. */
 int mpcd_surrogate_set_fault(mpcd_surrogate *s, int drop_chunk);
+/* Scale of the drawn exchange's fluctuation about the network's mean: 1 (the default) draws
+ * with the network's predicted variance, 0 applies the predicted mean only (a deterministic
+ * drag without the fluctuations that balance it). */
+int mpcd_surrogate_set_noise(mpcd_surrogate *s, double scale);
 
 /* ---- fluid sums without allocation (no counterpart in the reference) ---------------- */
 /* For callers that cannot call cudaMalloc: their device memory is all handed out by their

@@ -82,11 +82,22 @@ def loss_and_grad(p, x, y, xmean, xstd, ymean, ystd, bf16_emul=True, dtype=np.fl
     return loss, flat
 
 
-def forward(p, x, xmean, xstd, ymean, ystd, dtype=np.float64):
-    """Outputs in physical units: means (6) and log-variances (6)."""
-    layers = [(np.asarray(W, dtype), np.asarray(b, dtype)) for W, b in unflatten(np.asarray(p, dtype))]
-    a = np.clip((x - xmean) / np.where(xstd > 0, xstd, np.inf), -6, 6)
+def forward(p, x, xmean, xstd, ymean, ystd, dtype=np.float64, bf16_emul=False):
+    """Outputs in physical units: means (6) and log-variances (6).  With bf16_emul, in float32
+    with every tensor the GPU stores in BF16 (normalised inputs, weights, activations) rounded
+    to BF16 where it does, as loss_and_grad does."""
+    if bf16_emul:
+        dtype = np.float32
+        r = bf16
+    else:
+        r = lambda a: a  # noqa: E731
+    layers = [(r(np.asarray(W, dtype)), np.asarray(b, dtype)) for W, b in unflatten(np.asarray(p, dtype))]
+    if bf16_emul:
+        xs = np.where(xstd > 0, 1.0 / np.where(xstd > 0, xstd, 1.0), 0.0).astype(dtype)
+        a = r(np.clip((np.asarray(x, dtype) - xmean) * xs, -6, 6))
+    else:
+        a = np.clip((x - xmean) / np.where(xstd > 0, xstd, np.inf), -6, 6)
     for l, (W, b) in enumerate(layers):
         z = a @ W + b
-        a = z * sig(z) if l < 3 else z
+        a = r(z * sig(z)) if l < 3 else z
     return np.concatenate([a[:, :NY] * ystd + ymean, np.clip(a[:, NY:], -6, 6) + 2 * np.log(ystd)], axis=1)

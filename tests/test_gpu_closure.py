@@ -33,12 +33,15 @@ def test_gradients_match_cpu_oracle():
     net, p, x, y, xm, xs, ym, ys, xd, yd = _setup(300, 1)
     loss, g = net.grad(xd.data_ptr(), yd.data_ptr(), 300)
     lref, gref = M.loss_and_grad(p, x, y, xm, xs, ym, ys, bf16_emul=True)
-    assert abs(loss - lref) <= 1e-3 * abs(lref)
+    assert abs(loss - lref) <= 1e-5 * abs(lref)
     o = 0
     for k, n in M.DIMS:
         for size in (k * n, n):
             a, b = g[o:o + size], gref[o:o + size]
-            assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-7, (o, size)
+            # BF16 products where the restatement rounds to BF16 too: what remains is the FP32
+            # accumulation order (split-K atomics) and the rare BF16 rounding it flips, measured
+            # at 3e-4 relative at most on GB300
+            assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b) + 1e-7, (o, size)
             o += size
     net.close()
 
@@ -49,9 +52,13 @@ def test_forward_matches_cpu_oracle():
     out = torch.zeros((1000, M.OUT), dtype=torch.float32, device="cuda")
     net.forward(xd.data_ptr(), out.data_ptr(), 1000)
     torch.cuda.synchronize()
-    ref = M.forward(p, x.astype(np.float64), xm, xs, ym, ys)
     got = out.cpu().numpy()
-    assert np.linalg.norm(got - ref) <= 2e-2 * np.linalg.norm(ref)
+    # against FP64 arithmetic: the BF16 storage of inputs, weights and activations (8 bits)
+    ref = M.forward(p, x.astype(np.float64), xm, xs, ym, ys)
+    assert np.linalg.norm(got - ref) <= 1e-2 * np.linalg.norm(ref)
+    # against the restatement that rounds to BF16 where the GPU stores BF16 (measured 5e-5)
+    ref16 = M.forward(p, x, xm, xs, ym, ys, bf16_emul=True)
+    assert np.linalg.norm(got - ref16) <= 3e-4 * np.linalg.norm(ref16)
     net.close()
 
 

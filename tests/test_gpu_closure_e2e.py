@@ -1,6 +1,7 @@
 """The learned closure end to end at a small size: samples from the exact collision
 kernel, training on the GPU, and what the trained network gains over the method
-without it (colloid-only dynamics with no fluid exchange), measured against full MPCD."""
+without it (colloid-only dynamics with no fluid exchange) and over its own mean without
+the learned variance, measured against full MPCD."""
 import numpy as np
 import pytest
 
@@ -27,10 +28,19 @@ def test_trained_closure_beats_no_closure():
     held = closure.nll(net, X[cut:], Y[cut:])
     free = closure.free_nll(Y[:cut], Y[cut:])  # without the network
     assert held < free - 0.2, (held, free)
-    res = closure.compare(_p(24, 40, 0.05, 42), net, steps=200, lags=(5, 20, 50))
-    d_c = abs(res["rel_diff_vs_full"]["closure"]["msd"][1])
-    d_n = abs(res["rel_diff_vs_full"]["no_closure"]["msd"][1])
-    assert d_c < d_n, res["rel_diff_vs_full"]
+    res = closure.compare(_p(24, 40, 0.05, 42), net, steps=400, lags=(5, 20, 50), blocks=2)
+    rel = res["rel_diff_vs_full"]
+    d_c = abs(rel["closure"]["msd"][1])
+    d_n = abs(rel["no_closure"]["msd"][1])
+    assert d_c < d_n, rel
+    # the learned variance matters: with the network's mean only the colloids lose the
+    # fluctuations of the fluid and their kinetic energy (VACF at lag 0) falls well below
+    # the full method's, which the closure with its variance keeps
+    v_c = abs(rel["closure"]["vacf"][0])
+    v_m = abs(rel["mean_only"]["vacf"][0])
+    assert v_c < v_m, rel
+    # the trained closure's colloids never outrun the force-partner skin
+    assert res["fast_steps"]["closure"] == 0, res["fast_steps"]
     # the trained closure's colloids never outrun the force-partner skin
     assert res["fast_steps"]["closure"] == 0, res["fast_steps"]
     net.close()
