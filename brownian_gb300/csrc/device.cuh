@@ -66,31 +66,52 @@ static __device__ __forceinline__ int block_base(int *counter, unsigned m, int l
   return block_base_n(counter, __popc(m), lane);
 }
 
-// Batched launches: block b of a launch over nrep systems belongs to the system r
-// with boff[r] <= b < boff[r+1] (boff ascending, boff[nrep] = the grid) and is
-// that system's virtual block b - boff[r] of boff[r+1] - boff[r]; its SysF64 is
-// copied into shared memory once per block.
-static __device__ __forceinline__ void batch_locate(const SysF64 *Ss, const int *boff, int nrep, SysF64 &sS, int &vb,
-                                                    int &nvb) {
+// Batched launches, persistent: the systems' virtual blocks (system r has boff[r+1] -
+// boff[r] of them; boff ascending, boff[nrep] in all) are shared out in contiguous runs
+// over the grid's blocks, a few resident per SM: block b runs the virtual blocks
+// [b T / G, (b+1) T / G) one after another, each as virtual block v - boff[r] of the
+// boff[r+1] - boff[r] of its system r, with that system's SysF64 copied into shared
+// memory when the run reaches it (a run crosses a system boundary at most a few times).
+// body(VB, NVB) must be called by the whole block, as a kernel body would be.
+template <typename Body>
+static __device__ __forceinline__ void batch_for(const SysF64 *Ss, const int *boff, int nrep, SysF64 &sS, Body body) {
   __shared__ int s_r;
+  const int total = boff[nrep];
+  const int v0 = (int)((long long)blockIdx.x * total / gridDim.x);
+  const int v1 = (int)((long long)(blockIdx.x + 1) * total / gridDim.x);
+  if (v0 >= v1) return;
   if (threadIdx.x == 0) {
     int lo = 0, hi = nrep;
-    const int b = blockIdx.x;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if (boff[mid] <= b) lo = mid;
+      if (boff[mid] <= v0) lo = mid;
       else hi = mid;
     }
     s_r = lo;
   }
   __syncthreads();
-  const int r = s_r;
-  const int *src = reinterpret_cast<const int *>(Ss + r);
-  int *dst = reinterpret_cast<int *>(&sS);
-  for (int k = threadIdx.x; k < (int)(sizeof(SysF64) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  int r = s_r;
+  int first = boff[r], next = boff[r + 1];
+  auto load = [&](int q) {
+    const int *src = reinterpret_cast<const int *>(Ss + q);
+    int *dst = reinterpret_cast<int *>(&sS);
+    for (int k = threadIdx.x; k < (int)(sizeof(SysF64) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  };
+  load(r);
   __syncthreads();
-  vb = (int)blockIdx.x - boff[r];
-  nvb = boff[r + 1] - boff[r];
+  for (int v = v0; v < v1; ++v) {
+    if (v >= next) {  // the run reaches the next system (systems without blocks skipped)
+      do {
+        ++r;
+        first = next;
+        next = boff[r + 1];
+      } while (v >= next);
+      load(r);
+      __syncthreads();
+    }
+    body(v - first, next - first);
+    __syncthreads();  // the body's shared memory and the descriptor are reused
+  }
 }
 
 // A cell-table entry is (tag << 32) | count with tag = substep + 1: substeps

@@ -402,13 +402,11 @@ __global__ void __launch_bounds__(256) k_stream32(__grid_constant__ const SysF64
   k_stream32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 template <int FLAGS>
 __global__ void __launch_bounds__(256) k_stream32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_stream32_body<FLAGS>(sS, VB, NVB, l, fb);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_stream32_body<FLAGS>(sS, VB, NVB, l, fb); });
 }
 
 int stream32_per_thread(int flags) { return stream32_u(flags); }
@@ -456,13 +454,11 @@ __global__ void __launch_bounds__(128) k_events32(__grid_constant__ const SysF64
   k_events32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 template <int FLAGS>
 __global__ void __launch_bounds__(128) k_events32_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_events32_body<FLAGS>(sS, VB, NVB, l, fb);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_events32_body<FLAGS>(sS, VB, NVB, l, fb); });
 }
 
 StreamKernel stream_kernel32(int flags) {
@@ -577,12 +573,10 @@ __global__ void __launch_bounds__(256) k_cell_prep32(__grid_constant__ const Sys
   k_cell_prep32_body(S, blockIdx.x, gridDim.x);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(256) k_cell_prep32_b(const SysF64 *Ss, const int *boff, int nrep) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_cell_prep32_body(sS, VB, NVB);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_cell_prep32_body(sS, VB, NVB); });
 }
 
 __device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &vy, float &vz) {
@@ -609,12 +603,10 @@ __global__ void __launch_bounds__(256) k_rotate32(__grid_constant__ const SysF64
   k_rotate32_body(S, blockIdx.x, gridDim.x, fb);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(256) k_rotate32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_rotate32_body(sS, VB, NVB, fb);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_rotate32_body(sS, VB, NVB, fb); });
 }
 
 static __device__ __forceinline__ void k_rotate_sort32_body(const SysF64 &S, const int VB, const int NVB, int src, int dst) {
@@ -646,12 +638,10 @@ __global__ void __launch_bounds__(256) k_rotate_sort32(__grid_constant__ const S
   k_rotate_sort32_body(S, blockIdx.x, gridDim.x, src, dst);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(256) k_rotate_sort32_b(const SysF64 *Ss, const int *boff, int nrep, int src, int dst) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_rotate_sort32_body(sS, VB, NVB, src, dst);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_rotate_sort32_body(sS, VB, NVB, src, dst); });
 }
 
 // run() (cpp/run.cpp:17-24) on the FP32 fluid: rear-shell test against V + v0 ra
@@ -686,12 +676,10 @@ __global__ void k_run_shell32(__grid_constant__ const SysF64 S, int fb) {
   k_run_shell32_body(S, blockIdx.x, gridDim.x, fb);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void k_run_shell32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_run_shell32_body(sS, VB, NVB, fb);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_run_shell32_body(sS, VB, NVB, fb); });
 }
 
 static __device__ __forceinline__ void k_run_kick32_body(const SysF64 &S, const int VB, const int NVB, int fb) {
@@ -716,12 +704,10 @@ __global__ void k_run_kick32(__grid_constant__ const SysF64 S, int fb) {
   k_run_kick32_body(S, blockIdx.x, gridDim.x, fb);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void k_run_kick32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_run_kick32_body(sS, VB, NVB, fb);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_run_kick32_body(sS, VB, NVB, fb); });
 }
 
 // AoS doubles (particle order) -> FP32 records; download scatters back by id

@@ -367,12 +367,10 @@ __global__ void __launch_bounds__(256) k_aux(__grid_constant__ const SysF64 S, i
   k_aux_body(S, blockIdx.x, gridDim.x, l, act);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(256) k_aux_b(const SysF64 *Ss, const int *boff, int nrep, int l, int act) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_aux_body(sS, VB, NVB, l, act);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_aux_body(sS, VB, NVB, l, act); });
 }
 
 EventKernel event_kernel(int flags) {
@@ -491,12 +489,11 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(__grid_constant__ const Sy
   k_scan_blocks_body(S, blockIdx.x, gridDim.x, nblk);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(1024) k_scan_blocks_b(const SysF64 *Ss, const int *boff, int nrep, int nblk) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_scan_blocks_body(sS, VB, NVB, (sS.Cpad + 255) / 256);  // each system's own block count
+  // each system's own block count
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_scan_blocks_body(sS, VB, NVB, (sS.Cpad + 255) / 256); });
 }
 
 // The SRD collision applied to each particle, w' = A w + b of its cell, and the
@@ -777,12 +774,10 @@ __global__ void __launch_bounds__(256) k_fin(__grid_constant__ const SysF64 S, i
   k_fin_body(S, blockIdx.x, gridDim.x, mode, l);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void __launch_bounds__(128) k_fin_b(const SysF64 *Ss, const int *boff, int nrep, int mode, int l) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_fin_body(sS, VB, NVB, mode, l);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_fin_body(sS, VB, NVB, mode, l); });
 }
 
 // Set-up (the prologue of main, cpp/active_brownian.cpp:17-20): forces at the
@@ -881,12 +876,10 @@ __global__ void k_end_step(__grid_constant__ const SysF64 S) {
   k_end_step_body(S, blockIdx.x, gridDim.x);
 }
 
-// the same over a batch of systems: block b runs virtual block b - boff[r] of system r
+// the same over a batch of systems (persistent: batch_for)
 __global__ void k_end_step_b(const SysF64 *Ss, const int *boff, int nrep) {
   __shared__ SysF64 sS;
-  int VB, NVB;
-  batch_locate(Ss, boff, nrep, sS, VB, NVB);
-  k_end_step_body(sS, VB, NVB);
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_end_step_body(sS, VB, NVB); });
 }
 
 // fluid diagnostics from the exact cell sums of the last binning: per block the
