@@ -503,6 +503,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.physics = p.physics == MPCD_PHYSICS_FIXED ? 1 : 0;
   S.aux_nw = S.fin_table ? 2 : 4;
   S.dtf = (float)dt;
+  S.kick32 = (float)(p.mass_colloid * p.v0 / p.mass_fl);
   S.vmaxf = (float)vmax;
   // the FP64 form sums displacements w = v dt, the FP32 form velocities
   const double wmax = p.precision == MPCD_FP64 ? vmax * dt : vmax;

@@ -693,8 +693,9 @@ static __device__ __forceinline__ void k_run_kick32_body(const SysF64 &S, const 
     for (int k = 0; k < rec.n; ++k) {
       if (!((rec.pass >> k) & 1)) continue;
       int j = rec.j[k];
-      double f = S.mass_colloid / (S.mass_fl * (double)S.shell_cnt[j]) * S.v0;
-      vx -= (float)(S.ra[3 * j] * f); vy -= (float)(S.ra[3 * j + 1] * f); vz -= (float)(S.ra[3 * j + 2] * f);
+      // M v0 / (m cnt) in FP32 (the velocity it changes is FP32): no double division
+      const float f = S.kick32 / (float)S.shell_cnt[j];
+      vx -= (float)S.ra[3 * j] * f; vy -= (float)S.ra[3 * j + 1] * f; vz -= (float)S.ra[3 * j + 2] * f;
     }
     F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
   }

@@ -163,6 +163,7 @@ struct SysF64 {
   float *v32[2][3];
   float *cell_ab32;    // [C][12] SRD map in FP32
   float dtf;           // dt in FP32
+  float kick32;        // M v0 / m in FP32: run()'s fluid kick times the shell count
   float vmaxf;         // speed bound of the exact cell sums
   float4 *Xcq[2];      // colloid cell (integer-valued floats), double-buffered like X
   float4 *Xco[2];      // colloid offset within the cell
