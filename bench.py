@@ -20,8 +20,9 @@ with CUDA events over a second timed region, against its algorithmic bytes
 Multi-GPU: one independent replica per rank (different seed), no collective
 in the data path ("scaling": "weak").
 
---impl reference: the reference's CPU algorithm on the host cores (the oracle port
-of cpp/, one single-threaded process per core on a bounded sample).
+--impl reference: the reference's CPU step on the host cores, one single-threaded process
+per core on a bounded sample: its own cpp/ routines (oracle/_ref/ref_harness) where they
+were compiled from the reference sources, else the oracle's restatement of cpp/.
 """
 import argparse
 import json
@@ -182,6 +183,44 @@ def _cpu_worker(args):
     dt = time.perf_counter() - t0
     o.close()
     return n_fluid_sample * steps / dt
+
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def reference_available():
+    """The reference's own cpp/ routines, compiled where the reference sources are (the
+    oracle Makefile's `ref` target); absent where the sources are not."""
+    return os.path.isfile(HARNESS) and os.access(HARNESS, os.X_OK)
+
+
+def reference_baseline(processes, steps, n_fluid, tmp="/tmp"):
+    """The stock reference step loop (oracle/_ref/ref_harness time mode): `processes`
+    independent single-threaded runs at once, each `steps` MPCD steps of the workload from a
+    synthetic state (seed = process), after the prologue and one untimed step."""
+    import numpy as np
+    w = workload(0)
+    kw = w["kw"]
+    procs = []
+    for q in range(processes):
+        st = synthetic_state(q, n_fluid)
+        path = os.path.join(tmp, f"bgb_ref_state_{os.getpid()}_{q}.bin")
+        with open(path, "wb") as f:
+            for k in ("pos_fl", "vel_fl", "pos_colloid", "vel_colloid", "ang_vel_colloid"):
+                np.ascontiguousarray(st[k], dtype=np.float64).tofile(f)
+        args = [HARNESS, "time", str(w["L"]), str(n_fluid), str(w["n_colloid"]), str(kw["n_sub"]), repr(kw["ndt"]),
+                repr(kw["kbt"]), repr(kw["kbt1"]), repr(kw["mass_fl"]), repr(kw["mass_colloid"]),
+                repr(kw["sig_colloid"]), repr(kw["eps"]), repr(kw["sigma"]), repr(kw["I_colloid"]), repr(kw["v0"]),
+                "77777", str(steps), path]
+        procs.append((subprocess.Popen(args, stdout=subprocess.PIPE, text=True), path))
+    rates = []
+    for pr, path in procs:
+        out, _ = pr.communicate()
+        os.remove(path)
+        if pr.returncode != 0:
+            raise RuntimeError(f"ref_harness exited {pr.returncode}")
+        rates.append(json.loads(out.strip().splitlines()[-1])["particle_steps_per_s"])
+    return sum(rates), rates
 
 
 def cpu_baseline(processes, steps, n_fluid):
@@ -658,16 +697,24 @@ def main():
         t0 = time.perf_counter()
         for _ in range(args.warmup):
             pass  # each timed worker does its own warm-up step
-        rate, rates = cpu_baseline(procs, args.steps, sample_n)
+        if reference_available():
+            # the reference's own cpp/ routines (compiled from its sources where they are present)
+            rate, rates = reference_baseline(procs, args.steps, sample_n)
+            kind, what = "reference", "the reference's own cpp/ step loop (oracle/_ref/ref_harness)"
+        else:
+            # where the reference sources are absent: the oracle's restatement of cpp/, pinned bit
+            # for bit to the reference's traces
+            rate, rates = cpu_baseline(procs, args.steps, sample_n)
+            kind, what = "port", "the oracle's restatement of cpp/ (the reference's sources are not on this machine)"
         wall = time.perf_counter() - t0
         line = {"impl": "reference", "metric": "MPCD fluid particle-steps/s", "value": rate,
                 "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": dict(config_dict("fp64"), parallelism=f"{procs} CPU processes"),
-                "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": procs, "kind": "port",
-                                 "sample": f"{procs} independent single-threaded oracle processes (restatement of "
-                                           f"cpp/), each {args.steps} MPCD steps of the 64^3 system with "
-                                           f"{sample_n} fluid particles, after one warm-up step; wall {wall:.1f} s"},
+                "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": procs, "kind": kind,
+                                 "sample": f"{procs} independent single-threaded processes of {what}, each "
+                                           f"{args.steps} MPCD steps of the 64^3 system with {sample_n} fluid "
+                                           f"particles, after one untimed step; wall {wall:.1f} s"},
                 "e2e": {"value": rate, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))

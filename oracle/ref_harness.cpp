@@ -11,6 +11,10 @@
 //
 // Output: a stream of records  [char tag[48]][uint64 nbytes][bytes].
 // Modes:
+//   ref_harness time   L N Nc n_sub ndt kbt kbt1 mass_fl M sig_colloid eps sigma I v0 seed nsteps state
+//     the reference's own step loop (cpp/active_brownian.cpp:23-38) timed over nsteps MPCD steps
+//     from the given state (file as below; initialize_fluid is skipped), after the prologue and
+//     one untimed step; prints {"steps": n, "seconds": s, "particle_steps_per_s": r}
 //   ref_harness trace  L N Nc n_sub ndt kbt kbt1 mass_fl M sig_colloid eps sigma I v0 seed nsteps detail_steps out [state]
 //     state (optional): raw doubles pos_fl[N][3] vel_fl[N][3] pos_colloid[Nc][3]
 //     vel_colloid[Nc][3] ang_vel_colloid[Nc][3] that replace the state the reference
@@ -18,6 +22,7 @@
 //   ref_harness ran    seed count out
 #include "parameters.hpp"
 
+#include <chrono>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -93,7 +98,8 @@ int main(int argc, char **argv) {
     fclose(out);
     return 0;
   }
-  if ((argc != 20 && argc != 21) || std::string(argv[1]) != "trace") {
+  const bool timing = argc == 19 && std::string(argv[1]) == "time";
+  if (!timing && ((argc != 20 && argc != 21) || std::string(argv[1]) != "trace")) {
     fprintf(stderr, "usage: ref_harness trace L N Nc n_sub ndt kbt kbt1 mass_fl M sig eps sigma I v0 seed nsteps detail out\n");
     return 2;
   }
@@ -113,8 +119,8 @@ int main(int argc, char **argv) {
   I_colloid = atof(argv[14]);
   v0 = atof(argv[15]);
   seed = atoi(argv[16]);
-  int nsteps = atoi(argv[17]), detail = atoi(argv[18]);
-  out = fopen(argv[19], "wb");
+  int nsteps = atoi(argv[17]), detail = timing ? 0 : atoi(argv[18]);
+  out = fopen(timing ? "/dev/null" : argv[19], "wb");
   if (!out) return 3;
   dt = ndt / (double)n;
   // the derived constants of cpp/update.cpp:3-6, recomputed for the new sig_colloid
@@ -126,9 +132,9 @@ int main(int argc, char **argv) {
 
   initialize();
   initialize_colloid();
-  initialize_fluid();
-  if (argc == 21) {
-    FILE *in = fopen(argv[20], "rb");
+  if (!timing) initialize_fluid();
+  if (timing || argc == 21) {
+    FILE *in = fopen(argv[timing ? 18 : 20], "rb");
     if (!in) return 4;
     size_t ok = fread(&pos_fl[1], sizeof(point), no_of_fluid, in) + fread(&vel_fl[1], sizeof(point), no_of_fluid, in) +
                 fread(&pos_colloid[1], sizeof(point), no_of_colloid, in) +
@@ -157,6 +163,34 @@ int main(int argc, char **argv) {
   tumble();
   rec_pts("setup.tumble/ra", ra, no_of_colloid);
 
+  if (timing) {
+    // the step loop of cpp/active_brownian.cpp:23-38 as it stands (one untimed step first)
+    auto one = [&]() {
+      rotation_mpcd();
+      run();
+      for (int l = 1; l <= n; l++) {
+        std::copy(f, f + no_of_colloid + 2, old_force);
+        update_pos_md();
+        neighbour_list_md();
+        update_pos_mpcd();
+        neighbour_list_mpcd();
+        if (!(l % 10) && nn > 10000) updown_velocity();
+        fluid_colloid_collision();
+        update_activity_direction();
+        compute_force_md();
+        update_velocity_colloid();
+      }
+    };
+    nn = 1;
+    one();
+    const auto t0 = std::chrono::steady_clock::now();
+    for (nn = 2; nn <= nsteps + 1; nn++) one();
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    printf("{\"steps\": %d, \"seconds\": %.6f, \"particle_steps_per_s\": %.6e}\n", nsteps, sec,
+           (double)no_of_fluid * nsteps / sec);
+    fclose(out);
+    return 0;
+  }
   for (nn = 1; nn <= niter && nn <= nsteps; nn++) {
     std::string s = "s" + std::to_string(nn);
     bool d = nn <= detail;
