@@ -695,8 +695,7 @@ def main():
         procs = os.cpu_count() or 1
         total = 0.0
         t0 = time.perf_counter()
-        for _ in range(args.warmup):
-            pass  # each timed worker does its own warm-up step
+        # each timed worker process does its own untimed warm-up step
         if reference_available():
             # the reference's own cpp/ routines (compiled from its sources where they are present)
             rate, rates = reference_baseline(procs, args.steps, sample_n)

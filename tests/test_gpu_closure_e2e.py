@@ -41,6 +41,4 @@ def test_trained_closure_beats_no_closure():
     assert v_c < v_m, rel
     # the trained closure's colloids never outrun the force-partner skin
     assert res["fast_steps"]["closure"] == 0, res["fast_steps"]
-    # the trained closure's colloids never outrun the force-partner skin
-    assert res["fast_steps"]["closure"] == 0, res["fast_steps"]
     net.close()

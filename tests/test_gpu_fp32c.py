@@ -65,6 +65,48 @@ def test_one_step_agrees_with_fp64():
     assert rel < 2e-2, rel
 
 
+def test_one_step_agrees_with_oracle():
+    """The FP32-compensated step against the FP64 oracle from the same state with the same
+    keyed draws: the error of every observable of one step, stated as a bar."""
+    import brownian_gb300 as bg
+    from oracle import oracle as O
+    L, N, Nc = 20, 80000, 20
+    kw = _kw()
+    o = O.Oracle(L=L, n_fluid=N, n_colloid=Nc, rng_mode=O.RNG_KEYED, **kw)
+    o.initialize_colloid()
+    o.initialize_fluid()
+    o.tumble()
+    st = o.state()
+    sim = bg.Simulation(L, N, Nc, precision=bg.FP32C, **kw)
+    sim.set_state(st["pos_fl"], st["vel_fl"], st["pos_colloid"], st["vel_colloid"], st["ang_vel_colloid"],
+                  st["ra"])
+    sim.setup()
+    o.setup()
+    sim.step(1)
+    o.run_steps(1)
+    g = sim.get_state()
+    dv = np.max(np.abs(g["vel_fl"] - o.get("vel_fl")), axis=1)
+    dx = np.max(np.abs(min_image(g["pos_fl"] - o.get("pos_fl"), float(L))), axis=1)
+    # FP32 rounding of a thermal velocity (|v| ~ 1) is 6e-8; a particle at a cell face or a
+    # sphere surface can take the other branch
+    assert np.quantile(dv, 0.99) < 1e-5
+    assert np.mean(dv > 1e-4) < 1e-3
+    assert np.mean(dx > 1e-5) < 1e-3
+    for k in ("pos_colloid", "ra"):
+        assert np.max(np.abs(min_image(g[k] - o.get(k), float(L)))) < 1e-4, k
+    rel = np.linalg.norm(g["vel_colloid"] - o.get("vel_colloid")) / np.linalg.norm(o.get("vel_colloid"))
+    assert rel < 2e-2, rel
+    # the cell occupancies of the next binning: a particle changes cell only at a face
+    _, occ_gpu, shift_gpu = sim.rotation_binning()
+    o.nn = o.nn + 1
+    o.rotation_mpcd()
+    _, occ_ref = o.binning(0)
+    assert np.array_equal(shift_gpu, o.shift())
+    assert np.sum(np.abs(occ_gpu.astype(np.int64) - occ_ref)) <= 1e-3 * N
+    sim.close()
+    o.close()
+
+
 def test_momentum_and_temperature():
     _, _, s32 = make_pair32(12, 17280, 5)
     d0 = s32.diag()

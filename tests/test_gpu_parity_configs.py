@@ -7,8 +7,9 @@
   WCA sigma 6, colloid mass the displaced fluid mass, 20 substeps, v0 0.02, Dr 0.0005),
   with colloid pairs placed inside the WCA cutoff: five steps, same bars;
 * the 20^3 system (80,000 fluid particles, 20 colloids, seed 0) for 1,000 steps on both
-  sides from the same keyed initial state: total momentum, fluid temperature, colloid
-  MSD and velocity autocorrelation compared within their statistical errors;
+  sides from the same keyed initial state, the GPU in either form: total momentum, fluid
+  temperature, colloid MSD and velocity autocorrelation compared within their statistical
+  errors;
 * mpcd_diag against the oracle's diagnostics (the sums of cpp/active_brownian.cpp:39-55);
 * mpcd_initialize against the oracle's keyed initialisation (cpp/initialize.cpp:31-83,
   cpp/run.cpp:3-8), and the physical initial state checked statistically.
@@ -161,9 +162,11 @@ def _msd_vacf(U, V, lags):
     return out
 
 
-def test_1000_steps_20cube_statistics_match_oracle():
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_1000_steps_20cube_statistics_match_oracle(precision):
     """20^3, 80,000 fluid particles, 20 colloids of radius 2, seed 0, 1,000 steps on both
-    sides from the oracle's keyed initial state.  Bars (stated): per-step total momentum
+    sides from the oracle's keyed initial state, the GPU in the FP64 form and in the
+    FP32-compensated form (each against the FP64 oracle).  Bars (stated): per-step total momentum
     equal to the oracle's within 1e-12 of sum |p| while the colloid trajectories agree to
     1e-10, else a drift of the oracle's order (the reference itself does not conserve
     momentum: a colloid whose rear shell is empty takes run()'s kick M v0 alone); block-averaged
@@ -178,7 +181,8 @@ def test_1000_steps_20cube_statistics_match_oracle():
     o.initialize_fluid()
     o.tumble()
     st = o.state()
-    sim = bg.Simulation(L, N, Nc, **kw)
+    prec = bg.FP64 if precision == "fp64" else bg.FP32C
+    sim = bg.Simulation(L, N, Nc, precision=prec, **kw)
     sim.set_state(*[st[k] for k in STATE])
     o.setup()
     sim.setup()
