@@ -301,8 +301,9 @@ def measure_resident(sim, stream, precision, args, world, dist, with_clocks=True
             "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": STREAM_BYTES[precision] * N,
             "peak_source": f"{peak_kind} hbm_gbs (burst copy)", "launch_ms": t_launch * 1e3,
             "launches": st_launches}
+    near = sim.flight_near() if precision == "fp32c" else None
     return dict(value=value, ms=ms, gpu_launches=gpu_launches, clocks=clk, roofline=roof, shares=shares,
-                step_frac=value / world * STEP_BYTES[precision] / (peak * 1e9))
+                step_frac=value / world * STEP_BYTES[precision] / (peak * 1e9), near=near)
 
 
 def form_statistics(replicas, steps, lag=100, every=10):
@@ -652,6 +653,8 @@ def run_ours(args, rank, world, dist):
                                 "speedup_vs_" + args.precision: o["value"] / r["value"],
                                 "hbm_roofline_frac_step": o["step_frac"], "roofline": o["roofline"],
                                 "kernel_share": o["shares"], "gpu_launches": o["gpu_launches"]}
+        if o.get("near") is not None:
+            line[f"form_{prec}"]["near_particles_last_step"] = o["near"]
     if stats:
         line["fp32c_vs_fp64"] = stats
     if ens:

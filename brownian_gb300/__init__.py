@@ -26,7 +26,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_substep", "mpcd_update_pos_md", "mpcd_neighbour_list_md", "mpcd_update_pos_mpcd",
            "mpcd_neighbour_list_mpcd", "mpcd_fluid_colloid_collision", "mpcd_update_activity_direction",
            "mpcd_compute_force_md", "mpcd_update_velocity_colloid", "mpcd_get_neighbour_md", "mpcd_get_box_binning",
-           "mpcd_step", "mpcd_step_async", "mpcd_sync", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
+           "mpcd_step", "mpcd_step_async", "mpcd_sync", "mpcd_set_flight", "mpcd_get_flight", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
@@ -111,6 +111,8 @@ def lib():
         L.mpcd_step.argtypes = [vp, C.c_int]
         L.mpcd_step_async.argtypes = [vp, C.c_int]
         L.mpcd_sync.argtypes = [vp]
+        L.mpcd_set_flight.argtypes = [vp, C.c_int]
+        L.mpcd_get_flight.argtypes = [vp, ip]
         L.mpcd_diag.argtypes = [vp, C.POINTER(Diag)]
         L.mpcd_get_rotation_binning.argtypes = [vp, ip, ip, dp]
         L.mpcd_get_shell_count.argtypes = [vp, ip]
@@ -453,6 +455,16 @@ class Simulation:
 
     def sync(self):
         self._ck(lib().mpcd_sync(self.h))
+
+    def set_flight(self, on=True):
+        """the free-flight schedule of mpcd_step (on by default; bit-identical results)"""
+        self._ck(lib().mpcd_set_flight(self.h, 1 if on else 0))
+
+    def flight_near(self):
+        """near particles of the last free-flight step"""
+        n = C.c_int32(0)
+        self._ck(lib().mpcd_get_flight(self.h, C.byref(n)))
+        return int(n.value)
 
     def diag(self):
         d = Diag()

@@ -53,6 +53,11 @@ struct mpcd_ctx {
   bool own_stream = false;
   cudaStream_t aux = nullptr;    // second stream: colloid work beside the fluid passes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // free-flight schedule (steps without a counting sort): the near particles' substeps run
+  // on nst (high priority) beside the free particles' pass on the context's stream
+  cudaStream_t nst = nullptr;
+  cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr;
+  bool flight = true;
   cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
   cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_finp[2] = {nullptr, nullptr};
 
@@ -338,9 +343,121 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
   cudaStreamWaitEvent(c->stream, c->ev_finp[n & 1], 0);
 }
 
+// One substep of the FP32 free-flight schedule on stream s: the pass over the near list,
+// the colloid side work beside it and the event pass, then the colloid finish.
+static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
+  const SysF64 &S = c->S;
+  const int n = S.n_sub;
+  const int flags = l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE);
+  const bool fork = S.Nc > 0;
+  if (fork) {
+    cudaEventRecord(c->ev_fork, s);
+    cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+  }
+  launch_on(c, s, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8, 256, S,
+            l, c->fbuf);
+  if (fork) {
+    launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0);
+    cudaEventRecord(c->ev_join, c->aux);
+  }
+  launch_on(c, s, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
+            c->fbuf);
+  if (fork) cudaStreamWaitEvent(s, c->ev_join, 0);
+  enq_fin_on(c, s, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+}
+
+// One step of the FP32 form in the free-flight schedule (steps without a counting sort).
+//   side stream: the flight table (from the colloids' positions at the start of the
+//                step), then run()'s rear-shell test;
+//   main:        the cell pass; the rotation with the classification (it needs the table);
+//                then the free particles' whole step, beside
+//   near stream: (high priority) run()'s kick (it needs the shell test; the kicked particles
+//                are all near), the colloid kick and the n_sub substeps of the near list;
+//   main:        the end of the step, after both.
+static void enq_step_flight32(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  const int n = S.n_sub;
+  cudaEventRecord(c->ev_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+  launch_on(c, c->aux, "k_flight_table", k_flight_table32, S.Nc > 0 ? S.Nc : 1, 128, S);
+  cudaEventRecord(c->ev_tab, c->aux);
+  if (S.Nc > 0) enq_run_shell(c, c->aux, c->fbuf);
+  cudaEventRecord(c->ev_join, c->aux);
+  launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
+  cudaStreamWaitEvent(c->stream, c->ev_tab, 0);
+  launch(c, "k_rotate_classify", k_rotate_classify32, blocks_for(S.N, 256), 256, S, c->fbuf);
+  cudaEventRecord(c->ev_cls, c->stream);
+  cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
+  cudaStreamWaitEvent(c->nst, c->ev_join, 0);
+  if (S.Nc > 0) launch_on(c, c->nst, "k_run_kick", k_run_kick32, 152 * 4, 256, S, c->fbuf);
+  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
+  for (int l = 1; l <= n; ++l) enq_substep_near32(c, c->nst, l);
+  cudaEventRecord(c->ev_end, c->nst);
+  launch(c, "k_free_flight", k_free_flight32, blocks_for(S.N, 256), 256, S, c->fbuf);
+  cudaStreamWaitEvent(c->stream, c->ev_end, 0);
+  launch(c, "k_end_step", k_end_step, 1, 256, S);
+}
+
+// One step of the FP64 form in the free-flight schedule (steps without a counting sort):
+// as the FP32 form's, with the FP64 substeps overlapped as in enq_substeps_overlapped
+// (the near list's streaming passes on the near stream, events and colloid finish on the
+// event stream, the side work on the side stream) and the near particles' binning after
+// the last streaming pass.
+static void enq_step_flight64(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  const int n = S.n_sub;
+  const bool nc = S.Nc > 0;
+  cudaEventRecord(c->ev_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+  launch_on(c, c->aux, "k_flight_table", k_flight_table32, nc ? S.Nc : 1, 128, S);
+  cudaEventRecord(c->ev_tab, c->aux);
+  if (nc) enq_run_shell(c, c->aux, c->fbuf);
+  cudaEventRecord(c->ev_join, c->aux);
+  launch(c, "k_cell_prep", k_cell_prep, prep_blocks(S), 256, S);
+  cudaStreamWaitEvent(c->stream, c->ev_tab, 0);
+  launch(c, "k_rotate_classify", k_rotate_classify, blocks_for(S.N, 256), 256, S, c->fbuf);
+  cudaEventRecord(c->ev_cls, c->stream);
+  cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
+  cudaStreamWaitEvent(c->nst, c->ev_join, 0);
+  if (nc) launch_on(c, c->nst, "k_run_kick", k_run_kick, 152 * 4, 256, S, c->fbuf);
+  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
+  cudaEventRecord(c->ev_start, c->nst);
+  cudaStreamWaitEvent(c->evs, c->ev_start, 0);
+  if (nc) cudaStreamWaitEvent(c->aux, c->ev_start, 0);
+  for (int l = 1; l <= n; ++l) {
+    const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
+    if (l >= 3) cudaStreamWaitEvent(c->nst, c->ev_finp[l & 1], 0);
+    launch_on(c, c->nst, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel_near(flags), c->n_sm * 5, 256,
+              S, l, c->fbuf);
+    cudaEventRecord(c->ev_str, c->nst);
+    if (l == n) launch_on(c, c->nst, "k_bin_near", k_bin_near, c->n_sm * 4, 256, S, c->fbuf);
+    if (nc) {
+      if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
+      launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0);
+      cudaEventRecord(c->ev_aux, c->aux);
+    }
+    cudaStreamWaitEvent(c->evs, c->ev_str, 0);
+    launch_on(c, c->evs, "k_events", event_kernel(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
+              c->fbuf);
+    if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
+    enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+    cudaEventRecord(c->ev_finp[l & 1], c->evs);
+  }
+  cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
+  cudaEventRecord(c->ev_end, c->nst);
+  launch(c, "k_free_flight", k_free_flight, blocks_for(S.N, 256), 256, S, c->fbuf);
+  cudaStreamWaitEvent(c->stream, c->ev_end, 0);
+  launch(c, "k_end_step", k_end_step, 1, 256, S);
+}
+
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:25-38)
 static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
+  if (c->flight && !sort) {
+    if (c->S.precision == MPCD_FP32C) enq_step_flight32(c);
+    else enq_step_flight64(c);
+    return;
+  }
   enq_rotation_run(c, sort);
   enq_fin(c, M_KICK | M_ADVANCE, 0);
   if (c->S.precision == MPCD_FP64) {
@@ -505,6 +622,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.dtf = (float)dt;
   S.kick32 = (float)(p.mass_colloid * p.v0 / p.mass_fl);
   S.vmaxf = (float)vmax;
+  // free flight: a particle moving further than 5 thermal speeds' worth in a step is near
+  S.flight_rv = (float)(5.0 * vth * p.ndt);
   // the FP64 form sums displacements w = v dt, the FP32 form velocities
   const double wmax = p.precision == MPCD_FP64 ? vmax * dt : vmax;
   // one scale for the sums of w and |w|^2: max_per_cell * max(wmax, 3 wmax^2) * 2^kw < 2^62
@@ -563,6 +682,9 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.shell = m.get<ShellRec>(S.shell_cap);
   S.events_cap = S.N / 16 + 65536;
   S.events = m.get<int>(S.events_cap);
+  S.near = m.get<int>(N);
+  S.fnear = m.get<uint8_t>(N);
+  S.ftab = m.get<FlightCell>(S.C);
   if (S.precision == MPCD_FP64) {
     S.newrec[0] = m.get<EventRec>(S.events_cap);
     S.newrec[1] = m.get<EventRec>(S.events_cap);
@@ -612,8 +734,12 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaStreamCreateWithPriority(&c->evs, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->nst, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_cls, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_end, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_str, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_aux, cudaEventDisableTiming) != cudaSuccess ||
@@ -646,10 +772,12 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   if (c->evs) cudaStreamDestroy(c->evs);
+  if (c->nst) cudaStreamDestroy(c->nst);
   for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc, (void *)c->box_cell,
                   (void *)c->box_occ, (void *)c->box_nn})
     if (q) cudaFree(q);
-  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_start, c->ev_str, c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_tab, c->ev_cls, c->ev_end, c->ev_start, c->ev_str, c->ev_aux,
+                        c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
   delete c;
   return MPCD_OK;
@@ -753,6 +881,7 @@ static int invalidate_tables(mpcd_ctx *c) {
   for (int b = 0; b < 2; ++b) CUDA_OK(c, cudaMemsetAsync(S.Tcnt[b], 0, sizeof(unsigned long long) * S.C, c->stream));
   CUDA_OK(c, cudaMemsetAsync(S.acc, 0, sizeof(CellAcc) * S.Cpad, c->stream));
   if (S.Nc) CUDA_OK(c, cudaMemsetAsync(S.exch, 0, sizeof(ExchAcc) * S.Nc, c->stream));
+  if (S.ftab) CUDA_OK(c, cudaMemsetAsync(S.ftab, 0, sizeof(FlightCell) * S.C, c->stream));
   c->setup_done = false;
   c->phase = 0;
   c->next_sub = 1;
@@ -861,6 +990,20 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
     return fail(c, MPCD_ERR_PARAM, "unknown launch");
   }
   return drop_graph(c);
+}
+
+extern "C" int mpcd_set_flight(mpcd_ctx *c, int on) {
+  if (!c) return MPCD_ERR_PARAM;
+  c->flight = on != 0;
+  return drop_graph(c);
+}
+
+extern "C" int mpcd_get_flight(mpcd_ctx *c, int32_t *near) {
+  if (!c || !near) return MPCD_ERR_PARAM;
+  int r;
+  if ((r = read_ss(c))) return r;
+  *near = c->ss_host->nnear;
+  return MPCD_OK;
 }
 
 extern "C" int64_t mpcd_get_step(const mpcd_ctx *c) {

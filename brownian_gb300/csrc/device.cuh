@@ -757,6 +757,13 @@ static __device__ void for_reach_cells(const SysF64 &S, int cb, float4 xc, float
   }
 }
 
+// grid shift of the SRD binning of step nn (rotation_mpcd draws it first,
+// cpp/rotation_mpcd.cpp:9), keyed by that step: each component a uniform minus 1/2
+static __device__ __forceinline__ void shift_of(const SysF64 &S, long long nn, double rr[3]) {
+  const uint4 r = draw4(S.key, DOM_SHIFT, 0, 0, 0, (uint32_t)nn);
+  rr[0] = u01(r.x) - 0.5; rr[1] = u01(r.y) - 0.5; rr[2] = u01(r.z) - 0.5;
+}
+
 // reach of the cell table of substep e: the run() shell on the last substep of a
 // step (its candidates are recorded there), the sphere otherwise
 static __device__ __forceinline__ float table_reach(const SysF64 &S, long long e) {

@@ -39,6 +39,16 @@ EventKernel event_kernel32(int flags);
 __global__ void k_cell_prep32(__grid_constant__ const SysF64 S);
 __global__ void k_rotate32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_rotate_sort32(__grid_constant__ const SysF64 S, int src, int dst);
+// the FP32 free-flight schedule: flight table, rotation with the classification, the free
+// particles' whole step, per-substep passes over the near list
+__global__ void k_flight_table32(__grid_constant__ const SysF64 S);
+__global__ void k_rotate_classify32(__grid_constant__ const SysF64 S, int fb);
+__global__ void k_free_flight32(__grid_constant__ const SysF64 S, int fb);
+StreamKernel stream_kernel32_near(int flags);
+__global__ void k_rotate_classify(const SysF64 S, int fb);
+__global__ void k_free_flight(const SysF64 S, int fb);
+__global__ void k_bin_near(const SysF64 S, int fb);
+StreamKernel stream_kernel_near(int flags);
 __global__ void k_run_shell32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_run_kick32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_aos_to_q(const SysF64 S, const double *pos, const double *vel, int fb);

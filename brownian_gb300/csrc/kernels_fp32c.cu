@@ -28,6 +28,16 @@ __device__ __forceinline__ uint4 pack(int cx, int cy, int cz, float ox, float oy
                     __float_as_uint(oy), __float_as_uint(oz));
 }
 
+// the SRD collision of one particle: v' = A v + b, the cell's FP32 affine map (A row-major, b)
+__device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &vy, float &vz) {
+  const float4 *m = reinterpret_cast<const float4 *>(ab);
+  float4 a = m[0], b = m[1], c = m[2];
+  float nx = fmaf(a.x, vx, fmaf(a.y, vy, fmaf(a.z, vz, c.y)));
+  float ny = fmaf(a.w, vx, fmaf(b.x, vy, fmaf(b.y, vz, c.z)));
+  float nz = fmaf(b.z, vx, fmaf(b.w, vy, fmaf(c.x, vz, c.w)));
+  vx = nx; vy = ny; vz = nz;
+}
+
 // keep the offset in [0, 1), carrying whole cells into the periodic cell index
 __device__ __forceinline__ void carry(int &c, float &o, int L) {
   if (o >= 0.f && o < 1.f) return;
@@ -277,29 +287,36 @@ __device__ __forceinline__ void finish32(const SysF64 &S, const Fluid32 &F, int 
 #define STREAM32_U_SHELL 1
 #endif
 static constexpr __host__ __device__ int stream32_u(int flags) { return (flags & F_SHELL) ? STREAM32_U_SHELL : STREAM32_U; }
-template <int FLAGS>
-static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
+// One chunk of 256 U particles: the particles i = chunk * 256 U + threadIdx.x + 256 u
+// below `count` of the fluid (NEAR false: slot i) or of the near list (NEAR true: slot
+// near[i], the free-flight schedule's per-substep passes).  The whole block calls it.
+template <int FLAGS, bool NEAR>
+static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int chunk, const int count, int l,
+                                                      int fb) {
   constexpr int flags = FLAGS;
   constexpr int U = stream32_u(FLAGS);
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const Fluid32 F = fluid32_at(S, fb);
-  const int p0 = VB * (256 * U) + threadIdx.x;
+  const int i0 = chunk * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
-  int cx[U], cy[U], cz[U];
+  int cx[U], cy[U], cz[U], pp[U];
   float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
   bool valid[U], ev[U];
   unsigned members[U];
   int cnt[U], lin[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
-    valid[u] = p < S.N;
+    const int i = i0 + 256 * u;
+    valid[u] = i < count;
     ev[u] = false;
     members[u] = 0;
     cnt[u] = 0;
     lin[u] = 0;
+    pp[u] = i;
     if (valid[u]) {
+      const int p = NEAR ? S.near[i] : i;
+      pp[u] = p;
       unpack(F.q[p], cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
       vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
     }
@@ -335,7 +352,7 @@ static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const in
         if ((flags & F_SHELL) && d2 <= rs2) members[u] |= 1u << k;
       }
     }
-    const int p = p0 + 256 * u;
+    const int p = pp[u];
     if (valid[u] && !ev[u] && (flags & F_BINROT))
       bt = bin32_term(S, rr, p, cx[u], cy[u], cz[u], ox[u], oy[u], oz[u], vx[u], vy[u], vz[u]);
     if (flags & F_BINROT) bin_add_warp(S.acc, bt.c, bt.fx, bt.fy, bt.fz, bt.f2);  // the whole warp
@@ -356,7 +373,7 @@ static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const in
   if (flags & F_SHELL) brec = block_base_n(&S.ss->nshell, nrec, lane);
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
+    const int p = pp[u];
     const unsigned mrec = mrecs[u];
     const bool has_rec = (mrec >> lane) & 1u;
     const unsigned mev = __ballot_sync(FULL, ev[u]);
@@ -398,6 +415,11 @@ static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const in
 }
 
 template <int FLAGS>
+static __device__ __forceinline__ void k_stream32_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
+  stream32_chunk<FLAGS, false>(S, VB, S.N, l, fb);
+}
+
+template <int FLAGS>
 __global__ void __launch_bounds__(256) k_stream32(__grid_constant__ const SysF64 S, int l, int fb) {
   k_stream32_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
 }
@@ -410,6 +432,148 @@ __global__ void __launch_bounds__(256) k_stream32_b(const SysF64 *Ss, const int 
 }
 
 int stream32_per_thread(int flags) { return stream32_u(flags); }
+
+// ------------------------------------------------------------ free-flight schedule
+//
+// Between two SRD collisions a fluid particle moves in a straight line unless a colloid
+// wall reflects it or run() kicks it, and both need a colloid within the run() shell
+// radius r_shell.  A particle farther than r_shell + (its travel in the step) + (the
+// colloids' largest move in the step) + slack from every colloid at the start of the
+// step can meet neither in any substep: the per-substep passes would only stream it and,
+// on the last substep, bin it.  The free-flight pass does that for such a particle
+// (k_free_flight32: the same FP32 operations substep by substep, so the same bits), beside
+// the substeps of the other particles, which the rotation pass lists (k_rotate_classify32)
+// and the per-substep passes walk (k_stream32_near).  The colloids' move is bounded by
+// n_sub cm (the colloid finish fails a step in which one moves further in a substep); a
+// particle's travel by n_sub dt |v| (particles faster than the table allows are near);
+// the slack of 0.01 covers the FP32 rounding of the distances and offsets.
+
+// reach of the flight table: colloids within it of a cell's box can come within a
+// particle's near radius of a particle in the cell
+static __device__ __forceinline__ float flight_reach(const SysF64 &S) {
+  return S.r_shell + S.flight_rv + (float)S.n_sub * S.ss->cm + 0.02f;
+}
+
+// the flight table of this step (both forms: the colloids' cell + offset copies are kept by
+// both): colloid j (its position at the start of the step) in every cell whose box comes
+// within the flight reach of it, the own box included.  A cell
+// with more than FLIGHT_CAP colloids keeps counting; its particles are all near.  Block 0
+// also empties the near list and draws the next step's grid shift for the free pass.
+__global__ void __launch_bounds__(128) k_flight_table32(__grid_constant__ const SysF64 S) {
+  const long long step = S.ss->step;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.ss->nnear = 0;
+    shift_of(S, step + 2, S.ss->rrn);
+  }
+  const int j = blockIdx.x;
+  if (j >= S.Nc) return;
+  const int b0 = (int)((step * S.n_sub - 1) & 1);
+  const float reach = flight_reach(S);
+  const float4 cq = S.Xcq[b0][j], co = S.Xco[b0][j];
+  const int K = (int)ceilf(reach) + 1, side = 2 * K + 1;
+  const int tot = side * side * side;
+  const unsigned long long tag = (unsigned long long)(unsigned)(step + 1) << 32;
+  for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+    const int ox = q % side - K, oy = (q / side) % side - K, oz = q / (side * side) - K;
+    // gap from the colloid (its cell + offset co) to the box of cell (its cell + o)
+    const float ex = ox > 0 ? (float)ox - co.x : (ox < 0 ? co.x - (float)ox - 1.f : 0.f);
+    const float ey = oy > 0 ? (float)oy - co.y : (oy < 0 ? co.y - (float)oy - 1.f : 0.f);
+    const float ez = oz > 0 ? (float)oz - co.z : (oz < 0 ? co.z - (float)oz - 1.f : 0.f);
+    if (ex * ex + ey * ey + ez * ez > reach * reach) continue;
+    int bx = ((int)cq.x + ox) % S.Lx, by = ((int)cq.y + oy) % S.Ly, bz = ((int)cq.z + oz) % S.Lz;
+    bx += bx < 0 ? S.Lx : 0; by += by < 0 ? S.Ly : 0; bz += bz < 0 ? S.Lz : 0;
+    FlightCell *fc = S.ftab + (bx + S.Lx * (by + S.Ly * bz));
+    atomicMax(&fc->tc, tag);
+    const int slot = (int)(unsigned)atomicAdd(&fc->tc, 1ull);
+    if (slot < FLIGHT_CAP) fc->id[slot] = (uint16_t)j;
+  }
+}
+
+// rotation_mpcd of one particle (the SRD map of its cell) and its classification: a near
+// particle is flagged and appended to the near list (one atomic per block).
+// Non-sorting steps (the particles keep their slots).
+__global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ const SysF64 S, int fb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < S.N;
+  const Fluid32 F = fluid32_at(S, fb);
+  const long long step = S.ss->step;
+  const int b0 = (int)((step * S.n_sub - 1) & 1);
+  bool near = false;
+  if (valid) {
+    const int c = S.rotcell[p];
+    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+    int cx, cy, cz;
+    float ox, oy, oz;
+    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    const bool inb = cx < S.Lx && cy < S.Ly && cz < S.Lz;  // (a record within the box)
+    const FlightCell *fc = S.ftab + (inb ? cx + S.Lx * (cy + S.Ly * cz) : 0);
+    const uint4 w0 = reinterpret_cast<const uint4 *>(fc)[0], w1 = reinterpret_cast<const uint4 *>(fc)[1];
+    if (c < S.C) apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
+    F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+    const float travel = (float)S.n_sub * S.dtf * sqrtf(vx * vx + vy * vy + vz * vz);
+    const int cnt = tcount(((unsigned long long)w0.y << 32) | w0.x, step);
+    if (!inb || !(travel <= S.flight_rv) || cnt > FLIGHT_CAP) {
+      near = true;  // faster than the table allows (or not finite), or a crowded cell
+    } else if (cnt > 0) {
+      const float r = S.r_shell + travel + (float)S.n_sub * S.ss->cm + 0.01f, r2 = r * r;
+      const unsigned ids[6] = {w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+      const float4 *Xq = S.Xcq[b0], *Xo = S.Xco[b0];
+      for (int k = 0; k < cnt; ++k) {
+        const int j = (int)((ids[k >> 1] >> (16 * (k & 1))) & 0xFFFFu);
+        const float4 cq = Xq[j], co = Xo[j];
+        const float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly),
+                    dz = rel(cz, oz, cq.z, co.z, S.Lz);
+        near = near || !(dx * dx + dy * dy + dz * dz > r2);
+      }
+    }
+    S.fnear[p] = near ? 1 : 0;
+  }
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(FULL, near);
+  const int base = block_base_n(&S.ss->nnear, __popc(m), lane);
+  if (near) S.near[base + __popc(m & ((1u << lane) - 1u))] = p;
+}
+
+// the free particles' whole step: n_sub streaming substeps (update_pos_mpcd, the
+// streaming passes' operations in order) and the binning of the last substep with the
+// next step's grid shift.  Runs beside the near particles' substeps, which touch none of
+// its particles.
+__global__ void __launch_bounds__(256) k_free_flight32(__grid_constant__ const SysF64 S, int fb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const Fluid32 F = fluid32_at(S, fb);
+  BinTerm32 bt{-1, 0, 0, 0, 0};
+  if (p < S.N && !S.fnear[p]) {
+    int cx, cy, cz;
+    float ox, oy, oz;
+    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    const float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+    for (int l = 0; l < S.n_sub; ++l) {
+      ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
+      carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+    }
+    const float rr[3] = {(float)S.ss->rrn[0], (float)S.ss->rrn[1], (float)S.ss->rrn[2]};
+    bt = bin32_term(S, rr, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+    F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+  }
+  bin_add_warp(S.acc, bt.c, bt.fx, bt.fy, bt.fz, bt.f2);  // the whole warp
+}
+
+// the per-substep pass over the near list (grid-stride over chunks of 256 U)
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32_near(__grid_constant__ const SysF64 S, int l, int fb) {
+  const int count = S.ss->nnear;
+  constexpr int per = 256 * stream32_u(FLAGS);
+  for (int chunk = blockIdx.x; chunk * per < count; chunk += gridDim.x)
+    stream32_chunk<FLAGS, true>(S, chunk, count, l, fb);
+}
+
+StreamKernel stream_kernel32_near(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_stream32_near<F_STREAM | F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream32_near<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
+  }
+  return nullptr;
+}
 
 // wall collisions of the listed particles in colloid order, then (last substep)
 // their run() record and binning; one particle per lane
@@ -577,15 +741,6 @@ __global__ void __launch_bounds__(256) k_cell_prep32(__grid_constant__ const Sys
 __global__ void __launch_bounds__(256) k_cell_prep32_b(const SysF64 *Ss, const int *boff, int nrep) {
   __shared__ SysF64 sS;
   batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_cell_prep32_body(sS, VB, NVB); });
-}
-
-__device__ __forceinline__ void apply_map32(const float *ab, float &vx, float &vy, float &vz) {
-  const float4 *m = reinterpret_cast<const float4 *>(ab);
-  float4 a = m[0], b = m[1], c = m[2];
-  float nx = fmaf(a.x, vx, fmaf(a.y, vy, fmaf(a.z, vz, c.y)));
-  float ny = fmaf(a.w, vx, fmaf(b.x, vy, fmaf(b.y, vz, c.z)));
-  float nz = fmaf(b.z, vx, fmaf(b.w, vy, fmaf(c.x, vz, c.w)));
-  vx = nx; vy = ny; vz = nz;
 }
 
 static __device__ __forceinline__ void k_rotate32_body(const SysF64 &S, const int VB, const int NVB, int fb) {

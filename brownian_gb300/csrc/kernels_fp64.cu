@@ -30,10 +30,10 @@ struct BinTerm {
   long long fx, fy, fz, f2;
 };
 
-__device__ __forceinline__ BinTerm bin_term(const SysF64 &S, int p, double x, double y, double z, double wx,
-                                            double wy, double wz) {
+// (rr: the grid shift of that binning)
+__device__ __forceinline__ BinTerm bin_term(const SysF64 &S, const double *rr, int p, double x, double y, double z,
+                                            double wx, double wy, double wz) {
   // (1 + mod(pos + rr, len).cell(len), cpp/rotation_mpcd.cpp:11)
-  const double *rr = S.ss->rr;
   double ax = ref_mod(__dadd_rn(x, rr[0]), S.dx), ay = ref_mod(__dadd_rn(y, rr[1]), S.dy),
          az = ref_mod(__dadd_rn(z, rr[2]), S.dz);
   bool alias;
@@ -51,7 +51,7 @@ __device__ __forceinline__ BinTerm bin_term(const SysF64 &S, int p, double x, do
 // the exact sums of the SRD binning for the next step: cell number, count, w, |w|^2
 __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double x, double y, double z, double wx,
                                                  double wy, double wz) {
-  const BinTerm t = bin_term(S, p, x, y, z, wx, wy, wz);
+  const BinTerm t = bin_term(S, S.ss->rr, p, x, y, z, wx, wy, wz);
   bin_add(S.acc + t.c, 1, t.fx, t.fy, t.fz, t.f2);
 }
 
@@ -74,16 +74,18 @@ __device__ __forceinline__ void bin_for_rotation(const SysF64 &S, int p, double 
 #define STREAM64_U_SHELL 1
 #endif
 static constexpr __host__ __device__ int stream64_u(int flags) { return (flags & F_SHELL) ? STREAM64_U_SHELL : STREAM64_U; }
-// Five blocks per SM (48 registers, a few spilled to L1) measured faster than four
-// without spills.
-template <int FLAGS>
-__global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb) {
+// One chunk of 256 U particles: i = chunk * 256 U + threadIdx.x + 256 u below `count`,
+// slot i of the fluid (NEAR false) or slot near[i] (NEAR true: the free-flight schedule's
+// passes over the near list).  The whole block calls it.
+template <int FLAGS, bool NEAR>
+static __device__ __forceinline__ void stream64_chunk(const SysF64 &S, const int chunk, const int count, int l,
+                                                      int fb) {
   constexpr int flags = FLAGS;
   constexpr int U = stream64_u(FLAGS);
   const long long step = S.ss->step;
   const long long gs = step * S.n_sub + (l - 1);
   const Fluid F = fluid_at(S, fb);
-  const int p0 = blockIdx.x * (256 * U) + threadIdx.x;
+  const int i0 = chunk * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
   // F_PIPE: the colloid positions of the previous substep (this substep's are being
   // computed meanwhile) and the displacement bound as margin; pending particles
@@ -94,19 +96,22 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
   double x[U], y[U], z[U], wx[U], wy[U], wz[U];
   bool valid[U], ev[U];
   unsigned members[U];  // run() shell members among the cell-table slots
-  int cnt[U], lin[U];
+  int cnt[U], lin[U], pp[U];
   uint8_t pd[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
-    const int p = p0 + 256 * u;
-    valid[u] = p < S.N;
+    const int i = i0 + 256 * u;
+    valid[u] = i < count;
     ev[u] = false;
     members[u] = 0;
     cnt[u] = 0;
     lin[u] = 0;
     pd[u] = 0;
+    pp[u] = i;
     wx[u] = wy[u] = wz[u] = 0;
     if (valid[u]) {
+      const int p = NEAR ? S.near[i] : i;
+      pp[u] = p;
       x[u] = F.x[p]; y[u] = F.y[p]; z[u] = F.z[p];
       if (flags & (F_STREAM | F_BINROT | F_COLLIDE)) { wx[u] = F.wx[p]; wy[u] = F.wy[p]; wz[u] = F.wz[p]; }
       if (flags & F_PIPE) pd[u] = S.pend[p];
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
         }
       }
     }
-    const int p = p0 + 256 * u;
+    const int p = pp[u];
     if (valid[u]) {
       if (!ev[u] && (flags & F_BINROT)) bin_for_rotation(S, p, x[u], y[u], z[u], wx[u], wy[u], wz[u]);
       if (flags & F_STREAM) { F.x[p] = x[u]; F.y[p] = y[u]; F.z[p] = z[u]; }
@@ -179,7 +184,7 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     if (!(flags & F_SHELL)) break;
-    const int p = p0 + 256 * u;
+    const int p = pp[u];
     const bool has_rec = valid[u] && !ev[u] && members[u] != 0;
     const unsigned mrec = __ballot_sync(FULL, has_rec);
     const int brec = block_base(&S.ss->nshell, mrec, lane);
@@ -209,6 +214,22 @@ __global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb
       }
     }
   }
+}
+
+// Five blocks per SM (48 registers, a few spilled to L1) measured faster than four
+// without spills.
+template <int FLAGS>
+__global__ void __launch_bounds__(256, 5) k_stream(const SysF64 S, int l, int fb) {
+  stream64_chunk<FLAGS, false>(S, blockIdx.x, S.N, l, fb);
+}
+
+// the same over the near list of the free-flight schedule (grid-stride over chunks)
+template <int FLAGS>
+__global__ void __launch_bounds__(256, 5) k_stream_near(const SysF64 S, int l, int fb) {
+  const int count = S.ss->nnear;
+  constexpr int per = 256 * stream64_u(FLAGS);
+  for (int chunk = blockIdx.x; chunk * per < count; chunk += gridDim.x)
+    stream64_chunk<FLAGS, true>(S, chunk, count, l, fb);
 }
 
 int stream64_per_thread(int flags) { return stream64_u(flags); }
@@ -335,9 +356,114 @@ __global__ void __launch_bounds__(256) k_bin(const SysF64 S, int fb) {
   for (int base = blockIdx.x * blockDim.x; base < S.N; base += gridDim.x * blockDim.x) {
     const int p = base + threadIdx.x;
     BinTerm t{-1, 0, 0, 0, 0};
-    if (p < S.N && !S.pend[p]) t = bin_term(S, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
+    if (p < S.N && !S.pend[p]) t = bin_term(S, S.ss->rr, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
     bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);
   }
+}
+
+// ------------------------------------------------------------ free-flight schedule
+// (the FP64 form's kernels; the schedule and the flight table are described with the FP32
+// form's, kernels_fp32c.cu)
+
+// the last substep's binning of the near particles the streaming pass finished (pending
+// ones are binned by the event pass)
+__global__ void __launch_bounds__(256) k_bin_near(const SysF64 S, int fb) {
+  const Fluid F = fluid_at(S, fb);
+  const int count = S.ss->nnear;
+  for (int base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+    const int i = base + threadIdx.x;
+    BinTerm t{-1, 0, 0, 0, 0};
+    if (i < count) {
+      const int p = S.near[i];
+      if (!S.pend[p]) t = bin_term(S, S.ss->rr, p, F.x[p], F.y[p], F.z[p], F.wx[p], F.wy[p], F.wz[p]);
+    }
+    bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);
+  }
+}
+
+// rotation_mpcd of one particle (w' = A w + b of its cell, as k_rotate) and its
+// classification against the flight table: a near particle is flagged and listed (one
+// atomic per block).  Non-sorting steps.
+__global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < S.N;
+  const Fluid F = fluid_at(S, fb);
+  const long long step = S.ss->step;
+  const int b0 = (int)((step * S.n_sub - 1) & 1);
+  bool near = false;
+  if (valid) {
+    S.pend[p] = 0;  // no particle is pending at the start of a step
+    const int c = S.rotcell[p];
+    double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
+    const float px = d2f_trunc(F.x[p]), py = d2f_trunc(F.y[p]), pz = d2f_trunc(F.z[p]);
+    int cx = (int)px, cy = (int)py, cz = (int)pz;  // positions in (0, L]: L is cell 0
+    cx -= cx == S.Lx ? S.Lx : 0; cy -= cy == S.Ly ? S.Ly : 0; cz -= cz == S.Lz ? S.Lz : 0;
+    // a position outside the box (a state that is not finite) reads no table: near
+    const bool inb = cx >= 0 && cx < S.Lx && cy >= 0 && cy < S.Ly && cz >= 0 && cz < S.Lz;
+    const FlightCell *fc = S.ftab + (inb ? cx + S.Lx * (cy + S.Ly * cz) : 0);
+    const uint4 w0 = reinterpret_cast<const uint4 *>(fc)[0], w1 = reinterpret_cast<const uint4 *>(fc)[1];
+    if (c < S.C) {
+      const double2 *ab = reinterpret_cast<const double2 *>(S.cell_ab + (size_t)c * 12);
+      double2 a01 = ab[0], a23 = ab[1], a45 = ab[2], a67 = ab[3], a8b0 = ab[4], b12 = ab[5];
+      const double nx = fma(a01.x, wx, fma(a01.y, wy, fma(a23.x, wz, a8b0.y)));
+      const double ny = fma(a23.y, wx, fma(a45.x, wy, fma(a45.y, wz, b12.x)));
+      const double nz = fma(a67.x, wx, fma(a67.y, wy, fma(a8b0.x, wz, b12.y)));
+      wx = nx; wy = ny; wz = nz;
+      F.wx[p] = wx; F.wy[p] = wy; F.wz[p] = wz;
+    }
+    const float fx = (float)wx, fy = (float)wy, fz = (float)wz;
+    const float travel = (float)S.n_sub * sqrtf(fx * fx + fy * fy + fz * fz);  // n_sub |w| = ndt |v|
+    const int cnt = tcount(((unsigned long long)w0.y << 32) | w0.x, step);
+    if (!inb || !(travel <= S.flight_rv) || cnt > FLIGHT_CAP) {
+      near = true;  // faster than the table allows (or not finite), or a crowded cell
+    } else if (cnt > 0) {
+      const float r = S.r_shell + travel + (float)S.n_sub * S.ss->cm + 0.01f, r2 = r * r;
+      const unsigned ids[6] = {w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+      const float4 *Xf = S.Xf[b0];
+      for (int k = 0; k < cnt; ++k) {
+        const int j = (int)((ids[k >> 1] >> (16 * (k & 1))) & 0xFFFFu);
+        const float4 q = Xf[j];
+        const float dx = wrap_half(q.x - px, S.Lxf), dy = wrap_half(q.y - py, S.Lyf), dz = wrap_half(q.z - pz, S.Lzf);
+        near = near || !(dx * dx + dy * dy + dz * dz > r2);
+      }
+    }
+    S.fnear[p] = near ? 1 : 0;
+  }
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(FULL, near);
+  const int base = block_base_n(&S.ss->nnear, __popc(m), lane);
+  if (near) S.near[base + __popc(m & ((1u << lane) - 1u))] = p;
+}
+
+// the free particles' whole step: update_pos_mpcd of every substep (pos = mod(pos +
+// vel dt, len), cpp/update.cpp:56-60, the streaming passes' operations in order) and the
+// binning of the last substep with the next step's grid shift, beside the near particles'
+// substeps, which touch none of its particles
+__global__ void __launch_bounds__(256) k_free_flight(const SysF64 S, int fb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const Fluid F = fluid_at(S, fb);
+  BinTerm t{-1, 0, 0, 0, 0};
+  if (p < S.N && !S.fnear[p]) {
+    double x = F.x[p], y = F.y[p], z = F.z[p];
+    const double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
+    for (int l = 0; l < S.n_sub; ++l) {
+      x = ref_mod(__dadd_rn(x, wx), S.dx);
+      y = ref_mod(__dadd_rn(y, wy), S.dy);
+      z = ref_mod(__dadd_rn(z, wz), S.dz);
+    }
+    t = bin_term(S, S.ss->rrn, p, x, y, z, wx, wy, wz);
+    F.x[p] = x; F.y[p] = y; F.z[p] = z;
+  }
+  bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);  // the whole warp
+}
+
+StreamKernel stream_kernel_near(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE | F_PIPE: return k_stream_near<F_STREAM | F_COLLIDE | F_PIPE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE:
+      return k_stream_near<F_STREAM | F_COLLIDE | F_SHELL | F_PIPE>;
+  }
+  return nullptr;
 }
 
 StreamKernel stream_kernel(int flags) {
@@ -631,9 +757,12 @@ __device__ __forceinline__ void colloid_q(const SysF64 &S, int b, int j, d3 X) {
 // of that step draws it first, cpp/rotation_mpcd.cpp:9), keyed by that step
 __device__ __forceinline__ void set_shift(const SysF64 &S, long long nn) {
   S.ss->nshell = 0;
-  uint4 r = draw4(S.key, DOM_SHIFT, 0, 0, 0, (uint32_t)nn);
-  S.ss->rr[0] = u01(r.x) - 0.5; S.ss->rr[1] = u01(r.y) - 0.5; S.ss->rr[2] = u01(r.z) - 0.5;
-  for (int k = 0; k < 3; ++k) S.ss->rrf[k] = (float)S.ss->rr[k];
+  double rr[3];
+  shift_of(S, nn, rr);
+  for (int k = 0; k < 3; ++k) {
+    S.ss->rr[k] = rr[k];
+    S.ss->rrf[k] = (float)rr[k];
+  }
 }
 
 // One warp per colloid (warp w of block b holds colloid b + gridDim.x * w), its
@@ -830,13 +959,14 @@ static __device__ __forceinline__ void k_end_step_body(const SysF64 &S, const in
   // run()'s shell counts start from zero for the next step (its rear-shell test runs beside
   // the next step's cell pass, so the cell pass cannot clear them)
   for (int j = threadIdx.x; j < S.Nc; j += blockDim.x) S.shell_cnt[j] = 0;
-  if (S.precision == MPCD_FP64 && S.Nc > 0) {
+  if (S.Nc > 0) {
     // the next step's colloid margin: twice the largest displacement a substep gives at
     // the colloids' present speeds, within [0.005, the static bound], and never below the
-    // move the next step's first streaming pass assumes (from the last substep's positions
-    // to the present ones, already checked against this step's margin; from the FP32
-    // copies of the positions, plus 2e-5 for their rounding).  A colloid that moves further
-    // in a substep fails the step (the finish checks every move).
+    // move the FP64 form's next first streaming pass assumes (from the last substep's
+    // positions to the present ones, already checked against this step's margin; from the
+    // FP32 copies of the positions, plus 2e-5 for their rounding).  A colloid that moves
+    // further in a substep fails the step (the finish checks every move), so the FP32
+    // form's free-flight classification may take n_sub times it as the colloids' move.
     __shared__ float s_vm[32], s_dm[32];
     const long long g = (S.ss->step + 1) * S.n_sub;  // the substep the colloids are at
     const float4 *Fc = S.Xf[g & 1], *Fp = S.Xf[(g - 1) & 1];

@@ -64,10 +64,21 @@ struct StepState {
   long long ev_total;  // events summed over substeps (diagnostics)
   double rr[3];     // grid shift of the SRD binning the next streaming pass performs
   float rrf[3];     // the same, FP32
-  // FP64 form: the bound on a colloid's displacement in one substep the streaming pass's
-  // prefilter uses as margin this step and the colloid finish checks (cm2 = cm^2)
+  // the bound on a colloid's displacement in one substep the colloid finish checks this
+  // step (cm2 = cm^2): the FP64 form's streaming pass uses it as margin, the FP32 form's
+  // free-flight classification as the colloids' move over the step (n_sub cm)
   float cm;
   double cm2;
+  int nnear;        // free-flight schedule: particles listed for the near passes this step
+  double rrn[3];    // free-flight schedule: the next step's grid shift (the free pass bins with it)
+};
+
+// one cell of the FP32 form's flight table: (step + 1) << 32 | count, and the first
+// FLIGHT_CAP colloids (a cell with more is treated as near for all its particles)
+constexpr int FLIGHT_CAP = 12;
+struct __align__(32) FlightCell {
+  unsigned long long tc;
+  uint16_t id[FLIGHT_CAP];
 };
 
 struct SysF64 {
@@ -167,6 +178,15 @@ struct SysF64 {
   float vmaxf;         // speed bound of the exact cell sums
   float4 *Xcq[2];      // colloid cell (integer-valued floats), double-buffered like X
   float4 *Xco[2];      // colloid offset within the cell
+  // free-flight schedule: a particle that no colloid can reach during a step is streamed
+  // through all its substeps by one pass beside the substeps of the others, which the
+  // rotation pass lists in near[] for the per-substep passes.  The flight table lists per
+  // cell the colloids that come within the flight reach of it at the start of the step
+  // (tag step + 1, like Tcnt).
+  int *near;                    // [N] slots of the near particles
+  uint8_t *fnear;               // [N] 1: the slot's particle is near this step
+  FlightCell *ftab;             // [C]
+  float flight_rv;              // travel allowance: particles moving further in a step are near
   // step state
   StepState *ss;
   double *pot_part;    // [Nc] per-colloid share of the WCA potential

@@ -171,6 +171,16 @@ int mpcd_step(mpcd_ctx *c, int nsteps);
  * enqueued before them (they synchronise). */
 int mpcd_step_async(mpcd_ctx *c, int nsteps);
 int mpcd_sync(mpcd_ctx *c);
+/* The free-flight schedule (on by default, both forms), used by mpcd_step on the steps
+ * without a counting sort: a fluid particle that no colloid can reach during the step (farther
+ * from every colloid at its start than the run() shell radius sigma/2 + 1/2 plus its own travel
+ * in the step plus n_sub times the colloids' bound on a substep's move) is streamed through all
+ * substeps and binned by one pass, with the operations the substep passes would apply to it,
+ * beside the substeps of the other (near) particles, which the substep passes walk alone.  The
+ * results are those of the schedule without it, bit for bit.  mpcd_get_flight gives the near
+ * particles of the last step that used it. */
+int mpcd_set_flight(mpcd_ctx *c, int on);
+int mpcd_get_flight(mpcd_ctx *c, int32_t *near);
 /* diagnostics of the state now (cpp/active_brownian.cpp:39-55) */
 int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out);
 

@@ -113,6 +113,32 @@ def test_routine_calls_equal_fused_step():
     assert a.step_count == b.step_count == 3
 
 
+@pytest.mark.parametrize("sort_every", [-1, 3])
+def test_free_flight_schedule_gives_the_same_bits(sort_every):
+    """The free-flight schedule (the particles no colloid can reach in a step streamed
+    through all its substeps by one pass beside the near particles' substeps) against the
+    same steps without it: every array bit for bit after six steps of a 24^3 system with 20
+    active colloids, and the next binning."""
+    _, a = make_pair(24, 138240, 20, sort_every=sort_every, v0=0.05)
+    _, b = make_pair(24, 138240, 20, sort_every=sort_every, v0=0.05)
+    b.set_flight(False)
+    near = []
+    for _ in range(6):
+        a.step(1)
+        b.step(1)
+        near.append(a.flight_near())
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    da, db = a.diag(), b.diag()
+    assert da["events"] == db["events"] > 0
+    assert da["shell_records"] == db["shell_records"] > 0
+    assert 0 < max(near) < 0.6 * 138240, near
+    ca, oa, ra = a.rotation_binning()
+    cb, ob, rb = b.rotation_binning()
+    assert np.array_equal(ca, cb) and np.array_equal(oa, ob) and np.array_equal(ra, rb)
+
+
 def test_runs_are_deterministic():
     _, a = make_pair(12, 17280, 5)
     _, b = make_pair(12, 17280, 5)
