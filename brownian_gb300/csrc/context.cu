@@ -400,9 +400,9 @@ static void enq_step_flight32(mpcd_ctx *c) {
 
 // One step of the FP64 form in the free-flight schedule (steps without a counting sort):
 // as the FP32 form's, with the FP64 substeps overlapped as in enq_substeps_overlapped
-// (the near list's streaming passes on the near stream, events and colloid finish on the
-// event stream, the side work on the side stream) and the near particles' binning after
-// the last streaming pass.
+// (the near list's streaming passes on the near stream; the event pass fused with the
+// colloid side work, then the colloid finish, on the event stream) and the near
+// particles' binning after the last streaming pass.
 static void enq_step_flight64(mpcd_ctx *c) {
   const SysF64 &S = c->S;
   const int n = S.n_sub;
@@ -423,7 +423,7 @@ static void enq_step_flight64(mpcd_ctx *c) {
   enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
   cudaEventRecord(c->ev_start, c->nst);
   cudaStreamWaitEvent(c->evs, c->ev_start, 0);
-  if (nc) cudaStreamWaitEvent(c->aux, c->ev_start, 0);
+  const int nevb = c->ev_grid > 0 ? c->ev_grid : c->n_sm;
   for (int l = 1; l <= n; ++l) {
     const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
     if (l >= 3) cudaStreamWaitEvent(c->nst, c->ev_finp[l & 1], 0);
@@ -431,15 +431,11 @@ static void enq_step_flight64(mpcd_ctx *c) {
               S, l, c->fbuf);
     cudaEventRecord(c->ev_str, c->nst);
     if (l == n) launch_on(c, c->nst, "k_bin_near", k_bin_near, c->n_sm * 4, 256, S, c->fbuf);
-    if (nc) {
-      if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
-      launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0);
-      cudaEventRecord(c->ev_aux, c->aux);
-    }
+    // the event pass with the substep's colloid side work (which needs the finish of l-1,
+    // earlier on this stream)
     cudaStreamWaitEvent(c->evs, c->ev_str, 0);
-    launch_on(c, c->evs, "k_events", event_kernel(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
-              c->fbuf);
-    if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
+    launch_on(c, c->evs, "k_events_aux", event_aux_kernel(flags), nevb + (S.Nc + 1) / 2, 128, S, l, c->fbuf, nevb,
+              l >= 2 ? 1 : 0);
     enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
     cudaEventRecord(c->ev_finp[l & 1], c->evs);
   }

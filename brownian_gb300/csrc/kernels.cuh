@@ -49,6 +49,10 @@ __global__ void k_rotate_classify(const SysF64 S, int fb);
 __global__ void k_free_flight(const SysF64 S, int fb);
 __global__ void k_bin_near(const SysF64 S, int fb);
 StreamKernel stream_kernel_near(int flags);
+// the FP64 event pass fused with the substep's colloid side work (grid: nevb event blocks,
+// then one block per two colloids)
+using EventAuxKernel = void (*)(const SysF64, int, int, int, int);
+EventAuxKernel event_aux_kernel(int flags);
 __global__ void k_run_shell32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_run_kick32(__grid_constant__ const SysF64 S, int fb);
 __global__ void k_aos_to_q(const SysF64 S, const double *pos, const double *vel, int fb);

@@ -242,7 +242,7 @@ int stream64_per_thread(int flags) { return stream64_u(flags); }
 // second collision follows its first), and each particle is finished by its own
 // thread.  blockDim.x <= 128.
 template <int FLAGS>
-__global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
+static __device__ __forceinline__ void k_events_body(const SysF64 &S, const int VB, const int NVB, int l, int fb) {
   constexpr int flags = FLAGS;
   __shared__ EvState sst[128];
   __shared__ int stask[128];
@@ -259,13 +259,13 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
   const int np = (flags & F_PIPE) ? S.ss->npend : 0;
   int n = np + nn;
   if ((flags & F_PIPE) && n > S.pend_cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&S.ss->err, ERRB_EVENTS);
+    if (VB == 0 && threadIdx.x == 0) atomicOr(&S.ss->err, ERRB_EVENTS);
     n = S.pend_cap;
   }
-  // item i goes to block i % gridDim.x: the items of a substep spread over all SMs
+  // item i goes to block i % NVB: the items of a substep spread over all SMs
   EvState &st = sst[threadIdx.x];
   for (int base = 0;; base += blockDim.x) {
-    const int i = blockIdx.x + gridDim.x * (threadIdx.x + base);
+    const int i = VB + NVB * (threadIdx.x + base);
     const bool valid = i < n;
     if (!__syncthreads_or(valid)) break;  // block-uniform trip count
     const bool old = i < np;
@@ -342,6 +342,26 @@ __global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
     }
     __syncthreads();  // the next round reuses the shared state
   }
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(128) k_events(const SysF64 S, int l, int fb) {
+  k_events_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
+}
+
+// the event pass (blocks 0..nevb-1) and, after them, the colloid side work of the same
+// substep (colloid_aux: forces and orientation, two colloids per block of four warps),
+// which needs only the positions the colloid finish of the substep before computed: one
+// launch where the side work would take a second stream per substep
+template <int FLAGS>
+__global__ void __launch_bounds__(128) k_events_aux(const SysF64 S, int l, int fb, int nevb, int act) {
+  if ((int)blockIdx.x < nevb) {
+    k_events_body<FLAGS>(S, blockIdx.x, nevb, l, fb);
+    return;
+  }
+  const int j = 2 * ((int)blockIdx.x - nevb) + (threadIdx.x >> 6);
+  const long long gs = S.ss->step * S.n_sub + (l - 1);
+  if (j < S.Nc) colloid_aux(S, gs, j, act != 0, (threadIdx.x >> 5) & 1, 2);
 }
 
 // The SRD binning of the particles the last streaming pass of a step finished
@@ -455,6 +475,14 @@ __global__ void __launch_bounds__(256) k_free_flight(const SysF64 S, int fb) {
     F.x[p] = x; F.y[p] = y; F.z[p] = z;
   }
   bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);  // the whole warp
+}
+
+EventAuxKernel event_aux_kernel(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE | F_PIPE: return k_events_aux<F_COLLIDE | F_PIPE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE: return k_events_aux<F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
+  }
+  return nullptr;
 }
 
 StreamKernel stream_kernel_near(int flags) {

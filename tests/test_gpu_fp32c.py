@@ -171,6 +171,16 @@ def test_free_flight_schedule_gives_the_same_bits(sort_every):
     ca, oa, _ = a.rotation_binning()
     cb, ob, _ = b.rotation_binning()
     assert np.array_equal(ca, cb) and np.array_equal(oa, ob)
+    # a step routine by routine after them (it reads the cell tables the last free-flight
+    # step left for the next step's first substeps)
+    for sim in (a, b):
+        sim.rotation_mpcd()
+        sim.run()
+        for l in range(1, 11):
+            sim.substep(l)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
 
 
 def test_free_flight_without_colloids():
