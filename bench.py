@@ -38,10 +38,28 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L, DENSITY, NC, RADIUS = 64, 10, 500, 2.0
-# algorithmic bytes per particle: one streaming launch, and one MPCD step (10 substeps + rotation)
-STREAM_BYTES = {"fp64": 72,   # read x 24 + w 24, write x 24
-                "fp32c": 44}  # read cell+offset record 16 + velocity 12, write record 16
-STEP_BYTES = {"fp64": 808, "fp32c": 496}
+# Algorithmic bytes per particle.  The free-flight schedule (steps without a counting sort):
+# the free-flight pass reads every particle's near flag (1 B) and moves a free particle
+# through the step: FP64 reads x, w (48 B) and writes x and its next cell (28 B); FP32 reads
+# the cell+offset record and the velocity (28 B) and writes the record and the cell (20 B).
+FREE_BYTES = {"fp64": 76, "fp32c": 48}
+# one MPCD step in that schedule, with a fraction f of near particles (density 10, per-cell
+# data per particle):
+#   FP64: rotation + classification 77 (rotcell 4, w 24 read and 24 written, x 24, flag 1)
+#         + SRD map 9.6 + flight table 3.2; free pass 1 + 76 (1 - f); cell pass 13.6 and the
+#         binning's cell sums 4; near passes 10 x 77 f (index 4, x and w 48, pending mark 1,
+#         x written 24) + near binning 57 f + list 4 f
+#   FP32: rotation + classification 45 (rotcell 4, v 12 read and 12 written, record 16, flag 1)
+#         + map 4.8 + table 3.2; free pass 1 + 48 (1 - f); cell pass 8.8, cell sums 4; near
+#         passes 10 x 48 f (index 4, record 16 read and written, velocity 12) + 4 f + list 4 f
+#   (the near binning of the FP32 form is part of its last near pass)
+#   (with n substeps the near passes count n times: b = 77 n - 15 and 48 (n - 1) + 8)
+STEP_BYTES_FLIGHT = {"fp64": 184.4, "fp32c": 114.8}
+
+
+def step_bytes(precision, near_frac, n_sub=10):
+    b = 77.0 * n_sub - 15.0 if precision == "fp64" else 48.0 * (n_sub - 1) + 8.0
+    return STEP_BYTES_FLIGHT[precision] + b * near_frac
 
 
 def workload(seed=0):
@@ -121,11 +139,11 @@ def measured_peak_hbm():
 
 
 def ncu_traffic_per_particle(precision):
-    """DRAM bytes per particle of one streaming launch from the committed ncu summary."""
+    """DRAM bytes per fluid particle of one free-flight launch from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as f:
-            return float(json.load(f)[f"k_stream_{precision}"]["dram_bytes_per_particle"])
+            return float(json.load(f)[f"k_free_flight_{precision}"]["dram_bytes_per_particle"])
     except (OSError, KeyError, ValueError):
         return None
 
@@ -288,22 +306,27 @@ def measure_resident(sim, stream, precision, args, world, dist, with_clocks=True
     _barrier(dist)
     prof = sim.profile_read()
     sim.profile(False)
-    st_launches, st_ms = prof.get("k_stream", (0, 0.0))
-    t_launch = st_ms / max(st_launches, 1) / 1e3
-    achieved = STREAM_BYTES[precision] * N / t_launch / 1e9 if st_launches else None
+    near = sim.flight_near()
+    f = near / N
+    ff_launches, ff_ms = prof.get("k_free_flight", (0, 0.0))
+    t_launch = ff_ms / max(ff_launches, 1) / 1e3
+    alg = N * (1.0 + (1.0 - f) * FREE_BYTES[precision])
+    achieved = alg / t_launch / 1e9 if ff_launches else None
     peak, peak_kind = measured_peak_hbm()
     tpp = ncu_traffic_per_particle(precision)
     total = sum(x[1] for x in prof.values())
     shares = {k: {"share": round(v[1] / total, 4), "launches": v[0], "us_per_launch": round(v[1] / v[0] * 1e3, 2)}
               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
-    roof = {"bound": "hbm", "kernel": "k_stream (fluid streaming + wall-collision flagging)",
+    roof = {"bound": "hbm",
+            "kernel": "k_free_flight (the free particles' whole step: streaming and binning; the largest fluid pass, "
+                      "run beside the substeps' latency-bound chain, which sets the step time)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-            "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": STREAM_BYTES[precision] * N,
+            "traffic": (tpp * N) if tpp else None, "algorithmic_bytes": alg,
             "peak_source": f"{peak_kind} hbm_gbs (burst copy)", "launch_ms": t_launch * 1e3,
-            "launches": st_launches}
-    near = sim.flight_near() if precision == "fp32c" else None
+            "launches": ff_launches}
+    sb = step_bytes(precision, f)
     return dict(value=value, ms=ms, gpu_launches=gpu_launches, clocks=clk, roofline=roof, shares=shares,
-                step_frac=value / world * STEP_BYTES[precision] / (peak * 1e9), near=near)
+                step_frac=value / world * sb / (peak * 1e9), near=near, near_frac=f, step_bytes=sb)
 
 
 def form_statistics(replicas, steps, lag=100, every=10):
@@ -403,18 +426,26 @@ def run_ensemble(nrep, steps, rank):
     # the same replicas, each stepped by its own single-system call, one after the other:
     # each replica's step graph enqueued back to back on one stream, one synchronisation
     # per sweep over the replicas (a replica's next step needs its previous one only)
+    # First with the batched kernels' schedule (every particle through every substep), so
+    # that the ratio is the batching alone; then with the single-system free-flight schedule
     st = torch.cuda.Stream()
-    for s in ens:
-        s.set_stream(st.cuda_stream)
-        s.step(1)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+
+    def looped(flight):
         for s in ens:
-            s.step_async(1)
-        ens[0].sync()
-    for s in ens:
-        s.sync()  # every replica's device checks
-    looped_s = time.perf_counter() - t0
+            s.set_stream(st.cuda_stream)
+            s.set_flight(flight)
+            s.step(1)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for s in ens:
+                s.step_async(1)
+            ens[0].sync()
+        for s in ens:
+            s.sync()  # every replica's device checks
+        return time.perf_counter() - t0
+
+    looped_s = looped(False)
+    looped_flight_s = looped(True)
     n_particles = sum(p.n_fluid for p in P)
     ens.close()
     return {"workload": "256 replicas" if nrep == 256 else f"{nrep} replicas",
@@ -423,8 +454,12 @@ def run_ensemble(nrep, steps, rank):
             "particle_steps_per_s": n_particles * steps / batched_s,
             "looped": {"value": nrep * steps / looped_s, "unit": "replica-steps/s",
                        "how": "mpcd_step_async(1) of each replica in turn on one stream, one "
-                              "synchronisation per sweep over the replicas"},
+                              "synchronisation per sweep over the replicas; the per-substep schedule of "
+                              "the batched kernels (mpcd_set_flight(0))"},
             "speedup_vs_looped": looped_s / batched_s,
+            "looped_free_flight": {"value": nrep * steps / looped_flight_s, "unit": "replica-steps/s",
+                                   "how": "the same loop with the single-system free-flight schedule"},
+            "speedup_vs_looped_free_flight": looped_flight_s / batched_s,
             "launches_per_step": launches_per_step,
             "autotune": {"choice": tuned["choice"], "ms_per_step": tuned["ms_per_step"],
                          "trials": len(tuned["log"])},
@@ -462,12 +497,16 @@ def run_large(steps, warmup=3):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     d1 = sim.diag()
+    near_frac = sim.flight_near() / N
     sim.profile(True)
     sim.step(2)
     prof = sim.profile_read()
     sim.profile(False)
     peak = measured_peak_hbm()[0]
-    per_particle = {"k_stream": 44, "k_rotate": 28, "k_rotate_sort": 64}  # algorithmic bytes, FP32 form
+    # algorithmic bytes per fluid particle, FP32 form (the free-flight pass: the flag of every
+    # particle and the free particles' record, velocity, record and cell)
+    per_particle = {"k_stream": 44, "k_rotate": 28, "k_rotate_sort": 64, "k_rotate_classify": 45,
+                    "k_free_flight": 1.0 + (1.0 - near_frac) * FREE_BYTES["fp32c"]}
     kernels = {}
     for k, (n, tms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
         us = tms / max(n, 1) * 1e3
@@ -478,12 +517,13 @@ def run_large(steps, warmup=3):
                         "frac_of_measured_copy": gbs / peak})
         kernels[k] = row
     sim.close()
-    b_step = NSUB * 44 + 56
+    b_step = step_bytes("fp32c", near_frac, NSUB)
     ps = N / (ms / 1e3)
     return {"workload": "128^3 cells, density 10 (20,971,520 fluid particles), 2000 colloids r=3 (WCA sigma 6), "
                         "v0 0.02, Dr 0.0005, SRD angle 130 deg, 20 substeps; FP32 form",
             "steps": steps, "warmup": warmup, "ms_per_step": ms, "value": ps, "unit": "particle-steps/s",
             "hbm_roofline_frac_step": b_step * ps / (peak * 1e9), "bytes_per_particle_step": b_step,
+            "near_fraction": near_frac,
             "peak_gbs": peak, "kernels": kernels,
             "diag": {"temperature": d1["temperature_fluid"],
                      # total momentum change over the timed steps, relative to sum |p_i| of a thermal fluid
@@ -639,6 +679,8 @@ def run_ours(args, rank, world, dist):
         "data": "synthetic",
         "config": dict(config_dict(args.precision), parallelism=f"replicas x{world}"),
         "hbm_roofline_frac_step": r["step_frac"],
+        "step_bytes_per_particle": r["step_bytes"],
+        "near_fraction": r["near_frac"],
         "roofline": r["roofline"],
         "kernel_share": r["shares"],
         "e2e": e2e,
@@ -651,10 +693,9 @@ def run_ours(args, rank, world, dist):
         o = res[prec]
         line[f"form_{prec}"] = {"value": o["value"], "unit": "particle-steps/s", "ms_per_step": o["ms"] / args.steps,
                                 "speedup_vs_" + args.precision: o["value"] / r["value"],
-                                "hbm_roofline_frac_step": o["step_frac"], "roofline": o["roofline"],
+                                "hbm_roofline_frac_step": o["step_frac"], "step_bytes_per_particle": o["step_bytes"],
+                                "near_fraction": o["near_frac"], "roofline": o["roofline"],
                                 "kernel_share": o["shares"], "gpu_launches": o["gpu_launches"]}
-        if o.get("near") is not None:
-            line[f"form_{prec}"]["near_particles_last_step"] = o["near"]
     if stats:
         line["fp32c_vs_fp64"] = stats
     if ens:

@@ -56,7 +56,7 @@ struct mpcd_ctx {
   // free-flight schedule (steps without a counting sort): the near particles' substeps run
   // on nst (high priority) beside the free particles' pass on the context's stream
   cudaStream_t nst = nullptr;
-  cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr;
+  cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr, ev_list = nullptr;
   bool flight = true;
   cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
   cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_finp[2] = {nullptr, nullptr};
@@ -173,6 +173,33 @@ static cudaError_t scopy(const mpcd_ctx *c, void *dst, const void *src, size_t n
 
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// the pair-list grid for a list radius rl: per axis as many buckets as fit with width
+// at least rl (with 1e-4 to spare for the rounding of the bucket index), at most NBK_MAX
+static NListGeo nlist_geo(const mpcd_ctx *c, double rl) {
+  NListGeo g;
+  const int L[3] = {c->S.Lx, c->S.Ly, c->S.Lz};
+  for (int a = 0; a < 3; ++a) {
+    int nb = (int)floor((double)L[a] / (rl * 1.0001));
+    nb = nb < 1 ? 1 : (nb > NBK_MAX ? NBK_MAX : nb);
+    g.nb[a] = nb;
+    g.bs[a] = (double)L[a] / nb;
+  }
+  g.r2 = pow(rl, 2);
+  return g;
+}
+
+// the free-flight schedule's pair list at the positions at the start of the step, on
+// stream s (recorded as ev_list): radius r_cutoff + 2 n_sub cmargin + 0.05, within which
+// every pair that comes within r_cutoff during the step starts (each colloid moves at most
+// cmargin a substep; the colloid finish fails a step in which one moves further)
+static void enq_step_pairs(mpcd_ctx *c, cudaStream_t s) {
+  if (!c->S.vlist) return;
+  const NListGeo geo = nlist_geo(c, c->S.r_cutoff + 2.0 * c->S.n_sub * sqrt(c->S.cmargin2) + 0.05);
+  launch_on(c, s, "k_cbucket", k_cbucket, 1, 1024, c->S, (const double *)nullptr, geo);
+  launch_on(c, s, "k_nlist_step", k_nlist_step, blocks_for(c->S.Nc, 4), 128, c->S, geo);
+  cudaEventRecord(c->ev_list, s);
+}
+
 static int colloid_grid(const mpcd_ctx *c) {
   int g = (int)blocks_for((long long)c->S.Nc * 32, 128);
   return g > 0 ? g : 1;
@@ -205,7 +232,7 @@ static void enq_stream(mpcd_ctx *c, int flags, int l, int act) {
          blocks_for(c->S.N, 256 * (f32 ? stream32_per_thread(flags) : stream64_per_thread(flags))), 256, c->S, l, fb);
   if (!f32 && (flags & F_PIPE) && (flags & F_BINROT)) launch(c, "k_bin", k_bin, c->n_sm * 8, 256, c->S, fb);
   if (fork) {
-    launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act);
+    launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, act, 0);
     cudaEventRecord(c->ev_join, c->aux);
   }
   // the particles it left near a sphere surface, one per lane
@@ -330,7 +357,7 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
     if (l == n) launch(c, "k_bin", k_bin, c->n_sm * 8, 256, c->S, c->fbuf);
     if (nc) {
       if (l >= 2) cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
-      launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, l >= 2 ? 1 : 0);
+      launch_on(c, c->aux, "k_aux", k_aux, c->S.Nc, 32 * c->S.aux_nw, c->S, l, l >= 2 ? 1 : 0, 0);
       cudaEventRecord(c->ev_aux, c->aux);
     }
     cudaStreamWaitEvent(c->evs, c->ev_str, 0);
@@ -353,11 +380,12 @@ static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
   if (fork) {
     cudaEventRecord(c->ev_fork, s);
     cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+    if (l == 1 && S.vlist) cudaStreamWaitEvent(c->aux, c->ev_list, 0);
   }
   launch_on(c, s, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8, 256, S,
             l, c->fbuf);
   if (fork) {
-    launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0);
+    launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0, S.vlist);
     cudaEventRecord(c->ev_join, c->aux);
   }
   launch_on(c, s, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
@@ -381,6 +409,12 @@ static void enq_step_flight32(mpcd_ctx *c) {
   cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
   launch_on(c, c->aux, "k_flight_table", k_flight_table32, S.Nc > 0 ? S.Nc : 1, 128, S);
   cudaEventRecord(c->ev_tab, c->aux);
+  if (S.vlist) {
+    // the step's pair list on the third stream, which this schedule leaves idle; the side
+    // work of the first substep waits for it
+    cudaStreamWaitEvent(c->evs, c->ev_fork, 0);
+    enq_step_pairs(c, c->evs);
+  }
   if (S.Nc > 0) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
@@ -393,7 +427,7 @@ static void enq_step_flight32(mpcd_ctx *c) {
   enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
   for (int l = 1; l <= n; ++l) enq_substep_near32(c, c->nst, l);
   cudaEventRecord(c->ev_end, c->nst);
-  launch(c, "k_free_flight", k_free_flight32, blocks_for(S.N, 256), 256, S, c->fbuf);
+  launch(c, "k_free_flight", k_free_flight32, c->n_sm * 2, 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
 }
@@ -411,6 +445,11 @@ static void enq_step_flight64(mpcd_ctx *c) {
   cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
   launch_on(c, c->aux, "k_flight_table", k_flight_table32, nc ? S.Nc : 1, 128, S);
   cudaEventRecord(c->ev_tab, c->aux);
+  if (S.vlist) {
+    // the step's pair list on the event stream before its substeps, whose side work reads it
+    cudaStreamWaitEvent(c->evs, c->ev_fork, 0);
+    enq_step_pairs(c, c->evs);
+  }
   if (nc) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep, prep_blocks(S), 256, S);
@@ -441,7 +480,7 @@ static void enq_step_flight64(mpcd_ctx *c) {
   }
   cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
   cudaEventRecord(c->ev_end, c->nst);
-  launch(c, "k_free_flight", k_free_flight, blocks_for(S.N, 256), 256, S, c->fbuf);
+  launch(c, "k_free_flight", k_free_flight, c->n_sm * 2, 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
 }
@@ -620,6 +659,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.vmaxf = (float)vmax;
   // free flight: a particle moving further than 5 thermal speeds' worth in a step is near
   S.flight_rv = (float)(5.0 * vth * p.ndt);
+  // the free-flight steps' forces from a pair list built at the start of each step
+  S.vlist = p.n_colloid > 1 ? 1 : 0;
   // the FP64 form sums displacements w = v dt, the FP32 form velocities
   const double wmax = p.precision == MPCD_FP64 ? vmax * dt : vmax;
   // one scale for the sums of w and |w|^2: max_per_cell * max(wmax, 3 wmax^2) * 2^kw < 2^62
@@ -733,6 +774,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
       cudaStreamCreateWithPriority(&c->nst, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_cls, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_end, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_list, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess ||
@@ -772,8 +814,8 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc, (void *)c->box_cell,
                   (void *)c->box_occ, (void *)c->box_nn})
     if (q) cudaFree(q);
-  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_tab, c->ev_cls, c->ev_end, c->ev_start, c->ev_str, c->ev_aux,
-                        c->ev_finp[0], c->ev_finp[1]})
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_tab, c->ev_cls, c->ev_end, c->ev_list, c->ev_start, c->ev_str,
+                        c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
   delete c;
   return MPCD_OK;

@@ -712,6 +712,41 @@ static __device__ d3 wca_force(const SysF64 &S, const double *Xc, const float4 *
   return f;
 }
 
+// The same sum with the FP32 prefilter over colloid j's pair list instead of over every
+// colloid: the list holds (ascending) every colloid within r_cutoff plus twice the
+// colloids' largest move in the step of j at the start of the step, so it holds every
+// partner the scan of all colloids finds, and the same partners are summed in the same
+// order.
+static __device__ d3 wca_force_vlist(const SysF64 &S, const double *Xc, const float4 *Xf, int j, int lane) {
+  d3 f = mk(0, 0, 0);
+  double pot = 0;
+  const float4 xj = Xf[j];
+  const float Lx = S.Lxf, Ly = S.Lyf, Lz = S.Lzf;
+  const float iLx = __frcp_rn(Lx), iLy = __frcp_rn(Ly), iLz = __frcp_rn(Lz);
+  const float rcf = S.rcf;
+  const d3 Xj = ldv(Xc, j);
+  const int n = min(S.nbr_n[j], NBR_CAP);
+  const uint16_t *lst = S.nbr + (size_t)j * NBR_CAP;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + lane;
+    int k = 0;
+    bool cand = false;
+    if (i < n) {
+      k = lst[i];
+      const float4 xk = Xf[k];
+      const float dx = wrapf_r(xj.x - xk.x, Lx, iLx), dy = wrapf_r(xj.y - xk.y, Ly, iLy),
+                  dz = wrapf_r(xj.z - xk.z, Lz, iLz);
+      cand = dx * dx + dy * dy + dz * dz < rcf * rcf;
+    }
+    if (!__ballot_sync(FULL, cand)) continue;
+    d3 ff = mk(0, 0, 0);
+    double pt = 0;
+    const bool hit = cand && wca_pair(S, Xj, Xc, k, false, ff, pt);
+    wca_gather(hit, ff, pt, f, pot);
+  }
+  return f;
+}
+
 // The same sum over colloid j's pair list (neighbour_list_md: its partners within the
 // list radius, both below and above j, in ascending order), one partner per lane.
 static __device__ d3 wca_force_list(const SysF64 &S, const double *Xc, int j, int lane, bool want_pot, double &pot) {
@@ -802,16 +837,18 @@ static __device__ __forceinline__ void rotdiff_draw(const SysF64 &S, long long g
 // (k_aux, on a second stream beside the streaming and event passes of this
 // substep): the WCA forces at the positions X_g (compute_force_md) and the cell
 // table of substep g+1, built from X_g with a margin for the colloid's own move.
-// The colloid has `nw` (2 to 8) warps and `w` is this thread's warp among them:
+// (vlist: the forces from the pair list the free-flight schedule builds at the start of
+// each step.)  The colloid has `nw` (2 to 8) warps and `w` is this thread's warp among them:
 // the forces on warp 0, the table on warps 2.. (on warp 0 after the forces when
 // nw = 2); the pending orientation update and this substep's
 // rotational-diffusion draws on warp 1, whose lanes 0-2 take one component each.
-static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, int j, bool act, int w, int nw) {
+static __device__ __noinline__ void colloid_aux(const SysF64 &S, long long g, int j, bool act, int w, int nw,
+                                                bool vlist = false) {
   const int b = (int)(g & 1);
   const int lane = threadIdx.x & 31;
   if (w == 0) {
     double pot;
-    d3 fn = wca_force(S, S.X[b], S.Xf[b], j, lane, false, pot);
+    d3 fn = vlist ? wca_force_vlist(S, S.X[b], S.Xf[b], j, lane) : wca_force(S, S.X[b], S.Xf[b], j, lane, false, pot);
     if (lane == 0) stv(S.fnew, j, fn);
   }
   if (!S.fin_table && (w >= 2 || (w == 0 && nw == 2))) {

@@ -64,12 +64,13 @@ __global__ void k_rotate(const SysF64 S, int fb);
 __global__ void k_run_shell(const SysF64 S, int fb);
 __global__ void k_run_kick(const SysF64 S, int fb);
 __global__ void k_fin(__grid_constant__ const SysF64 S, int mode, int l);
-__global__ void k_aux(__grid_constant__ const SysF64 S, int l, int act);
+__global__ void k_aux(__grid_constant__ const SysF64 S, int l, int act, int vl);
 __global__ void k_colloid_setup(const SysF64 S);
 __global__ void k_colloid_pot(const SysF64 S, int b);
 // routine-by-routine substeps (routines.cu)
 __global__ void k_cbucket(const SysF64 S, const double *Xc, NListGeo geo);
 __global__ void k_nlist(const SysF64 S, const double *Xc, NListGeo geo);
+__global__ void k_nlist_step(const SysF64 S, NListGeo geo);
 __global__ void k_force_list(const SysF64 S, const double *Xc);
 __global__ void k_act_now(const SysF64 S, int l);
 __global__ void k_vel_colloid(const SysF64 S);

@@ -537,25 +537,28 @@ __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ con
 // the free particles' whole step: n_sub streaming substeps (update_pos_mpcd, the
 // streaming passes' operations in order) and the binning of the last substep with the
 // next step's grid shift.  Runs beside the near particles' substeps, which touch none of
-// its particles.
+// its particles; a grid of a few blocks per SM walks the fluid (it shares the SMs with the
+// substeps' latency-bound chain).
 __global__ void __launch_bounds__(256) k_free_flight32(__grid_constant__ const SysF64 S, int fb) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const Fluid32 F = fluid32_at(S, fb);
-  BinTerm32 bt{-1, 0, 0, 0, 0};
-  if (p < S.N && !S.fnear[p]) {
-    int cx, cy, cz;
-    float ox, oy, oz;
-    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
-    const float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
-    for (int l = 0; l < S.n_sub; ++l) {
-      ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
-      carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+  const float rr[3] = {(float)S.ss->rrn[0], (float)S.ss->rrn[1], (float)S.ss->rrn[2]};
+  for (int p0 = blockIdx.x * blockDim.x; p0 < S.N; p0 += gridDim.x * blockDim.x) {
+    const int p = p0 + threadIdx.x;
+    BinTerm32 bt{-1, 0, 0, 0, 0};
+    if (p < S.N && !S.fnear[p]) {
+      int cx, cy, cz;
+      float ox, oy, oz;
+      unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+      const float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+      for (int l = 0; l < S.n_sub; ++l) {
+        ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
+        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
+      }
+      bt = bin32_term(S, rr, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
+      F.q[p] = pack(cx, cy, cz, ox, oy, oz);
     }
-    const float rr[3] = {(float)S.ss->rrn[0], (float)S.ss->rrn[1], (float)S.ss->rrn[2]};
-    bt = bin32_term(S, rr, p, cx, cy, cz, ox, oy, oz, vx, vy, vz);
-    F.q[p] = pack(cx, cy, cz, ox, oy, oz);
+    bin_add_warp(S.acc, bt.c, bt.fx, bt.fy, bt.fz, bt.f2);  // the whole warp
   }
-  bin_add_warp(S.acc, bt.c, bt.fx, bt.fy, bt.fz, bt.f2);  // the whole warp
 }
 
 // the per-substep pass over the near list (grid-stride over chunks of 256 U)

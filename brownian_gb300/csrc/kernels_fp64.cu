@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(128) k_events_aux(const SysF64 S, int l, int f
   }
   const int j = 2 * ((int)blockIdx.x - nevb) + (threadIdx.x >> 6);
   const long long gs = S.ss->step * S.n_sub + (l - 1);
-  if (j < S.Nc) colloid_aux(S, gs, j, act != 0, (threadIdx.x >> 5) & 1, 2);
+  if (j < S.Nc) colloid_aux(S, gs, j, act != 0, (threadIdx.x >> 5) & 1, 2, S.vlist != 0);
 }
 
 // The SRD binning of the particles the last streaming pass of a step finished
@@ -458,23 +458,26 @@ __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb)
 // the free particles' whole step: update_pos_mpcd of every substep (pos = mod(pos +
 // vel dt, len), cpp/update.cpp:56-60, the streaming passes' operations in order) and the
 // binning of the last substep with the next step's grid shift, beside the near particles'
-// substeps, which touch none of its particles
+// substeps, which touch none of its particles.  A grid of a few blocks per SM walks the
+// fluid (it shares the SMs and their FP64 units with the substeps' latency-bound chain).
 __global__ void __launch_bounds__(256) k_free_flight(const SysF64 S, int fb) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const Fluid F = fluid_at(S, fb);
-  BinTerm t{-1, 0, 0, 0, 0};
-  if (p < S.N && !S.fnear[p]) {
-    double x = F.x[p], y = F.y[p], z = F.z[p];
-    const double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
-    for (int l = 0; l < S.n_sub; ++l) {
-      x = ref_mod(__dadd_rn(x, wx), S.dx);
-      y = ref_mod(__dadd_rn(y, wy), S.dy);
-      z = ref_mod(__dadd_rn(z, wz), S.dz);
+  for (int p0 = blockIdx.x * blockDim.x; p0 < S.N; p0 += gridDim.x * blockDim.x) {
+    const int p = p0 + threadIdx.x;
+    BinTerm t{-1, 0, 0, 0, 0};
+    if (p < S.N && !S.fnear[p]) {
+      double x = F.x[p], y = F.y[p], z = F.z[p];
+      const double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
+      for (int l = 0; l < S.n_sub; ++l) {
+        x = ref_mod(__dadd_rn(x, wx), S.dx);
+        y = ref_mod(__dadd_rn(y, wy), S.dy);
+        z = ref_mod(__dadd_rn(z, wz), S.dz);
+      }
+      t = bin_term(S, S.ss->rrn, p, x, y, z, wx, wy, wz);
+      F.x[p] = x; F.y[p] = y; F.z[p] = z;
     }
-    t = bin_term(S, S.ss->rrn, p, x, y, z, wx, wy, wz);
-    F.x[p] = x; F.y[p] = y; F.z[p] = z;
+    bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);  // the whole warp
   }
-  bin_add_warp(S.acc, t.c, t.fx, t.fy, t.fz, t.f2);  // the whole warp
 }
 
 EventAuxKernel event_aux_kernel(int flags) {
@@ -512,13 +515,15 @@ StreamKernel stream_kernel(int flags) {
 // colloid_aux of substep l (1..n_sub) as a kernel of its own (blocks of
 // S.aux_nw warps, one colloid each); `act`: with the pending orientation update
 // of substep l-1
-static __device__ __forceinline__ void k_aux_body(const SysF64 &S, const int VB, const int NVB, int l, int act) {
+static __device__ __forceinline__ void k_aux_body(const SysF64 &S, const int VB, const int NVB, int l, int act,
+                                                  bool vlist = false) {
   const long long gs = S.ss->step * S.n_sub + (l - 1);
-  if ((int)VB < S.Nc) colloid_aux(S, gs, VB, act != 0, threadIdx.x >> 5, S.aux_nw);
+  if ((int)VB < S.Nc) colloid_aux(S, gs, VB, act != 0, threadIdx.x >> 5, S.aux_nw, vlist);
 }
 
-__global__ void __launch_bounds__(256) k_aux(__grid_constant__ const SysF64 S, int l, int act) {
-  k_aux_body(S, blockIdx.x, gridDim.x, l, act);
+// (vl: the forces from the step's pair list, the free-flight schedule)
+__global__ void __launch_bounds__(256) k_aux(__grid_constant__ const SysF64 S, int l, int act, int vl) {
+  k_aux_body(S, blockIdx.x, gridDim.x, l, act, vl != 0);
 }
 
 // the same over a batch of systems (persistent: batch_for)

@@ -31,9 +31,11 @@ static __device__ __forceinline__ int bucket_of(const double *Xc, int j, const N
 
 // The colloids by bucket (a counting sort, one block of 1024 threads): bkt_start[b]
 // the first slot of bucket b in bkt_list, bkt_start[nbk] = Nc.
+// (Xc null: the positions at the start of the present step, the free-flight schedule's list)
 __global__ void __launch_bounds__(1024) k_cbucket(const SysF64 S, const double *Xc, NListGeo geo) {
   __shared__ int wsum[32];
   __shared__ int carry;
+  if (!Xc) Xc = S.X[(int)((S.ss->step * S.n_sub - 1) & 1)];
   const int nbk = geo.nb[0] * geo.nb[1] * geo.nb[2];
   for (int b = threadIdx.x; b <= nbk; b += blockDim.x) S.bkt_start[b] = 0;
   __syncthreads();
@@ -128,6 +130,88 @@ __global__ void __launch_bounds__(128) k_nlist(const SysF64 S, const double *Xc,
           n += __popc(m);
         }
       }
+  if (__any_sync(FULL, over) && lane == 0) atomicOr(&S.ss->err, ERRB_NBR);
+  n = n < NBR_CAP ? n : NBR_CAP;
+  __syncwarp();
+  uint16_t *out = S.nbr + (size_t)j * NBR_CAP;
+  for (int e = lane; e < n; e += 32) {
+    const uint16_t v = buf[e];
+    int rank = 0;
+    for (int q = 0; q < n; ++q) rank += buf[q] < v;
+    out[rank] = v;
+  }
+  if (lane == 0) S.nbr_n[j] = n;
+}
+
+// The free-flight schedule's pair list of colloid j (one warp per colloid, four per
+// block): every colloid k != j with |img(X_j - X_k)|^2 < r2 at the positions at the start
+// of the step, ascending, for the forces of the step's substeps.  The candidates of the
+// buckets next to j's are flattened across the warp (a prefix over the buckets' counts), so
+// a colloid takes a round per 32 candidates instead of a round per bucket.
+__global__ void __launch_bounds__(128) k_nlist_step(const SysF64 S, NListGeo geo) {
+  __shared__ uint16_t sbuf[4][NBR_CAP];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 4 + w;
+  if (j >= S.Nc) return;
+  const double *Xc = S.X[(int)((S.ss->step * S.n_sub - 1) & 1)];
+  const d3 Xj = ldv(Xc, j);
+  const int b0[3] = {bucket_axis(Xj.x, geo.bs[0], geo.nb[0]), bucket_axis(Xj.y, geo.bs[1], geo.nb[1]),
+                     bucket_axis(Xj.z, geo.bs[2], geo.nb[2])};
+  int lo[3], cnt3[3];
+  for (int a = 0; a < 3; ++a) {
+    if (geo.nb[a] >= 3) {
+      lo[a] = b0[a] - 1;
+      cnt3[a] = 3;
+    } else {
+      lo[a] = 0;
+      cnt3[a] = geo.nb[a];
+    }
+  }
+  const int nbb = cnt3[0] * cnt3[1] * cnt3[2];  // buckets to visit (<= 27), one per lane
+  int start = 0, cnt = 0;
+  if (lane < nbb) {
+    int bx = lo[0] + lane % cnt3[0], by = lo[1] + (lane / cnt3[0]) % cnt3[1], bz = lo[2] + lane / (cnt3[0] * cnt3[1]);
+    bx += bx < 0 ? geo.nb[0] : 0; bx -= bx >= geo.nb[0] ? geo.nb[0] : 0;
+    by += by < 0 ? geo.nb[1] : 0; by -= by >= geo.nb[1] ? geo.nb[1] : 0;
+    bz += bz < 0 ? geo.nb[2] : 0; bz -= bz >= geo.nb[2] ? geo.nb[2] : 0;
+    const int b = bx + geo.nb[0] * (by + geo.nb[1] * bz);
+    start = S.bkt_start[b];
+    cnt = S.bkt_start[b + 1] - start;
+  }
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
+  const int excl = incl - cnt;
+  uint16_t *buf = sbuf[w];
+  int n = 0;
+  bool over = false;
+  for (int t0 = 0; t0 < total; t0 += 32) {
+    const int t = t0 + lane;
+    // the bucket q holding candidate t: the last lane whose exclusive prefix is <= t
+    int q = 0;
+    for (int r = 1; r < nbb; ++r) q = __shfl_sync(FULL, excl, r) <= t ? r : q;
+    const int sq = __shfl_sync(FULL, start, q), eq = __shfl_sync(FULL, excl, q);
+    bool in = false;
+    int k = 0;
+    if (t < total) {
+      k = S.bkt_list[sq + (t - eq)];
+      if (k != j) {
+        const double tx = ref_img(__dsub_rn(Xj.x, Xc[3 * k]), S.dx), ty = ref_img(__dsub_rn(Xj.y, Xc[3 * k + 1]), S.dy),
+                     tz = ref_img(__dsub_rn(Xj.z, Xc[3 * k + 2]), S.dz);
+        in = norm2_ref(tx, ty, tz) < geo.r2;
+      }
+    }
+    const unsigned m = __ballot_sync(FULL, in);
+    const int slot = n + __popc(m & ((1u << lane) - 1u));
+    if (in) {
+      if (slot < NBR_CAP) buf[slot] = (uint16_t)k;
+      else over = true;
+    }
+    n += __popc(m);
+  }
   if (__any_sync(FULL, over) && lane == 0) atomicOr(&S.ss->err, ERRB_NBR);
   n = n < NBR_CAP ? n : NBR_CAP;
   __syncwarp();

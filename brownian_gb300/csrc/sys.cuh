@@ -187,6 +187,8 @@ struct SysF64 {
   uint8_t *fnear;               // [N] 1: the slot's particle is near this step
   FlightCell *ftab;             // [C]
   float flight_rv;              // travel allowance: particles moving further in a step are near
+  int vlist;                    // the free-flight steps compute the forces from a pair list built
+                                // at the start of the step
   // step state
   StepState *ss;
   double *pot_part;    // [Nc] per-colloid share of the WCA potential
