@@ -455,24 +455,67 @@ __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb)
   if (near) S.near[base + __popc(m & ((1u << lane) - 1u))] = p;
 }
 
-// the free particles' whole step: update_pos_mpcd of every substep (pos = mod(pos +
-// vel dt, len), cpp/update.cpp:56-60, the streaming passes' operations in order) and the
-// binning of the last substep with the next step's grid shift, beside the near particles'
-// substeps, which touch none of its particles.  A grid of a few blocks per SM walks the
-// fluid (it shares the SMs and their FP64 units with the substeps' latency-bound chain).
+// n substeps of update_pos_mpcd along one axis for a free particle: x = mod(x + w, L) n
+// times (cpp/update.cpp:56-60), with the result of the additions one by one.  x > 0 has
+// the unit u = ulp(x) of its binade [2^e, 2^(e+1)); w/u = Mw 2^-s (Mw the significand of w).
+// While an exact sum x + w lies inside that binade, the nearest double to it is x plus the
+// multiple of u nearest to w, k u with k = round(Mw 2^-s), the same k at every addition
+// unless w/u is exactly halfway between two integers (then ties-to-even would depend on x).
+// So if the n results x + j k u (j = 0..n) all stay at least u inside the binade (the exact
+// sums then lie inside it) and inside [2^-30 L, L), where mod is the identity, the n
+// additions give x + n k u, built here on the integer pipe from the bits (the FP64 units
+// stay free for the substeps' chains).  Otherwise, or on a tie, the additions one by one.
+static __device__ __forceinline__ double free_stream(double x, double w, int n, const Dim &D) {
+  const long long bx = dbits(x), bw = dbits(w);
+  const long long aw = bw & 0x7FFFFFFFFFFFFFFFll;
+  const int ex = (int)((bx >> 52) & 0x7FF), ew = (int)((aw >> 52) & 0x7FF);
+  bool fast = bx >= D.lo_bits && bx < D.L_bits && ex > 0 && (aw == 0 || ew > 0);
+  long long k = 0;
+  if (fast && aw != 0) {
+    const long long mw = (aw & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
+    const int sh = ex - ew;
+    if (sh <= 0) {
+      fast = sh > -8;  // w a multiple of u (a w that large leaves the binade anyway)
+      k = fast ? (mw << -sh) : 0;
+    } else if (sh <= 53) {
+      k = mw >> sh;
+      const long long rem = mw & ((1ll << sh) - 1), half = 1ll << (sh - 1);
+      fast = rem != half;  // a tie: the additions one by one
+      k += rem > half ? 1 : 0;
+    }  // sh > 53: |w| < u/2, every sum rounds back to x (k = 0)
+    if (bw < 0) k = -k;
+  }
+  // (n |k| >= 2^52 leaves the binade; the bound also keeps n k from overflowing)
+  fast = fast && n > 0 && (k < 0 ? -k : k) < 0x10000000000000ll / n;
+  if (fast) {
+    const long long mx = (bx & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
+    const long long mn = mx + (long long)n * k;
+    const long long lo = 0x10000000000000ll + 1, hi = 0x20000000000000ll - 1;
+    fast = mx >= lo && mx <= hi && mn >= lo && mn <= hi;
+    if (fast) {
+      const long long bn = ((long long)ex << 52) | (mn & 0xFFFFFFFFFFFFFll);
+      fast = bn >= D.lo_bits && bn < D.L_bits;
+      if (fast) return __longlong_as_double(bn);
+    }
+  }
+  for (int l = 0; l < n; ++l) x = ref_mod(__dadd_rn(x, w), D);
+  return x;
+}
+
+// the free particles' whole step: update_pos_mpcd of every substep (free_stream: the
+// streaming passes' operations in order, or their exact result) and the binning of the
+// last substep with the next step's grid shift, beside the near particles' substeps,
+// which touch none of its particles.  A grid of a few blocks per SM walks the fluid (it
+// shares the SMs with the substeps' latency-bound chain).
 __global__ void __launch_bounds__(256) k_free_flight(const SysF64 S, int fb) {
   const Fluid F = fluid_at(S, fb);
   for (int p0 = blockIdx.x * blockDim.x; p0 < S.N; p0 += gridDim.x * blockDim.x) {
     const int p = p0 + threadIdx.x;
     BinTerm t{-1, 0, 0, 0, 0};
     if (p < S.N && !S.fnear[p]) {
-      double x = F.x[p], y = F.y[p], z = F.z[p];
       const double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
-      for (int l = 0; l < S.n_sub; ++l) {
-        x = ref_mod(__dadd_rn(x, wx), S.dx);
-        y = ref_mod(__dadd_rn(y, wy), S.dy);
-        z = ref_mod(__dadd_rn(z, wz), S.dz);
-      }
+      const double x = free_stream(F.x[p], wx, S.n_sub, S.dx), y = free_stream(F.y[p], wy, S.n_sub, S.dy),
+                   z = free_stream(F.z[p], wz, S.n_sub, S.dz);
       t = bin_term(S, S.ss->rrn, p, x, y, z, wx, wy, wz);
       F.x[p] = x; F.y[p] = y; F.z[p] = z;
     }
