@@ -53,7 +53,7 @@ struct mpcd_ctx {
   bool own_stream = false;
   cudaStream_t aux = nullptr;    // second stream: colloid work beside the fluid passes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // free-flight schedule (steps without a counting sort): the near particles' substeps run
+  // free-flight schedule (mpcd_step): the near particles' substeps run
   // on nst (high priority) beside the free particles' pass on the context's stream
   cudaStream_t nst = nullptr;
   cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr, ev_list = nullptr;
@@ -370,6 +370,19 @@ static void enq_substeps_overlapped(mpcd_ctx *c) {
   cudaStreamWaitEvent(c->stream, c->ev_finp[n & 1], 0);
 }
 
+// A counting-sort step of the free-flight schedule: the rotation fused with the scatter into
+// the other buffer in cell order (the classification then only classifies).  The scatter
+// moves the particles and rewrites the slots run()'s rear-shell test reads, so it waits for
+// that test (ev_join, on the side stream).
+static void enq_sort_scatter(mpcd_ctx *c) {
+  const SysF64 &S = c->S;
+  const bool f32 = S.precision == MPCD_FP32C;
+  cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+  launch(c, "k_scan_blocks", k_scan_blocks, 1, 1024, S, c->nblk);
+  launch(c, "k_rotate_sort", f32 ? k_rotate_sort32 : k_rotate_sort, blocks_for(S.N, 256), 256, S, c->fbuf, 1 - c->fbuf);
+  c->fbuf = 1 - c->fbuf;
+}
+
 // One substep of the FP32 free-flight schedule on stream s: the pass over the near list,
 // the colloid side work beside it and the event pass, then the colloid finish.
 static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
@@ -394,7 +407,7 @@ static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
   enq_fin_on(c, s, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
 }
 
-// One step of the FP32 form in the free-flight schedule (steps without a counting sort).
+// One step of the FP32 form in the free-flight schedule.
 //   side stream: the flight table (from the colloids' positions at the start of the
 //                step), then run()'s rear-shell test;
 //   main:        the cell pass; the rotation with the classification (it needs the table);
@@ -402,7 +415,7 @@ static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
 //   near stream: (high priority) run()'s kick (it needs the shell test; the kicked particles
 //                are all near), the colloid kick and the n_sub substeps of the near list;
 //   main:        the end of the step, after both.
-static void enq_step_flight32(mpcd_ctx *c) {
+static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
   const int n = S.n_sub;
   cudaEventRecord(c->ev_fork, c->stream);
@@ -418,8 +431,9 @@ static void enq_step_flight32(mpcd_ctx *c) {
   if (S.Nc > 0) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
+  if (sort) enq_sort_scatter(c);
   cudaStreamWaitEvent(c->stream, c->ev_tab, 0);
-  launch(c, "k_rotate_classify", k_rotate_classify32, blocks_for(S.N, 256), 256, S, c->fbuf);
+  launch(c, "k_rotate_classify", classify_kernel32(!sort), blocks_for(S.N, 256), 256, S, c->fbuf);
   cudaEventRecord(c->ev_cls, c->stream);
   cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
   cudaStreamWaitEvent(c->nst, c->ev_join, 0);
@@ -432,12 +446,12 @@ static void enq_step_flight32(mpcd_ctx *c) {
   launch(c, "k_end_step", k_end_step, 1, 256, S);
 }
 
-// One step of the FP64 form in the free-flight schedule (steps without a counting sort):
+// One step of the FP64 form in the free-flight schedule:
 // as the FP32 form's, with the FP64 substeps overlapped as in enq_substeps_overlapped
 // (the near list's streaming passes on the near stream; the event pass fused with the
 // colloid side work, then the colloid finish, on the event stream) and the near
 // particles' binning after the last streaming pass.
-static void enq_step_flight64(mpcd_ctx *c) {
+static void enq_step_flight64(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
   const int n = S.n_sub;
   const bool nc = S.Nc > 0;
@@ -453,8 +467,9 @@ static void enq_step_flight64(mpcd_ctx *c) {
   if (nc) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep, prep_blocks(S), 256, S);
+  if (sort) enq_sort_scatter(c);
   cudaStreamWaitEvent(c->stream, c->ev_tab, 0);
-  launch(c, "k_rotate_classify", k_rotate_classify, blocks_for(S.N, 256), 256, S, c->fbuf);
+  launch(c, "k_rotate_classify", classify_kernel(!sort), blocks_for(S.N, 256), 256, S, c->fbuf);
   cudaEventRecord(c->ev_cls, c->stream);
   cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
   cudaStreamWaitEvent(c->nst, c->ev_join, 0);
@@ -488,9 +503,9 @@ static void enq_step_flight64(mpcd_ctx *c) {
 // one MPCD step: rotation_mpcd, run, n_sub substeps (cpp/active_brownian.cpp:25-38)
 static void enq_step(mpcd_ctx *c, bool sort) {
   const int n = c->S.n_sub;
-  if (c->flight && !sort) {
-    if (c->S.precision == MPCD_FP32C) enq_step_flight32(c);
-    else enq_step_flight64(c);
+  if (c->flight) {
+    if (c->S.precision == MPCD_FP32C) enq_step_flight32(c, sort);
+    else enq_step_flight64(c, sort);
     return;
   }
   enq_rotation_run(c, sort);
@@ -528,7 +543,9 @@ static const char *err_text(int bits) {
   if (bits & ERRB_SHELL) return "run() candidate records overflowed";
   if (bits & ERRB_VRANGE) return "a fluid velocity exceeded vmax (range of the exact cell sums)";
   if (bits & ERRB_OCCUPANCY) return "a cell holds more than max_per_cell particles";
-  if (bits & ERRB_DISPLACE) return "a wall collision displaced a particle beyond the cell-table margin";
+  if (bits & ERRB_DISPLACE)
+    return "a wall collision displaced a particle, or a colloid moved in a substep, beyond the margin of the cell "
+           "tables and the free-flight classification";
   if (bits & ERRB_SHELLSLOTS) return "a particle lies in more rear shells than a record holds";
   if (bits & ERRB_DELTA) return "a colloid momentum exchange left the range of the exact sums";
   if (bits & ERRB_EVENTS) return "the wall-collision event lists overflowed";

@@ -42,10 +42,12 @@ __global__ void k_rotate_sort32(__grid_constant__ const SysF64 S, int src, int d
 // the FP32 free-flight schedule: flight table, rotation with the classification, the free
 // particles' whole step, per-substep passes over the near list
 __global__ void k_flight_table32(__grid_constant__ const SysF64 S);
-__global__ void k_rotate_classify32(__grid_constant__ const SysF64 S, int fb);
+// the rotation with the classification (rotate false: after a counting-sort scatter)
+using ClassifyKernel = void (*)(const SysF64, int);
+ClassifyKernel classify_kernel32(bool rotate);
 __global__ void k_free_flight32(__grid_constant__ const SysF64 S, int fb);
 StreamKernel stream_kernel32_near(int flags);
-__global__ void k_rotate_classify(const SysF64 S, int fb);
+ClassifyKernel classify_kernel(bool rotate);
 __global__ void k_free_flight(const SysF64 S, int fb);
 __global__ void k_bin_near(const SysF64 S, int fb);
 StreamKernel stream_kernel_near(int flags);

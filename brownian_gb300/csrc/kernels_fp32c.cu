@@ -489,9 +489,10 @@ __global__ void __launch_bounds__(128) k_flight_table32(__grid_constant__ const 
   }
 }
 
-// rotation_mpcd of one particle (the SRD map of its cell) and its classification: a near
-// particle is flagged and appended to the near list (one atomic per block).
-// Non-sorting steps (the particles keep their slots).
+// rotation_mpcd of one particle (the SRD map of its cell; ROT false: a counting-sort step,
+// whose scatter rotated it) and its classification: a near particle is flagged and appended to
+// the near list (one atomic per block).
+template <bool ROT>
 __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ const SysF64 S, int fb) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < S.N;
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ con
   const int b0 = (int)((step * S.n_sub - 1) & 1);
   bool near = false;
   if (valid) {
-    const int c = S.rotcell[p];
+    const int c = ROT ? S.rotcell[p] : S.C;
     float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
     int cx, cy, cz;
     float ox, oy, oz;
@@ -508,8 +509,10 @@ __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ con
     const bool inb = cx < S.Lx && cy < S.Ly && cz < S.Lz;  // (a record within the box)
     const FlightCell *fc = S.ftab + (inb ? cx + S.Lx * (cy + S.Ly * cz) : 0);
     const uint4 w0 = reinterpret_cast<const uint4 *>(fc)[0], w1 = reinterpret_cast<const uint4 *>(fc)[1];
-    if (c < S.C) apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
-    F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+    if (ROT) {
+      if (c < S.C) apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
+      F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+    }
     const float travel = (float)S.n_sub * S.dtf * sqrtf(vx * vx + vy * vy + vz * vz);
     const int cnt = tcount(((unsigned long long)w0.y << 32) | w0.x, step);
     if (!inb || !(travel <= S.flight_rv) || cnt > FLIGHT_CAP) {
@@ -568,6 +571,10 @@ __global__ void __launch_bounds__(256) k_stream32_near(__grid_constant__ const S
   constexpr int per = 256 * stream32_u(FLAGS);
   for (int chunk = blockIdx.x; chunk * per < count; chunk += gridDim.x)
     stream32_chunk<FLAGS, true>(S, chunk, count, l, fb);
+}
+
+ClassifyKernel classify_kernel32(bool rotate) {
+  return rotate ? k_rotate_classify32<true> : k_rotate_classify32<false>;
 }
 
 StreamKernel stream_kernel32_near(int flags) {

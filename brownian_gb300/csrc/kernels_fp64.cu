@@ -401,9 +401,10 @@ __global__ void __launch_bounds__(256) k_bin_near(const SysF64 S, int fb) {
   }
 }
 
-// rotation_mpcd of one particle (w' = A w + b of its cell, as k_rotate) and its
-// classification against the flight table: a near particle is flagged and listed (one
-// atomic per block).  Non-sorting steps.
+// rotation_mpcd of one particle (w' = A w + b of its cell, as k_rotate; ROT false: a
+// counting-sort step, whose scatter rotated it) and its classification against the flight
+// table: a near particle is flagged and listed (one atomic per block).
+template <bool ROT>
 __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < S.N;
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb)
   bool near = false;
   if (valid) {
     S.pend[p] = 0;  // no particle is pending at the start of a step
-    const int c = S.rotcell[p];
+    const int c = ROT ? S.rotcell[p] : S.C;
     double wx = F.wx[p], wy = F.wy[p], wz = F.wz[p];
     const float px = d2f_trunc(F.x[p]), py = d2f_trunc(F.y[p]), pz = d2f_trunc(F.z[p]);
     int cx = (int)px, cy = (int)py, cz = (int)pz;  // positions in (0, L]: L is cell 0
@@ -431,8 +432,10 @@ __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb)
       wx = nx; wy = ny; wz = nz;
       F.wx[p] = wx; F.wy[p] = wy; F.wz[p] = wz;
     }
-    const float fx = (float)wx, fy = (float)wy, fz = (float)wz;
-    const float travel = (float)S.n_sub * sqrtf(fx * fx + fy * fy + fz * fz);  // n_sub |w| = ndt |v|
+    // n_sub |w| = ndt |v| (FP32 copies by truncation, on the integer pipe: below 2^-23 of
+    // the travel under it, which the slack covers)
+    const float fx = d2f_trunc(wx), fy = d2f_trunc(wy), fz = d2f_trunc(wz);
+    const float travel = (float)S.n_sub * sqrtf(fx * fx + fy * fy + fz * fz);
     const int cnt = tcount(((unsigned long long)w0.y << 32) | w0.x, step);
     if (!inb || !(travel <= S.flight_rv) || cnt > FLIGHT_CAP) {
       near = true;  // faster than the table allows (or not finite), or a crowded cell
@@ -530,6 +533,8 @@ EventAuxKernel event_aux_kernel(int flags) {
   }
   return nullptr;
 }
+
+ClassifyKernel classify_kernel(bool rotate) { return rotate ? k_rotate_classify<true> : k_rotate_classify<false>; }
 
 StreamKernel stream_kernel_near(int flags) {
   switch (flags) {

@@ -171,8 +171,7 @@ int mpcd_step(mpcd_ctx *c, int nsteps);
  * enqueued before them (they synchronise). */
 int mpcd_step_async(mpcd_ctx *c, int nsteps);
 int mpcd_sync(mpcd_ctx *c);
-/* The free-flight schedule (on by default, both forms), used by mpcd_step on the steps
- * without a counting sort: a fluid particle that no colloid can reach during the step (farther
+/* The free-flight schedule (on by default, both forms), used by mpcd_step: a fluid particle that no colloid can reach during the step (farther
  * from every colloid at its start than the run() shell radius sigma/2 + 1/2 plus its own travel
  * in the step plus n_sub times the colloids' bound on a substep's move) is streamed through all
  * substeps and binned by one pass, with the operations the substep passes would apply to it,
