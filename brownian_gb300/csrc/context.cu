@@ -80,6 +80,7 @@ struct mpcd_ctx {
   int part_blocks = 256;
   double *staging = nullptr;     // AoS transfer buffer, allocated on first use
   double *staging2 = nullptr;    // second one (FP32 form: velocities)
+  double *diag_host = nullptr;   // page-locked: what mpcd_diag reads, allocated on first use
   int phase = 0;                 // 0: between steps; 1: rotation_mpcd of the next step done
   int next_sub = 1;              // routine-level: the substep mpcd_substep expects
   int nblk = 0;                  // 256-cell blocks of the counting sort
@@ -824,6 +825,7 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   if (c->staging) cudaFree(c->staging);
   if (c->staging2) cudaFree(c->staging2);
   if (c->ss_host) cudaFreeHost(c->ss_host);
+  if (c->diag_host) cudaFreeHost(c->diag_host);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   if (c->evs) cudaStreamDestroy(c->evs);
@@ -1203,11 +1205,34 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   if (!out) return MPCD_ERR_PARAM;
   if ((r = need_setup(c))) return r;
   const SysF64 &S = c->S;
+  const size_t np = (size_t)c->part_blocks * 5, nc = (size_t)S.Nc;
+  if (!c->diag_host && cudaMallocHost(&c->diag_host, sizeof(double) * (np + 7 * nc + 1)) != cudaSuccess) {
+    c->diag_host = nullptr;
+    return fail(c, MPCD_ERR_NOMEM, "page-locked diagnostics buffer");
+  }
   launch(c, "k_diag_fluid", k_diag_fluid, c->part_blocks, 256, S, c->part);
   if (S.Nc) launch(c, "k_colloid_pot", k_colloid_pot, colloid_grid(c), 128, S, cur_buf(c));
-  if ((r = check_device(c))) return r;
-  std::vector<double> part((size_t)c->part_blocks * 5);
-  CUDA_OK(c, scopy(c, part.data(), c->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
+  // everything the diagnostics read in one round trip: the step state (error bits, event
+  // count), the fluid partial sums and the colloid arrays into page-locked memory, then the
+  // event count reset, then one synchronisation
+  double *h = c->diag_host;
+  CUDA_OK(c, cudaMemcpyAsync(c->ss_host, S.ss, sizeof(StepState), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OK(c, cudaMemcpyAsync(h, c->part, sizeof(double) * np, cudaMemcpyDeviceToHost, c->stream));
+  if (nc) {
+    CUDA_OK(c, cudaMemcpyAsync(h + np, S.V, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(c, cudaMemcpyAsync(h + np + 3 * nc, S.W, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OK(c, cudaMemcpyAsync(h + np + 6 * nc, S.pot_part, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_OK(c, cudaMemsetAsync(&S.ss->ev_total, 0, sizeof(long long), c->stream));
+  CUDA_OK(c, cudaStreamSynchronize(c->stream));
+  CUDA_OK(c, cudaGetLastError());
+  if (c->profile) collect_profile(c);
+  if (int bits = c->ss_host->err) {
+    char buf[200];
+    snprintf(buf, sizeof buf, "device error bits 0x%x: %s", bits, err_text(bits));
+    return fail(c, (bits & (ERRB_VRANGE | ERRB_DELTA)) ? MPCD_ERR_RANGE : MPCD_ERR_CAPACITY, buf);
+  }
+  const double *part = h;
   double sw[3] = {0, 0, 0}, s2 = 0, n = 0;
   for (int b = 0; b < c->part_blocks; ++b) {
     for (int k = 0; k < 3; ++k) sw[k] += part[5 * b + k];
@@ -1223,15 +1248,10 @@ extern "C" int mpcd_diag(mpcd_ctx *c, mpcd_diag_t *out) {
   out->temperature_fluid = n > 0 ? 2.0 * out->ke_fluid / (3.0 * n) / c->p.kbt : 0;
   // wall-collision candidates handled exactly, summed since the last call
   out->events = c->ss_host->ev_total;
-  const long long zero64 = 0;
-  CUDA_OK(c, scopy(c, &c->S.ss->ev_total, &zero64, sizeof zero64, cudaMemcpyHostToDevice));
   out->shell_records = c->ss_host->nshell;
   double mom[3] = {out->momentum_fluid[0], out->momentum_fluid[1], out->momentum_fluid[2]};
   if (S.Nc) {
-    std::vector<double> V(3 * S.Nc), W(3 * S.Nc), pot(S.Nc);
-    CUDA_OK(c, scopy(c, V.data(), S.V, sizeof(double) * V.size(), cudaMemcpyDeviceToHost));
-    CUDA_OK(c, scopy(c, W.data(), S.W, sizeof(double) * W.size(), cudaMemcpyDeviceToHost));
-    CUDA_OK(c, scopy(c, pot.data(), S.pot_part, sizeof(double) * pot.size(), cudaMemcpyDeviceToHost));
+    const double *V = h + np, *W = h + np + 3 * nc, *pot = h + np + 6 * nc;
     double ke = 0, ake = 0, pe = 0;
     for (int j = 0; j < S.Nc; ++j) {
       ke += V[3 * j] * V[3 * j] + V[3 * j + 1] * V[3 * j + 1] + V[3 * j + 2] * V[3 * j + 2];
