@@ -415,14 +415,20 @@ def run_ensemble(nrep, steps, rank):
         s.initialize(bg.INIT_PHYSICAL)
         s.setup()
     tuned = autotune(ens, steps=2)
-    ens.step(2)
-    t0 = time.perf_counter()
-    ens.step(steps)
-    batched_s = time.perf_counter() - t0
-    launches_per_step = None
+
+    def batched(flight):
+        ens.set_flight(flight)
+        ens.step(2)
+        t0 = time.perf_counter()
+        ens.step(steps)
+        return time.perf_counter() - t0
+
+    # the batched step in the free-flight schedule (the default), then in the per-substep one
+    batched_s = batched(True)
     l0 = ens.launch_count
     ens.step(1)
     launches_per_step = ens.launch_count - l0 - 1  # minus the error read-back
+    batched_sub_s = batched(False)
     # the same replicas, each stepped by its own single-system call, one after the other:
     # each replica's step graph enqueued back to back on one stream, one synchronisation
     # per sweep over the replicas (a replica's next step needs its previous one only)
@@ -451,15 +457,22 @@ def run_ensemble(nrep, steps, rank):
     return {"workload": "256 replicas" if nrep == 256 else f"{nrep} replicas",
             "replicas": nrep, "fluid_particles": n_particles, "steps": steps,
             "value": nrep * steps / batched_s, "unit": "replica-steps/s",
+            "schedule": "free flight (mpcd_ensemble_set_flight(1), the default)",
             "particle_steps_per_s": n_particles * steps / batched_s,
+            "per_substep": {"value": nrep * steps / batched_sub_s, "unit": "replica-steps/s",
+                            "how": "the batched step with one pass over every particle per substep "
+                                   "(mpcd_ensemble_set_flight(0))"},
+            # against the faster of the two looped arms
+            "speedup_vs_looped": min(looped_s, looped_flight_s) / batched_s,
             "looped": {"value": nrep * steps / looped_s, "unit": "replica-steps/s",
                        "how": "mpcd_step_async(1) of each replica in turn on one stream, one "
-                              "synchronisation per sweep over the replicas; the per-substep schedule of "
-                              "the batched kernels (mpcd_set_flight(0))"},
-            "speedup_vs_looped": looped_s / batched_s,
+                              "synchronisation per sweep over the replicas; the single-system per-substep "
+                              "schedule (mpcd_set_flight(0))"},
+            "speedup_vs_looped_per_substep": looped_s / batched_s,
             "looped_free_flight": {"value": nrep * steps / looped_flight_s, "unit": "replica-steps/s",
                                    "how": "the same loop with the single-system free-flight schedule"},
             "speedup_vs_looped_free_flight": looped_flight_s / batched_s,
+            "speedup_per_substep_schedules": looped_s / batched_sub_s,
             "launches_per_step": launches_per_step,
             "autotune": {"choice": tuned["choice"], "ms_per_step": tuned["ms_per_step"],
                          "trials": len(tuned["log"])},

@@ -30,6 +30,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
+           "mpcd_ensemble_set_flight", "mpcd_ensemble_get_flight",
            "mpcd_exchange_read", "mpcd_mlp_create", "mpcd_mlp_destroy", "mpcd_mlp_last_error", "mpcd_mlp_param_count",
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
            "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
@@ -42,7 +43,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
 SUBSTEP_ROUTINES = ("update_pos_md", "neighbour_list_md", "update_pos_mpcd", "neighbour_list_mpcd",
                     "fluid_colloid_collision", "update_activity_direction", "compute_force_md",
                     "update_velocity_colloid")
-ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX = 0, 1, 2, 3
+ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX, ENS_FREE = 0, 1, 2, 3, 4
 NOALLOC_MAX_PARTICLES = 33554432
 PHYSICS_REFERENCE, PHYSICS_FIXED = 0, 1
 LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
@@ -145,6 +146,8 @@ def lib():
         L.mpcd_ensemble_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.mpcd_ensemble_launch_count.argtypes = [vp]
         L.mpcd_ensemble_launch_count.restype = C.c_int64
+        L.mpcd_ensemble_set_flight.argtypes = [vp, C.c_int]
+        L.mpcd_ensemble_get_flight.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -538,6 +541,15 @@ class Ensemble:
 
     def set_launch(self, which, per_system=1, block=32):
         self._ck(lib().mpcd_ensemble_set_launch(self.h, which, per_system, block))
+
+    def set_flight(self, on=True):
+        """The batched step's schedule: free flight (default) or one pass per substep
+        over every particle; both leave the same bits."""
+        self._ck(lib().mpcd_ensemble_set_flight(self.h, 1 if on else 0))
+
+    @property
+    def flight(self):
+        return bool(lib().mpcd_ensemble_get_flight(self.h))
 
     @property
     def launch_count(self):

@@ -47,6 +47,12 @@ using ClassifyKernel = void (*)(const SysF64, int);
 ClassifyKernel classify_kernel32(bool rotate);
 __global__ void k_free_flight32(__grid_constant__ const SysF64 S, int fb);
 StreamKernel stream_kernel32_near(int flags);
+// the same over a batch of systems (persistent, batch_for)
+__global__ void k_flight_table32_b(const SysF64 *Ss, const int *boff, int nrep);
+using ClassifyKernelB = void (*)(const SysF64 *, const int *, int, int);
+ClassifyKernelB classify_kernel32_b(bool rotate);
+__global__ void k_free_flight32_b(const SysF64 *Ss, const int *boff, int nrep, int fb);
+StreamKernelB stream_kernel32_near_b(int flags);
 ClassifyKernel classify_kernel(bool rotate);
 __global__ void k_free_flight(const SysF64 S, int fb);
 __global__ void k_bin_near(const SysF64 S, int fb);

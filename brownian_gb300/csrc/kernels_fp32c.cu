@@ -459,13 +459,12 @@ static __device__ __forceinline__ float flight_reach(const SysF64 &S) {
 // within the flight reach of it, the own box included.  A cell
 // with more than FLIGHT_CAP colloids keeps counting; its particles are all near.  Block 0
 // also empties the near list and draws the next step's grid shift for the free pass.
-__global__ void __launch_bounds__(128) k_flight_table32(__grid_constant__ const SysF64 S) {
+static __device__ __forceinline__ void k_flight_table32_body(const SysF64 &S, const int j) {
   const long long step = S.ss->step;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (j == 0 && threadIdx.x == 0) {
     S.ss->nnear = 0;
     shift_of(S, step + 2, S.ss->rrn);
   }
-  const int j = blockIdx.x;
   if (j >= S.Nc) return;
   const int b0 = (int)((step * S.n_sub - 1) & 1);
   const float reach = flight_reach(S);
@@ -489,12 +488,22 @@ __global__ void __launch_bounds__(128) k_flight_table32(__grid_constant__ const 
   }
 }
 
+__global__ void __launch_bounds__(128) k_flight_table32(__grid_constant__ const SysF64 S) {
+  k_flight_table32_body(S, blockIdx.x);
+}
+
+// the same over a batch of systems (persistent: batch_for; max(Nc, 1) virtual blocks each)
+__global__ void __launch_bounds__(128) k_flight_table32_b(const SysF64 *Ss, const int *boff, int nrep) {
+  __shared__ SysF64 sS;
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_flight_table32_body(sS, VB); });
+}
+
 // rotation_mpcd of one particle (the SRD map of its cell; ROT false: a counting-sort step,
 // whose scatter rotated it) and its classification: a near particle is flagged and appended to
 // the near list (one atomic per block).
 template <bool ROT>
-__global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ const SysF64 S, int fb) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+static __device__ __forceinline__ void k_rotate_classify32_body(const SysF64 &S, const int VB, int fb) {
+  const int p = VB * blockDim.x + threadIdx.x;
   const bool valid = p < S.N;
   const Fluid32 F = fluid32_at(S, fb);
   const long long step = S.ss->step;
@@ -537,15 +546,27 @@ __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ con
   if (near) S.near[base + __popc(m & ((1u << lane) - 1u))] = p;
 }
 
+template <bool ROT>
+__global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ const SysF64 S, int fb) {
+  k_rotate_classify32_body<ROT>(S, blockIdx.x, fb);
+}
+
+// the same over a batch of systems (persistent: batch_for)
+template <bool ROT>
+__global__ void __launch_bounds__(256) k_rotate_classify32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
+  __shared__ SysF64 sS;
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_rotate_classify32_body<ROT>(sS, VB, fb); });
+}
+
 // the free particles' whole step: n_sub streaming substeps (update_pos_mpcd, the
 // streaming passes' operations in order) and the binning of the last substep with the
 // next step's grid shift.  Runs beside the near particles' substeps, which touch none of
 // its particles; a grid of a few blocks per SM walks the fluid (it shares the SMs with the
 // substeps' latency-bound chain).
-__global__ void __launch_bounds__(256) k_free_flight32(__grid_constant__ const SysF64 S, int fb) {
+static __device__ __forceinline__ void k_free_flight32_body(const SysF64 &S, const int VB, const int NVB, int fb) {
   const Fluid32 F = fluid32_at(S, fb);
   const float rr[3] = {(float)S.ss->rrn[0], (float)S.ss->rrn[1], (float)S.ss->rrn[2]};
-  for (int p0 = blockIdx.x * blockDim.x; p0 < S.N; p0 += gridDim.x * blockDim.x) {
+  for (int p0 = VB * blockDim.x; p0 < S.N; p0 += NVB * blockDim.x) {
     const int p = p0 + threadIdx.x;
     BinTerm32 bt{-1, 0, 0, 0, 0};
     if (p < S.N && !S.fnear[p]) {
@@ -564,17 +585,52 @@ __global__ void __launch_bounds__(256) k_free_flight32(__grid_constant__ const S
   }
 }
 
-// the per-substep pass over the near list (grid-stride over chunks of 256 U)
+__global__ void __launch_bounds__(256) k_free_flight32(__grid_constant__ const SysF64 S, int fb) {
+  k_free_flight32_body(S, blockIdx.x, gridDim.x, fb);
+}
+
+// the same over a batch of systems (persistent: batch_for; each virtual block walks its
+// system's fluid with the system's virtual blocks as stride)
+__global__ void __launch_bounds__(256) k_free_flight32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
+  __shared__ SysF64 sS;
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_free_flight32_body(sS, VB, NVB, fb); });
+}
+
+// the per-substep pass over the near list (stride over chunks of 256 U)
 template <int FLAGS>
-__global__ void __launch_bounds__(256) k_stream32_near(__grid_constant__ const SysF64 S, int l, int fb) {
+static __device__ __forceinline__ void k_stream32_near_body(const SysF64 &S, const int VB, const int NVB, int l,
+                                                            int fb) {
   const int count = S.ss->nnear;
   constexpr int per = 256 * stream32_u(FLAGS);
-  for (int chunk = blockIdx.x; chunk * per < count; chunk += gridDim.x)
-    stream32_chunk<FLAGS, true>(S, chunk, count, l, fb);
+  for (int chunk = VB; chunk * per < count; chunk += NVB) stream32_chunk<FLAGS, true>(S, chunk, count, l, fb);
+}
+
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32_near(__grid_constant__ const SysF64 S, int l, int fb) {
+  k_stream32_near_body<FLAGS>(S, blockIdx.x, gridDim.x, l, fb);
+}
+
+// the same over a batch of systems (persistent: batch_for)
+template <int FLAGS>
+__global__ void __launch_bounds__(256) k_stream32_near_b(const SysF64 *Ss, const int *boff, int nrep, int l, int fb) {
+  __shared__ SysF64 sS;
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int NVB) { k_stream32_near_body<FLAGS>(sS, VB, NVB, l, fb); });
 }
 
 ClassifyKernel classify_kernel32(bool rotate) {
   return rotate ? k_rotate_classify32<true> : k_rotate_classify32<false>;
+}
+
+ClassifyKernelB classify_kernel32_b(bool rotate) {
+  return rotate ? k_rotate_classify32_b<true> : k_rotate_classify32_b<false>;
+}
+
+StreamKernelB stream_kernel32_near_b(int flags) {
+  switch (flags) {
+    case F_STREAM | F_COLLIDE: return k_stream32_near_b<F_STREAM | F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream32_near_b<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
+  }
+  return nullptr;
 }
 
 StreamKernel stream_kernel32_near(int flags) {

@@ -2,7 +2,7 @@
 
 Coordinate descent over the knobs of mpcd_ensemble_set_launch (event blocks per
 system, run() blocks per system, colloid-finish block size, threads per colloid
-of the colloid side work): each candidate is timed over a few whole ensemble
+of the colloid side work, resident blocks per SM of the free-flight pass): each candidate is timed over a few whole ensemble
 steps (the step call synchronises, so wall time is device time plus one host
 round trip), the fastest is kept, and every timing is logged.  The results do
 not depend on the shapes (every sum is exact), so tuning can run on the warm-up
@@ -10,16 +10,17 @@ steps of a production run.
 """
 import time
 
-from . import ENS_AUX, ENS_EVENTS, ENS_FIN, ENS_RUN
+from . import ENS_AUX, ENS_EVENTS, ENS_FIN, ENS_FREE, ENS_RUN
 
 CANDIDATES = {
     "events_blocks_per_system": (ENS_EVENTS, [(1, 32), (2, 32), (4, 32), (8, 32)]),
     "run_blocks_per_system": (ENS_RUN, [(1, 32), (2, 32), (4, 32), (8, 32)]),
     "fin_threads_per_block": (ENS_FIN, [(1, 32), (1, 64), (1, 128)]),
     "aux_threads_per_colloid": (ENS_AUX, [(1, 64), (1, 128), (1, 256)]),
+    "free_blocks_per_sm": (ENS_FREE, [(2, 256), (4, 256), (8, 256)]),
 }
 DEFAULTS = {"events_blocks_per_system": (2, 32), "run_blocks_per_system": (4, 32), "fin_threads_per_block": (1, 128),
-            "aux_threads_per_colloid": (1, 128)}
+            "aux_threads_per_colloid": (1, 128), "free_blocks_per_sm": (4, 256)}
 
 
 def _time(ens, steps):

@@ -268,11 +268,18 @@ int mpcd_ensemble_step(mpcd_ensemble *e, int nsteps);
 enum { MPCD_ENS_EVENTS = 0,  /* blocks per system of the event pass (1..64) */
        MPCD_ENS_RUN = 1,     /* blocks per system of run() (1..64) */
        MPCD_ENS_FIN = 2,     /* threads per block of the colloid finish (32, 64, 128) */
-       MPCD_ENS_AUX = 3 };   /* threads per colloid of the colloid side work (64, 128, 256) */
+       MPCD_ENS_AUX = 3,     /* threads per colloid of the colloid side work (64, 128, 256) */
+       MPCD_ENS_FREE = 4 };  /* resident blocks per SM of the free-flight pass (1..8; block ignored) */
 /* launch shapes of the batched step (the autotuner's knobs); results do not depend on them */
 int mpcd_ensemble_set_launch(mpcd_ensemble *e, int which, int per_system, int block);
 /* kernels the ensemble launched since creation */
 int64_t mpcd_ensemble_launch_count(const mpcd_ensemble *e);
+/* the schedule of the batched step: the free-flight schedule (on = 1, the default: particles
+ * no colloid can reach in a step streamed through all substeps by one batched pass beside the
+ * other particles' substeps) or one pass over every particle per substep (on = 0).  Both
+ * leave the same bits. */
+int mpcd_ensemble_set_flight(mpcd_ensemble *e, int on);
+int mpcd_ensemble_get_flight(const mpcd_ensemble *e);
 
 /* ---- learned closure network (no counterpart in the reference) ----------------------- */
 /* MLP 81 -> 256 -> 256 -> 256 -> 12 with SiLU, BF16 weights on the tensor cores with FP32
