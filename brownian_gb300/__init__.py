@@ -27,7 +27,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_neighbour_list_mpcd", "mpcd_fluid_colloid_collision", "mpcd_update_activity_direction",
            "mpcd_compute_force_md", "mpcd_update_velocity_colloid", "mpcd_get_neighbour_md", "mpcd_get_box_binning",
            "mpcd_step", "mpcd_step_async", "mpcd_sync", "mpcd_set_flight", "mpcd_get_flight", "mpcd_diag", "mpcd_get_rotation_binning", "mpcd_get_shell_count",
-           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_launch_count", "mpcd_set_launch",
+           "mpcd_profile_enable", "mpcd_profile_read", "mpcd_trace_step", "mpcd_launch_count", "mpcd_set_launch",
            "mpcd_fluid_sums_noalloc", "mpcd_ensemble_create", "mpcd_ensemble_destroy", "mpcd_ensemble_last_error",
            "mpcd_ensemble_system", "mpcd_ensemble_step", "mpcd_ensemble_set_launch", "mpcd_ensemble_launch_count",
            "mpcd_ensemble_set_flight", "mpcd_ensemble_get_flight",
@@ -46,7 +46,7 @@ SUBSTEP_ROUTINES = ("update_pos_md", "neighbour_list_md", "update_pos_mpcd", "ne
 ENS_EVENTS, ENS_RUN, ENS_FIN, ENS_AUX, ENS_FREE = 0, 1, 2, 3, 4
 NOALLOC_MAX_PARTICLES = 33554432
 PHYSICS_REFERENCE, PHYSICS_FIXED = 0, 1
-LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX = 0, 1, 2
+LAUNCH_EVENTS, LAUNCH_FIN, LAUNCH_AUX, LAUNCH_FREE = 0, 1, 2, 3
 
 
 class MPCDError(RuntimeError):
@@ -119,6 +119,7 @@ def lib():
         L.mpcd_get_shell_count.argtypes = [vp, ip]
         L.mpcd_profile_enable.argtypes = [vp, C.c_int]
         L.mpcd_profile_read.argtypes = [vp, C.c_void_p, C.POINTER(C.c_int64), dp, C.c_int]
+        L.mpcd_trace_step.argtypes = [vp, C.c_void_p, dp, dp, C.c_int]
         L.mpcd_launch_count.argtypes = [vp]
         L.mpcd_launch_count.restype = C.c_int64
         L.mpcd_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
@@ -499,6 +500,17 @@ class Simulation:
         ms = (C.c_double * cap)()
         n = lib().mpcd_profile_read(self.h, names, launches, ms, cap)
         return {bytes(names[i]).split(b"\0", 1)[0].decode(): (launches[i], ms[i]) for i in range(min(n, cap))}
+
+    def trace_step(self, cap=1024):
+        """One step (the state advances) traced: [(kernel, start_ms, end_ms)] in launch
+        order, times from the step's start on the graph's own timeline."""
+        names = (C.c_char * 48 * cap)()
+        t0 = (C.c_double * cap)()
+        t1 = (C.c_double * cap)()
+        n = lib().mpcd_trace_step(self.h, names, t0, t1, cap)
+        if n < 0:
+            self._ck(n)
+        return [(bytes(names[i]).split(b"\0", 1)[0].decode(), t0[i], t1[i]) for i in range(min(n, cap))]
 
     def set_launch(self, which, grid=0, block=32):
         """Launch shape of the event (LAUNCH_EVENTS) or colloid-finish (LAUNCH_FIN)

@@ -72,6 +72,8 @@ struct mpcd_ctx {
   bool profile = false;
   std::vector<ProfEvent> pending;
   std::vector<cudaEvent_t> event_pool;
+  bool tracing = false;          // capturing a traced step (mpcd_trace_step)
+  std::vector<ProfEvent> trace;  // its launches, each between two timing events
   std::map<std::string, std::pair<int64_t, double>> prof;
   StepState *ss_host = nullptr;  // pinned
   double *insw_n = nullptr, *sqcs_n = nullptr;
@@ -93,6 +95,7 @@ struct mpcd_ctx {
   ExchAcc *ud_acc = nullptr;
   long long ud_epoch = -1;
   int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
+  int free_grid = 0;                 // free-flight pass blocks of 256 (0: the form's default)
   // routine-by-routine substep: the next routine of the substep body (0: update_pos_md)
   int rseq = 0;
   // neighbour_list_mpcd observables (allocated on first use): box of each particle,
@@ -147,16 +150,17 @@ template <typename... KArgs, typename... Args>
 static void launch_on(mpcd_ctx *c, cudaStream_t s, const char *name, void (*k)(KArgs...), dim3 g, dim3 b,
                       Args... args) {
   ProfEvent pe{name, nullptr, nullptr};
-  if (c->profile) {
+  if (c->profile || c->tracing) {
     pe.a = pool_event(c);
     pe.b = pool_event(c);
-    cudaEventRecord(pe.a, s);
+    // (in a traced capture the records become nodes of the graph)
+    cudaEventRecordWithFlags(pe.a, s, c->tracing ? cudaEventRecordExternal : cudaEventRecordDefault);
   }
   k<<<g, b, 0, s>>>(args...);
   c->launches++;
-  if (c->profile) {
-    cudaEventRecord(pe.b, s);
-    c->pending.push_back(pe);
+  if (c->profile || c->tracing) {
+    cudaEventRecordWithFlags(pe.b, s, c->tracing ? cudaEventRecordExternal : cudaEventRecordDefault);
+    (c->tracing ? c->trace : c->pending).push_back(pe);
   }
 }
 
@@ -265,6 +269,13 @@ static void enq_fin_on(mpcd_ctx *c, cudaStream_t s, int mode, int l) {
 static void enq_fin(mpcd_ctx *c, int mode, int l) { enq_fin_on(c, c->stream, mode, l); }
 
 static unsigned prep_blocks(const SysF64 &S) { return blocks_for(S.Cpad > S.Nc ? S.Cpad : S.Nc, 256); }
+
+// the free-flight pass: a persistent grid beside the substeps' chain, whose kernels need room
+// on the SMs next to it
+static unsigned free_blocks(const mpcd_ctx *c) {
+  if (c->free_grid > 0) return (unsigned)c->free_grid;
+  return (unsigned)(c->n_sm * 2);
+}
 
 static bool sorts_at(const mpcd_ctx *c, long long step) { return c->sort_every > 0 && step % c->sort_every == 0; }
 
@@ -384,52 +395,35 @@ static void enq_sort_scatter(mpcd_ctx *c) {
   c->fbuf = 1 - c->fbuf;
 }
 
-// One substep of the FP32 free-flight schedule on stream s: the pass over the near list,
-// the colloid side work beside it and the event pass, then the colloid finish.
-static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
-  const SysF64 &S = c->S;
-  const int n = S.n_sub;
-  const int flags = l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE);
-  const bool fork = S.Nc > 0;
-  if (fork) {
-    cudaEventRecord(c->ev_fork, s);
-    cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
-    if (l == 1 && S.vlist) cudaStreamWaitEvent(c->aux, c->ev_list, 0);
-  }
-  launch_on(c, s, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8, 256, S,
-            l, c->fbuf);
-  if (fork) {
-    launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0, S.vlist);
-    cudaEventRecord(c->ev_join, c->aux);
-  }
-  launch_on(c, s, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
-            c->fbuf);
-  if (fork) cudaStreamWaitEvent(s, c->ev_join, 0);
-  enq_fin_on(c, s, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
-}
-
 // One step of the FP32 form in the free-flight schedule.
 //   side stream: the flight table (from the colloids' positions at the start of the
-//                step), then run()'s rear-shell test;
+//                step), then run()'s rear-shell test; per substep the colloid side work;
 //   main:        the cell pass; the rotation with the classification (it needs the table);
 //                then the free particles' whole step, beside
 //   near stream: (high priority) run()'s kick (it needs the shell test; the kicked particles
-//                are all near), the colloid kick and the n_sub substeps of the near list;
+//                are all near), the colloid kick and the n_sub passes over the near list,
+//                each overlapped with
+//   event stream: the event pass and the colloid finish of the substep before (the near
+//                pass of substep l needs the finish of l-2 only: the colloid positions of
+//                l-1, with the displacement bound as margin, and the cell table of l;
+//                particles it cannot decide go to the event pass and stay there, pending,
+//                to the end of the step);
 //   main:        the end of the step, after both.
 static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
   const int n = S.n_sub;
+  const bool nc = S.Nc > 0;
   cudaEventRecord(c->ev_fork, c->stream);
   cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
-  launch_on(c, c->aux, "k_flight_table", k_flight_table32, S.Nc > 0 ? S.Nc : 1, 128, S);
+  launch_on(c, c->aux, "k_flight_table", k_flight_table32, nc ? S.Nc : 1, 128, S);
   cudaEventRecord(c->ev_tab, c->aux);
   if (S.vlist) {
-    // the step's pair list on the third stream, which this schedule leaves idle; the side
-    // work of the first substep waits for it
+    // the step's pair list on the event stream before its substeps; the side work of the
+    // first substep waits for it
     cudaStreamWaitEvent(c->evs, c->ev_fork, 0);
     enq_step_pairs(c, c->evs);
   }
-  if (S.Nc > 0) enq_run_shell(c, c->aux, c->fbuf);
+  if (nc) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
   if (sort) enq_sort_scatter(c);
@@ -438,11 +432,35 @@ static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   cudaEventRecord(c->ev_cls, c->stream);
   cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
   cudaStreamWaitEvent(c->nst, c->ev_join, 0);
-  if (S.Nc > 0) launch_on(c, c->nst, "k_run_kick", k_run_kick32, 152 * 4, 256, S, c->fbuf);
-  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
-  for (int l = 1; l <= n; ++l) enq_substep_near32(c, c->nst, l);
+  if (nc) launch_on(c, c->nst, "k_run_kick", k_run_kick32, 152 * 4, 256, S, c->fbuf);
+  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE | M_PIPE, 0);
+  cudaEventRecord(c->ev_finp[0], c->nst);
+  cudaStreamWaitEvent(c->evs, c->ev_finp[0], 0);
+  for (int l = 1; l <= n; ++l) {
+    const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
+    // the finish of l-2 (the colloid kick, earlier on this stream, for l = 2): the colloid
+    // positions of l-1 and the cell table of l
+    if (l >= 3) cudaStreamWaitEvent(c->nst, c->ev_finp[l & 1], 0);
+    launch_on(c, c->nst, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8,
+              256, S, l, c->fbuf);
+    cudaEventRecord(c->ev_str, c->nst);
+    if (nc) {
+      // the side work of l after the finish of l-1
+      cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
+      if (l == 1 && S.vlist) cudaStreamWaitEvent(c->aux, c->ev_list, 0);
+      launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0, S.vlist);
+      cudaEventRecord(c->ev_aux, c->aux);
+    }
+    cudaStreamWaitEvent(c->evs, c->ev_str, 0);
+    launch_on(c, c->evs, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
+              c->fbuf);
+    if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
+    enq_fin_on(c, c->evs, (l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT)) | M_PIPE, l);
+    cudaEventRecord(c->ev_finp[l & 1], c->evs);
+  }
+  cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
   cudaEventRecord(c->ev_end, c->nst);
-  launch(c, "k_free_flight", k_free_flight32, c->n_sm * 2, 256, S, c->fbuf);
+  launch(c, "k_free_flight", k_free_flight32, free_blocks(c), 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
 }
@@ -496,7 +514,7 @@ static void enq_step_flight64(mpcd_ctx *c, bool sort) {
   }
   cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
   cudaEventRecord(c->ev_end, c->nst);
-  launch(c, "k_free_flight", k_free_flight, c->n_sm * 2, 256, S, c->fbuf);
+  launch(c, "k_free_flight", k_free_flight, free_blocks(c), 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
 }
@@ -667,11 +685,12 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   S.precision = p.precision;
-  // the FP64 form builds the cell tables in the colloid finish: its side kernel
-  // needs two warps per colloid (forces; orientation), the FP32 form's four
-  S.fin_table = p.precision == MPCD_FP64 ? 1 : 0;
+  // the colloid finish builds the cell tables (a block per colloid), so the side kernel
+  // needs two warps per colloid (forces; orientation); the batched ensemble's descriptors
+  // turn this off (a warp per colloid in its finish, the tables in its side kernel)
+  S.fin_table = 1;
   S.physics = p.physics == MPCD_PHYSICS_FIXED ? 1 : 0;
-  S.aux_nw = S.fin_table ? 2 : 4;
+  S.aux_nw = 2;
   S.dtf = (float)dt;
   S.kick32 = (float)(p.mass_colloid * p.v0 / p.mass_fl);
   S.vmaxf = (float)vmax;
@@ -736,7 +755,8 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.shell_cap = (int)(est < (double)S.N ? est : (double)S.N) + 1024;
   S.shell = m.get<ShellRec>(S.shell_cap);
   S.events_cap = S.N / 16 + 65536;
-  S.events = m.get<int>(S.events_cap);
+  // (FP32 form: two lists, by substep parity, for the overlapped near substeps)
+  S.events = m.get<int>((size_t)S.events_cap * (S.precision == MPCD_FP64 ? 1 : 2));
   S.near = m.get<int>(N);
   S.fnear = m.get<uint8_t>(N);
   S.ftab = m.get<FlightCell>(S.C);
@@ -746,6 +766,9 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     S.pend_cap = S.events_cap;
     S.prec = m.get<EventRec>(S.pend_cap);
     S.pend = m.get<uint8_t>(S.N);
+  } else {
+    S.pend_cap = S.events_cap;
+    S.plist = m.get<int>(S.pend_cap);
   }
   S.ss = m.get<StepState>(1);
   c->insw_n = m.get<double>(S.max_per_cell + 1);
@@ -1032,7 +1055,12 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
   if (which == MPCD_LAUNCH_AUX) {
     if (grid > 0 && block != 64 && block != 128 && block != 256)
       return fail(c, MPCD_ERR_PARAM, "colloid side work: 64, 128 or 256 threads per colloid");
-    c->S.aux_nw = grid > 0 ? block / 32 : (c->S.fin_table ? 2 : 4);
+    c->S.aux_nw = grid > 0 ? block / 32 : 2;
+    return drop_graph(c);
+  }
+  if (which == MPCD_LAUNCH_FREE) {
+    if (grid > 65535) return fail(c, MPCD_ERR_PARAM, "free-flight pass: grid <= 65535");
+    c->free_grid = grid > 0 ? grid : 0;
     return drop_graph(c);
   }
   if (grid > 65535 || (grid > 0 && (block < 32 || block > 128 || block % 32)))
@@ -1323,6 +1351,57 @@ extern "C" int mpcd_profile_read(mpcd_ctx *c, char names[][48], int64_t *launche
 }
 
 extern "C" int64_t mpcd_launch_count(const mpcd_ctx *c) { return c ? c->launches : -1; }
+
+// One step as a graph with a timing event before and after every launch (event-record
+// nodes), replayed once: each launch's start and end in ms from the step's start.
+extern "C" int mpcd_trace_step(mpcd_ctx *c, char names[][48], double *t0_ms, double *t1_ms, int cap) {
+  int r;
+  if ((r = need_setup(c))) return r;
+  if (c->phase != 0) return fail(c, MPCD_ERR_STATE, "a step begun routine by routine is unfinished");
+  if (c->profile) return fail(c, MPCD_ERR_STATE, "profiling is on");
+  const int sort = sorts_at(c, c->host_step) ? 1 : 0, b = c->fbuf;
+  cudaEvent_t start = pool_event(c);
+  cudaGraph_t g;
+  cudaGraphExec_t x = nullptr;
+  c->trace.clear();
+  CUDA_OK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecordWithFlags(start, c->stream, cudaEventRecordExternal);
+  c->tracing = true;
+  const int64_t before = c->launches;
+  enq_step(c, sort != 0);
+  c->tracing = false;
+  c->launches = before;
+  c->fbuf = b;
+  CUDA_OK(c, cudaStreamEndCapture(c->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(c, MPCD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  e = cudaGraphLaunch(x, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaGraphExecDestroy(x);
+  if (e != cudaSuccess) return fail(c, MPCD_ERR_CUDA, std::string("traced step: ") + cudaGetErrorString(e));
+  c->launches += (int64_t)c->trace.size();
+  if (sort) c->fbuf = 1 - b;
+  c->host_step += 1;
+  int i = 0;
+  for (auto &pe : c->trace) {
+    if (i < cap) {
+      float a = 0, z = 0;
+      cudaEventElapsedTime(&a, start, pe.a);
+      cudaEventElapsedTime(&z, start, pe.b);
+      snprintf(names[i], 48, "%s", pe.name);
+      t0_ms[i] = a;
+      t1_ms[i] = z;
+    }
+    c->event_pool.push_back(pe.a);
+    c->event_pool.push_back(pe.b);
+    ++i;
+  }
+  c->event_pool.push_back(start);
+  c->trace.clear();
+  if ((r = check_device(c))) return r;
+  return i;
+}
 
 // initialisation lives in init.cu; it needs the context internals
 #include "init_host.inc"

@@ -196,21 +196,28 @@ int mpcd_get_shell_count(mpcd_ctx *c, int32_t *cnt);
 int mpcd_profile_enable(mpcd_ctx *c, int on);
 /* per kernel: name, launches, total ms; returns the number of kernels (writes up to cap) */
 int mpcd_profile_read(mpcd_ctx *c, char names[][48], int64_t *launches, double *total_ms, int cap);
+/* one MPCD step (a real step: the state advances) as a graph with a timing event before and
+ * after every launch, replayed once and synchronised: launch i's kernel name and its start
+ * and end in ms from the step's start (the graph's own timeline, streams overlapped as in
+ * mpcd_step).  Returns the number of launches (entries beyond cap are not written) or a
+ * negative MPCD_ERR_*. */
+int mpcd_trace_step(mpcd_ctx *c, char names[][48], double *t0_ms, double *t1_ms, int cap);
 /* kernels launched by this context since creation (all of them are this library's own) */
 int64_t mpcd_launch_count(const mpcd_ctx *c);
 
 /* ---- launch shapes (no counterpart in the reference: tuning of this implementation) -- */
 enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, multiple of 32) */
-       MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32); the FP64
-                                  form runs one block of 256 per colloid (it also builds the
+       MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32); a single
+                                  system runs one block of 256 per colloid (it also builds the
                                   cell tables) and ignores this shape */
-       MPCD_LAUNCH_AUX = 2 };  /* colloid side work (forces, cell table, orientation; a kernel on a
-                                  second stream beside the streaming and event passes): grid > 0
-                                  sets, block = threads per colloid (64, 128 or 256) */
-/* grid <= 0 restores the default (events: one block of 128 threads per SM; finish:
- * one block of 32 per SM; side work: 128 threads per colloid, 64 in the FP64 form,
- * whose colloid finish builds the cell tables); results do not depend on the shape (every sum is
- * exact); drops the captured step graphs */
+       MPCD_LAUNCH_AUX = 2,    /* colloid side work (forces, orientation; a kernel on a second
+                                  stream beside the streaming and event passes): grid > 0 sets,
+                                  block = threads per colloid (64, 128 or 256) */
+       MPCD_LAUNCH_FREE = 3 }; /* free-flight pass (a persistent grid beside the substeps): grid
+                                  blocks of 256 threads; block ignored */
+/* grid <= 0 restores the default (events: one block of 128 threads per SM; side work: 64
+ * threads per colloid; free flight: two blocks per SM); results do not depend on the shape (every sum is exact); drops the
+ * captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
 /* ---- exchange record (no counterpart in the reference) ------------------------------- */
