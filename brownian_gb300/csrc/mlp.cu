@@ -15,7 +15,11 @@
 // loads (the next tile prefetched into registers), four warps of 32 x 16 each,
 // and a fused epilogue (bias, SiLU, the SiLU derivative of the
 // backward pass, BF16 / FP32 stores, FP32 atomic accumulation for split-K
-// weight gradients).
+// weight gradients).  Training runs its layer products (forward x W and backward
+// dZ W^T, K and N <= 256) on the 5th-generation tensor cores instead: k_gemm_tc,
+// tcgen05.mma with the accumulator in tensor memory (TMEM); inference
+// (mpcd_mlp_forward) keeps the warp-level kernel, whose arithmetic the colloid-only
+// step's network reproduces bit for bit.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -124,6 +128,24 @@ struct Stage {
   }
 };
 
+// one element of C after the product: bias, pre-activation store, SiLU derivative
+// (backward), SiLU, stores; or FP32 accumulation (split-K weight gradients)
+__device__ __forceinline__ void epilogue(const Gemm &g, int m, int n, float v) {
+  if (g.Cacc) {
+    atomicAdd(&g.Cacc[m * g.ldca + n], v);
+    return;
+  }
+  if (g.bias) v += g.bias[n];
+  if (g.Zb) g.Zb[m * g.ldzb + n] = __float2bfloat16(v);
+  if (g.dz) {
+    const float z = __bfloat162float(g.dz[m * g.lddz + n]), s = sigm(z);
+    v *= s * (1.f + z * (1.f - s));
+  }
+  if (g.silu) v = v * sigm(v);
+  if (g.Cf) g.Cf[m * g.ldcf + n] = v;
+  if (g.Cb) g.Cb[m * g.ldcb + n] = __float2bfloat16(v);
+}
+
 // C tile TM x TN per block of 4 warps side by side along N (each TM x TN/4: TM/16
 // m16 by TN/32 n8 mma tiles), K in steps of TK; the next K tile is loaded into
 // registers while the current one is multiplied.  Two shapes: TK = 256 takes a
@@ -195,21 +217,139 @@ __global__ void __launch_bounds__(128) k_gemm(const Gemm g) {
         const int m = m0 + i * 16 + gq + (r >= 2 ? 8 : 0);
         const int n = n0 + warp * (TN / 4) + j * 8 + q * 2 + (r & 1);
         if (m >= g.M || n >= g.N) continue;
-        float v = acc[i][j][r];
-        if (g.Cacc) {
-          atomicAdd(&g.Cacc[m * g.ldca + n], v);
-          continue;
-        }
-        if (g.bias) v += g.bias[n];
-        if (g.Zb) g.Zb[m * g.ldzb + n] = __float2bfloat16(v);
-        if (g.dz) {
-          const float z = __bfloat162float(g.dz[m * g.lddz + n]), s = sigm(z);
-          v *= s * (1.f + z * (1.f - s));
-        }
-        if (g.silu) v = v * sigm(v);
-        if (g.Cf) g.Cf[m * g.ldcf + n] = v;
-        if (g.Cb) g.Cb[m * g.ldcb + n] = __float2bfloat16(v);
+        epilogue(g, m, n, acc[i][j][r]);
       }
+}
+
+// ------------------------------------------------------------- tcgen05 products
+//
+// C[M x N] = A[M x K] B[K x N] for A with K contiguous (sak = 1) and B with K contiguous
+// (sbk = 1: B(k, n) at B[n sbn + k]), N and K multiples of 16 up to 256.  One CTA of four
+// warps per 128 rows: the A tile (128 x K) and all of B (N x K) staged in shared memory in
+// the canonical K-major layout without swizzle (core matrices of 8 rows x 16 bytes, the K
+// direction LBO = 128 bytes apart, 8-row groups SBO = K/8 x 128 bytes apart), K/16
+// tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128) issued by one thread into a TMEM
+// accumulator of 128 lanes x N columns, their completion signalled on an mbarrier
+// (tcgen05.commit) and waited for with a time limit (a wait that runs out sets *err and
+// skips the epilogue); then each warp reads its 32 TMEM lanes (rows) 16 columns at a time
+// (tcgen05.ld) into the same epilogue as k_gemm.
+constexpr int TC_M = 128;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor (tcgen05): start address, leading and stride byte
+// offsets (16-byte units), descriptor version 1 at bit 46, no base offset, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool tc_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// gives up after 100 ms (the products take microseconds) or 2^24 tries
+__device__ __forceinline__ bool tc_wait_bounded(uint32_t bar, uint32_t parity) {
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (int it = 0; it < (1 << 24); ++it) {
+    if (tc_try_wait(bar, parity)) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > 100000000ull) break;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
+  extern __shared__ __align__(1024) uint8_t tc_smem[];
+  const int K = g.K, N = g.N, kv = K / 8;
+  const uint32_t sbo = (uint32_t)kv * 128u;
+  uint8_t *As = tc_smem;
+  uint8_t *Bs = tc_smem + (size_t)TC_M * K * 2;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Bs + (size_t)N * K * 2);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * TC_M;
+  const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // staging: 16-byte vector (row r, K chunk j) -> (r / 8) SBO + j LBO + (r % 8) 16
+  for (int v = tid; v < TC_M * kv; v += 128) {
+    const int r = v / kv, j = v - r * kv, m = m0 + r;
+    uint4 val = make_uint4(0u, 0u, 0u, 0u);
+    if (m < g.M) val = *reinterpret_cast<const uint4 *>(g.A + (long long)m * g.sam + j * 8);
+    *reinterpret_cast<uint4 *>(As + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = val;
+  }
+  for (int v = tid; v < N * kv; v += 128) {
+    const int r = v / kv, j = v - r * kv;
+    const uint4 val = *reinterpret_cast<const uint4 *>(g.B + (long long)r * g.sbn + j * 8);
+    *reinterpret_cast<uint4 *>(Bs + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = val;
+  }
+  // the staged tiles to the tensor cores' (async) proxy; the TMEM address to every thread
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {
+    // instruction descriptor: FP32 accumulator (bit 4), A and B BF16 (bits 7, 10), both
+    // K-major, N / 8 at bit 17, M / 16 at bit 24
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+    const uint32_t a0 = smem_addr(As), b0 = smem_addr(Bs);
+    for (int k = 0; k < K / 16; ++k) {
+      const uint64_t ad = tc_desc(a0 + k * 256, 128, sbo), bd = tc_desc(b0 + k * 256, 128, sbo);
+      const uint32_t accumulate = k > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+          ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+          : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+  }
+  const bool ok = tc_wait_bounded(smem_addr(bar), 0);
+  if (!ok && lane == 0) atomicExch(err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (__all_sync(0xFFFFFFFFu, ok)) {
+    const int m = m0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (m < g.M) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) epilogue(g, m, c0 + q, __uint_as_float(r[q]));
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+  }
 }
 
 // raw features [n][IN] -> normalised BF16 [n][INP] (zero padded), clipped to six
@@ -299,8 +439,13 @@ Layout layout() {
 
 // Adam on the FP32 masters, then the BF16 copies (weights at [k][n] of a padded
 // [kpad][npad] matrix; biases stay FP32)
+struct WeightCopies {
+  bf16 *w[4];   // [kpad][npad] (k major rows of n): the warp-level products, inference
+  bf16 *wt[4];  // [npad][kpad] (n major rows of k): the tcgen05 products of the forward pass
+};
+
 __global__ void k_adam(float *p, const float *gr, float *m, float *v, long long n, float lr, float b1, float b2,
-                       float eps, float c1, float c2, Layout L, bf16 *w0, bf16 *w1, bf16 *w2, bf16 *w3, float *bias) {
+                       float eps, float c1, float c2, Layout L, WeightCopies W, float *bias) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float g = gr[i];
@@ -309,14 +454,14 @@ __global__ void k_adam(float *p, const float *gr, float *m, float *v, long long 
   v[i] = vi;
   const float x = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   p[i] = x;
-  bf16 *ws[4] = {w0, w1, w2, w3};
-  const int npad[4] = {H, H, H, OUTP};
+  const int npad[4] = {H, H, H, OUTP}, kpad[4] = {INP, H, H, H};
   long long boff = 0;
   for (int l = 0; l < 4; ++l) {
     if (i >= L.w[l] && i < L.b[l]) {
       const long long j = i - L.w[l];
       const int k = (int)(j / L.nout[l]), c = (int)(j % L.nout[l]);
-      ws[l][(long long)k * npad[l] + c] = __float2bfloat16(x);
+      W.w[l][(long long)k * npad[l] + c] = __float2bfloat16(x);
+      W.wt[l][(long long)c * kpad[l] + k] = __float2bfloat16(x);
       return;
     }
     if (i >= L.b[l] && i < L.b[l] + L.nout[l]) {
@@ -333,7 +478,9 @@ struct mpcd_mlp {
   int max_batch = 0;
   Layout L;
   float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // flat FP32 params, grads, Adam moments
-  bf16 *w[4] = {nullptr, nullptr, nullptr, nullptr};               // padded BF16 weights
+  bf16 *w[4] = {nullptr, nullptr, nullptr, nullptr};               // padded BF16 weights [k][n]
+  bf16 *wt[4] = {nullptr, nullptr, nullptr, nullptr};              // the same transposed, [n][k]
+  int *tc_err = nullptr;                                           // a tcgen05 wait ran out
   float *bias = nullptr;                                           // padded biases [H][H][H][OUTP]
   float *xmean = nullptr, *xistd = nullptr, *ymean = nullptr, *yistd = nullptr;
   bf16 *X = nullptr, *Z[3] = {nullptr, nullptr, nullptr}, *A[3] = {nullptr, nullptr, nullptr};
@@ -365,6 +512,29 @@ T *dalloc(mpcd_mlp *n, size_t count) {
   return static_cast<T *>(p);
 }
 
+WeightCopies copies(const mpcd_mlp *nn) {
+  WeightCopies W;
+  for (int l = 0; l < 4; ++l) {
+    W.w[l] = nn->w[l];
+    W.wt[l] = nn->wt[l];
+  }
+  return W;
+}
+
+// a product on the tcgen05 path (A and B with K contiguous, N and K multiples of 16 up to 256)
+void gemm_tc(mpcd_mlp *nn, cudaStream_t s, const Gemm &g) {
+  // at least 80 KB of shared memory per CTA, so that at most two CTAs share an SM and their
+  // TMEM columns (256 each at most) always fit in its 512: an allocation never waits
+  const size_t need = (size_t)TC_M * g.K * 2 + (size_t)g.N * g.K * 2 + 16;
+  const size_t smem = need > 80 * 1024 ? need : 80 * 1024;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)TC_M * 256 * 2 + 256 * 256 * 2 + 16));
+    attr = true;
+  }
+  k_gemm_tc<<<(unsigned)((g.M + TC_M - 1) / TC_M), 128, smem, s>>>(g, nn->tc_err);
+}
+
 void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
   if (g.K <= 256 && ksplit == 1) {
     // whole K in one staging, 32 x 32 tiles: many blocks for inference-sized M
@@ -394,14 +564,19 @@ long long bias_off(int l) {
   return o;
 }
 
-// forward of rows [0, n) of n->X; stores Z (pre-activations) and A (activations) for the backward pass
-void forward(mpcd_mlp *nn, int n, cudaStream_t s) {
+// forward of rows [0, n) of n->X; stores Z (pre-activations) and A (activations) for the backward
+// pass.  tc: the products on the tcgen05 path (training), else the warp-level kernel (inference)
+void forward(mpcd_mlp *nn, int n, cudaStream_t s, bool tc) {
   const bf16 *in = nn->X;
   long long ldin = INP;
   for (int l = 0; l < 4; ++l) {
     Gemm g = base();
     g.A = in; g.sam = ldin; g.sak = 1;
-    g.B = nn->w[l]; g.sbk = kNpad[l]; g.sbn = 1;
+    if (tc) {
+      g.B = nn->wt[l]; g.sbk = 1; g.sbn = kKpad[l];
+    } else {
+      g.B = nn->w[l]; g.sbk = kNpad[l]; g.sbn = 1;
+    }
     g.M = n; g.N = kNpad[l]; g.K = kKpad[l];
     g.bias = nn->bias + bias_off(l);
     if (l < 3) {
@@ -413,7 +588,8 @@ void forward(mpcd_mlp *nn, int n, cudaStream_t s) {
     } else {
       g.Cf = nn->O; g.ldcf = OUTP;
     }
-    gemm(s, g);
+    if (tc) gemm_tc(nn, s, g);
+    else gemm(s, g);
   }
 }
 
@@ -444,7 +620,7 @@ void backward(mpcd_mlp *nn, int n, cudaStream_t s) {
     gd.dz = nn->Z[l - 1]; gd.lddz = H;
     bf16 *dst = (l % 2) ? nn->dA : nn->dZ;
     gd.Cb = dst; gd.ldcb = H;
-    gemm(s, gd);
+    gemm_tc(nn, s, gd);
     dcur = dst;
     ldd = H;
   }
@@ -467,7 +643,7 @@ int upload_params(mpcd_mlp *nn, const float *h) {
   cudaMemset(nn->g, 0, sizeof(float) * nn->L.total);
   const long long n = nn->L.total;
   k_adam<<<(unsigned)((n + 255) / 256), 256>>>(nn->p, nn->g, nn->m, nn->v, n, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f,
-                                              nn->L, nn->w[0], nn->w[1], nn->w[2], nn->w[3], nn->bias);
+                                              nn->L, copies(nn), nn->bias);
   cudaMemset(nn->m, 0, sizeof(float) * n);
   cudaMemset(nn->v, 0, sizeof(float) * n);
   return cudaDeviceSynchronize() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "parameter upload");
@@ -490,7 +666,11 @@ extern "C" int mpcd_mlp_create(int max_batch, uint64_t seed, mpcd_mlp **out) {
   nn->L = layout();
   const long long P = nn->L.total;
   nn->p = dalloc<float>(nn, P); nn->g = dalloc<float>(nn, P); nn->m = dalloc<float>(nn, P); nn->v = dalloc<float>(nn, P);
-  for (int l = 0; l < 4; ++l) nn->w[l] = dalloc<bf16>(nn, (size_t)kKpad[l] * kNpad[l]);
+  for (int l = 0; l < 4; ++l) {
+    nn->w[l] = dalloc<bf16>(nn, (size_t)kKpad[l] * kNpad[l]);
+    nn->wt[l] = dalloc<bf16>(nn, (size_t)kKpad[l] * kNpad[l]);
+  }
+  nn->tc_err = dalloc<int>(nn, 1);
   nn->bias = dalloc<float>(nn, 3 * H + OUTP);
   nn->xmean = dalloc<float>(nn, IN); nn->xistd = dalloc<float>(nn, IN);
   nn->ymean = dalloc<float>(nn, NY); nn->yistd = dalloc<float>(nn, NY);
@@ -566,7 +746,7 @@ extern "C" int mpcd_mlp_forward(mpcd_mlp *nn, const float *x, int n, float *out,
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int r = stage_inputs(nn, x, n, s);
   if (r) return r;
-  forward(nn, n, s);
+  forward(nn, n, s, false);
   k_denorm<<<(n * OUT + 255) / 256, 256, 0, s>>>(nn->O, n, nn->ymean, nn->yistd, out);
   return cudaGetLastError() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "forward launch");
 }
@@ -575,7 +755,7 @@ extern "C" int mpcd_mlp_grad(mpcd_mlp *nn, const float *x, const float *y, int n
   if (!nn || !x || !y) return MPCD_ERR_PARAM;
   int r = stage_inputs(nn, x, n, nullptr);
   if (r) return r;
-  forward(nn, n, nullptr);
+  forward(nn, n, nullptr, true);
   cudaMemset(nn->loss, 0, sizeof(double));
   k_nll<<<(n + 255) / 256, 256>>>(nn->O, y, n, nn->ymean, nn->yistd, nn->dO, nn->loss);
   backward(nn, n, nullptr);
@@ -584,6 +764,10 @@ extern "C" int mpcd_mlp_grad(mpcd_mlp *nn, const float *x, const float *y, int n
   double l = 0;
   if (cudaMemcpy(&l, nn->loss, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
     return mfail(nn, MPCD_ERR_CUDA, "loss download");
+  int te = 0;
+  if (cudaMemcpy(&te, nn->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return mfail(nn, MPCD_ERR_CUDA, "status download");
+  if (te) return mfail(nn, MPCD_ERR_CUDA, "a tensor-core product did not complete within its time limit");
   if (loss) *loss = l / n;
   return MPCD_OK;
 }
@@ -596,7 +780,7 @@ extern "C" int mpcd_mlp_train_step(mpcd_mlp *nn, const float *x, const float *y,
   const float c1 = 1.f / (1.f - std::pow(b1, (float)nn->adam_t)), c2 = 1.f / (1.f - std::pow(b2, (float)nn->adam_t));
   const long long P = nn->L.total;
   k_adam<<<(unsigned)((P + 255) / 256), 256>>>(nn->p, nn->g, nn->m, nn->v, P, lr, b1, b2, 1e-8f, c1, c2, nn->L,
-                                              nn->w[0], nn->w[1], nn->w[2], nn->w[3], nn->bias);
+                                              copies(nn), nn->bias);
   return cudaGetLastError() == cudaSuccess ? MPCD_OK : mfail(nn, MPCD_ERR_CUDA, "adam launch");
 }
 

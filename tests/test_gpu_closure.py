@@ -1,5 +1,6 @@
-"""The closure network on the GPU (BF16 tensor-core GEMMs, FP32 accumulation)
-against its CPU restatement (oracle/mlp_ref.py): gradients (the restatement
+"""The closure network on the GPU (BF16 tensor-core GEMMs, FP32 accumulation: tcgen05 with
+TMEM accumulators for training's layer products, warp-level MMA for inference) against its
+CPU restatement (oracle/mlp_ref.py): gradients (the restatement
 rounds to BF16 where the GPU stores BF16), outputs, and that training lowers
 the loss below what a network-free prediction gives."""
 import numpy as np
@@ -29,9 +30,12 @@ def _setup(n, seed):
     return net, p, x, y, xm, xs, ym, ys, xd, yd
 
 
-def test_gradients_match_cpu_oracle():
-    net, p, x, y, xm, xs, ym, ys, xd, yd = _setup(300, 1)
-    loss, g = net.grad(xd.data_ptr(), yd.data_ptr(), 300)
+@pytest.mark.parametrize("n", [300, 2049])
+def test_gradients_match_cpu_oracle(n):
+    """Training's products run on the tcgen05 path (128-row tiles: a partial last tile at
+    both sizes, one row in it at 2049)."""
+    net, p, x, y, xm, xs, ym, ys, xd, yd = _setup(n, 1)
+    loss, g = net.grad(xd.data_ptr(), yd.data_ptr(), n)
     lref, gref = M.loss_and_grad(p, x, y, xm, xs, ym, ys, bf16_emul=True)
     assert abs(loss - lref) <= 1e-5 * abs(lref)
     o = 0
