@@ -470,13 +470,47 @@ def demo(colloids=500, fraction=0.1, steps=30, seed=5):
         net.close()
 
 
+def train_demo(batch=8192, steps=20, seed=0):
+    """Training steps of the network on random data of `batch` rows (timing and profiling of
+    the training kernels): ms per step by CUDA events, and the FLOP rate of the layer products
+    that run on the tcgen05 path (forward and backward data: 2 x batch x 589,824 FLOP a step)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    x = torch.from_numpy(rng.normal(0, 1, (batch, IN)).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.normal(0, 1, (batch, NY)).astype(np.float32)).cuda()
+    net = Network(max_batch=batch, seed=seed)
+    try:
+        net.set_normalisation(np.zeros(IN, np.float32), np.ones(IN, np.float32), np.zeros(NY, np.float32),
+                              np.ones(NY, np.float32))
+        for _ in range(3):
+            net.train_step(x.data_ptr(), y.data_ptr(), batch, 1e-3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            loss = net.train_step(x.data_ptr(), y.data_ptr(), batch, 1e-3)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        inp, h, outp = 96, 256, 16  # the padded layer widths the products run at
+        flop = 2.0 * batch * (inp * h + 2 * h * h + h * outp) + 2.0 * batch * (outp * h + 2 * h * h)
+        return {"batch": batch, "ms_per_step": ms, "loss": loss, "tc_flop_per_step": flop}
+    finally:
+        net.close()
+
+
 if __name__ == "__main__":
     import argparse
-    ap = argparse.ArgumentParser(description="colloid-only step with a random network (timing and profiling)")
-    ap.add_argument("what", choices=["demo"])
+    ap = argparse.ArgumentParser(description="colloid-only step with a random network, or training steps on random "
+                                             "data (timing and profiling)")
+    ap.add_argument("what", choices=["demo", "train"])
     ap.add_argument("--colloids", type=int, default=500)
     ap.add_argument("--fraction", type=float, default=0.1)
     ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--batch", type=int, default=8192)
     a = ap.parse_args()
-    st = demo(a.colloids, a.fraction, a.steps)
-    print("ok", {k: float(np.abs(v).max()) for k, v in st.items()})
+    if a.what == "train":
+        print("ok", train_demo(a.batch, a.steps))
+    else:
+        st = demo(a.colloids, a.fraction, a.steps)
+        print("ok", {k: float(np.abs(v).max()) for k, v in st.items()})

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(128) k_gemm(const Gemm g) {
 //
 // C[M x N] = A[M x K] B[K x N] for A with K contiguous (sak = 1) and B with K contiguous
 // (sbk = 1: B(k, n) at B[n sbn + k]), N and K multiples of 16 up to 256.  One CTA of four
-// warps per 128 rows: the A tile (128 x K) and all of B (N x K) staged in shared memory in
+// warps per 128 rows and column tile (all N, or halves of it when the rows alone would leave
+// SMs idle): the A tile (128 x K) and the B tile (N x K) staged in shared memory in
 // the canonical K-major layout without swizzle (core matrices of 8 rows x 16 bytes, the K
 // direction LBO = 128 bytes apart, 8-row groups SBO = K/8 x 128 bytes apart), K/16
 // tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128) issued by one thread into a TMEM
@@ -267,16 +268,40 @@ __device__ __forceinline__ bool tc_wait_bounded(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-__global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
+// shared memory of k_gemm_tc: the mbarrier and the TMEM address, then from byte 1024 the
+// operand tiles (A: 128 x K, B: ntile x K, canonical layout) and, once the products are done,
+// in the same place the output tiles of the epilogue (BF16 pre-activations, BF16 outputs,
+// FP32 outputs, as the product asks for them; rows of ntile + 8 (BF16) or + 4 (FP32) elements)
+struct TcSmem {
+  size_t z, c, f, total;
+};
+
+__host__ __device__ inline TcSmem tc_smem_layout(const Gemm &g, int ntile) {
+  const size_t ops = (size_t)TC_M * g.K * 2 + (size_t)ntile * g.K * 2;
+  const size_t tz = g.Zb ? (size_t)TC_M * (ntile + 8) * 2 : 0, tc = g.Cb ? (size_t)TC_M * (ntile + 8) * 2 : 0,
+               tf = g.Cf ? (size_t)TC_M * (ntile + 4) * 4 : 0;
+  TcSmem L;
+  L.z = 1024;
+  L.c = L.z + tz;
+  L.f = L.c + tc;
+  const size_t epi = tz + tc + tf;
+  L.total = 1024 + (ops > epi ? ops : epi);
+  return L;
+}
+
+__global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int ntile, int *err) {
   extern __shared__ __align__(1024) uint8_t tc_smem[];
-  const int K = g.K, N = g.N, kv = K / 8;
+  // this CTA: rows m0.. (128), columns n0.. (ntile of them, a multiple of 16)
+  const int n0 = blockIdx.y * ntile;
+  const int K = g.K, N = ntile, kv = K / 8;
   const uint32_t sbo = (uint32_t)kv * 128u;
-  uint8_t *As = tc_smem;
-  uint8_t *Bs = tc_smem + (size_t)TC_M * K * 2;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(Bs + (size_t)N * K * 2);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tc_smem);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(tc_smem + 8);
+  uint8_t *As = tc_smem + 1024;
+  uint8_t *Bs = As + (size_t)TC_M * K * 2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * TC_M;
+  const int rows = min(TC_M, g.M - m0);
   const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
@@ -288,18 +313,24 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // staging: 16-byte vector (row r, K chunk j) -> (r / 8) SBO + j LBO + (r % 8) 16
+  // staging by asynchronous 16-byte copies, all in flight at once (rows past M zero-filled):
+  // vector (row r, K chunk j) -> (r / 8) SBO + j LBO + (r % 8) 16
   for (int v = tid; v < TC_M * kv; v += 128) {
-    const int r = v / kv, j = v - r * kv, m = m0 + r;
-    uint4 val = make_uint4(0u, 0u, 0u, 0u);
-    if (m < g.M) val = *reinterpret_cast<const uint4 *>(g.A + (long long)m * g.sam + j * 8);
-    *reinterpret_cast<uint4 *>(As + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = val;
+    const int r = v / kv, j = v - r * kv;
+    const bool in = r < rows;
+    const bf16 *src = in ? g.A + (long long)(m0 + r) * g.sam + j * 8 : g.A;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(As + (r >> 3) * sbo + j * 128 + (r & 7) * 16)),
+                 "l"(src), "r"(in ? 16 : 0)
+                 : "memory");
   }
   for (int v = tid; v < N * kv; v += 128) {
     const int r = v / kv, j = v - r * kv;
-    const uint4 val = *reinterpret_cast<const uint4 *>(g.B + (long long)r * g.sbn + j * 8);
-    *reinterpret_cast<uint4 *>(Bs + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = val;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(Bs + (r >> 3) * sbo + j * 128 + (r & 7) * 16)),
+                 "l"(g.B + (long long)(n0 + r) * g.sbn + j * 8)
+                 : "memory");
   }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   // the staged tiles to the tensor cores' (async) proxy; the TMEM address to every thread
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -326,8 +357,16 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
   const bool ok = tc_wait_bounded(smem_addr(bar), 0);
   if (!ok && lane == 0) atomicExch(err, 1);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (__all_sync(0xFFFFFFFFu, ok)) {
-    const int m = m0 + warp * 32 + lane;
+  // every thread past the wait before the operand tiles are overwritten
+  const bool all_ok = __syncthreads_and(ok) != 0;
+  const TcSmem SL = tc_smem_layout(g, ntile);
+  bf16 *Zt = reinterpret_cast<bf16 *>(tc_smem + SL.z);
+  bf16 *Ct = reinterpret_cast<bf16 *>(tc_smem + SL.c);
+  float *Ft = reinterpret_cast<float *>(tc_smem + SL.f);
+  const int ldt = N + 8, ldf = N + 4;
+  if (all_ok) {
+    // TMEM -> registers (one row per thread, 16 columns at a time) -> epilogue -> output tiles
+    const int rr = warp * 32 + lane, m = m0 + rr;
     for (int c0 = 0; c0 < N; c0 += 16) {
       uint32_t r[16];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
@@ -339,8 +378,26 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (m < g.M) {
+        bf16 dzv[16];
+        if (g.dz) {
+          const uint4 *dp = reinterpret_cast<const uint4 *>(g.dz + (long long)m * g.lddz + n0 + c0);
+          *reinterpret_cast<uint4 *>(&dzv[0]) = dp[0];
+          *reinterpret_cast<uint4 *>(&dzv[8]) = dp[1];
+        }
 #pragma unroll
-        for (int q = 0; q < 16; ++q) epilogue(g, m, c0 + q, __uint_as_float(r[q]));
+        for (int q = 0; q < 16; ++q) {
+          const int n = n0 + c0 + q, c = c0 + q;
+          float v = __uint_as_float(r[q]);
+          if (g.bias) v += g.bias[n];
+          if (g.Zb) Zt[rr * ldt + c] = __float2bfloat16(v);
+          if (g.dz) {
+            const float z = __bfloat162float(dzv[q]), sg = sigm(z);
+            v *= sg * (1.f + z * (1.f - sg));
+          }
+          if (g.silu) v = v * sigm(v);
+          if (g.Cf) Ft[rr * ldf + c] = v;
+          if (g.Cb) Ct[rr * ldt + c] = __float2bfloat16(v);
+        }
       }
     }
   }
@@ -349,6 +406,24 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int *err) {
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+  }
+  if (!all_ok) return;
+  // the output tiles to global memory, 16 bytes per store along the rows
+  const int nv = N / 8;
+  for (int v = tid; v < rows * nv; v += 128) {
+    const int r = v / nv, c = (v - r * nv) * 8;
+    if (g.Zb) *reinterpret_cast<uint4 *>(g.Zb + (long long)(m0 + r) * g.ldzb + n0 + c) =
+        *reinterpret_cast<const uint4 *>(Zt + r * ldt + c);
+    if (g.Cb) *reinterpret_cast<uint4 *>(g.Cb + (long long)(m0 + r) * g.ldcb + n0 + c) =
+        *reinterpret_cast<const uint4 *>(Ct + r * ldt + c);
+  }
+  if (g.Cf) {
+    const int nf = N / 4;
+    for (int v = tid; v < rows * nf; v += 128) {
+      const int r = v / nf, c = (v - r * nf) * 4;
+      *reinterpret_cast<float4 *>(g.Cf + (long long)(m0 + r) * g.ldcf + n0 + c) =
+          *reinterpret_cast<const float4 *>(Ft + r * ldf + c);
+    }
   }
 }
 
@@ -525,14 +600,16 @@ WeightCopies copies(const mpcd_mlp *nn) {
 void gemm_tc(mpcd_mlp *nn, cudaStream_t s, const Gemm &g) {
   // at least 80 KB of shared memory per CTA, so that at most two CTAs share an SM and their
   // TMEM columns (256 each at most) always fit in its 512: an allocation never waits
-  const size_t need = (size_t)TC_M * g.K * 2 + (size_t)g.N * g.K * 2 + 16;
+  const int mt = (g.M + TC_M - 1) / TC_M;
+  const int ntile = (mt < 120 && g.N % 32 == 0 && g.N >= 64) ? g.N / 2 : g.N;
+  const size_t need = tc_smem_layout(g, ntile).total;
   const size_t smem = need > 80 * 1024 ? need : 80 * 1024;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)TC_M * 256 * 2 + 256 * 256 * 2 + 16));
+    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 + TC_M * 256 * 2 + 256 * 256 * 2);
     attr = true;
   }
-  k_gemm_tc<<<(unsigned)((g.M + TC_M - 1) / TC_M), 128, smem, s>>>(g, nn->tc_err);
+  k_gemm_tc<<<dim3((unsigned)mt, (unsigned)(g.N / ntile)), 128, smem, s>>>(g, ntile, nn->tc_err);
 }
 
 void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
