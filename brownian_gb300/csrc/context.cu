@@ -395,35 +395,52 @@ static void enq_sort_scatter(mpcd_ctx *c) {
   c->fbuf = 1 - c->fbuf;
 }
 
+// One substep of the FP32 free-flight schedule on stream s: the pass over the near list,
+// the colloid side work beside it and the event pass, then the colloid finish.
+static void enq_substep_near32(mpcd_ctx *c, cudaStream_t s, int l) {
+  const SysF64 &S = c->S;
+  const int n = S.n_sub;
+  const int flags = l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE);
+  const bool fork = S.Nc > 0;
+  if (fork) {
+    cudaEventRecord(c->ev_fork, s);
+    cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+    if (l == 1 && S.vlist) cudaStreamWaitEvent(c->aux, c->ev_list, 0);
+  }
+  launch_on(c, s, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8, 256, S,
+            l, c->fbuf);
+  if (fork) {
+    launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0, S.vlist);
+    cudaEventRecord(c->ev_join, c->aux);
+  }
+  launch_on(c, s, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
+            c->fbuf);
+  if (fork) cudaStreamWaitEvent(s, c->ev_join, 0);
+  enq_fin_on(c, s, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
+}
+
 // One step of the FP32 form in the free-flight schedule.
 //   side stream: the flight table (from the colloids' positions at the start of the
-//                step), then run()'s rear-shell test; per substep the colloid side work;
+//                step), then run()'s rear-shell test;
 //   main:        the cell pass; the rotation with the classification (it needs the table);
 //                then the free particles' whole step, beside
 //   near stream: (high priority) run()'s kick (it needs the shell test; the kicked particles
-//                are all near), the colloid kick and the n_sub passes over the near list,
-//                each overlapped with
-//   event stream: the event pass and the colloid finish of the substep before (the near
-//                pass of substep l needs the finish of l-2 only: the colloid positions of
-//                l-1, with the displacement bound as margin, and the cell table of l;
-//                particles it cannot decide go to the event pass and stay there, pending,
-//                to the end of the step);
+//                are all near), the colloid kick and the n_sub substeps of the near list;
 //   main:        the end of the step, after both.
 static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   const SysF64 &S = c->S;
   const int n = S.n_sub;
-  const bool nc = S.Nc > 0;
   cudaEventRecord(c->ev_fork, c->stream);
   cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
-  launch_on(c, c->aux, "k_flight_table", k_flight_table32, nc ? S.Nc : 1, 128, S);
+  launch_on(c, c->aux, "k_flight_table", k_flight_table32, S.Nc > 0 ? S.Nc : 1, 128, S);
   cudaEventRecord(c->ev_tab, c->aux);
   if (S.vlist) {
-    // the step's pair list on the event stream before its substeps; the side work of the
-    // first substep waits for it
+    // the step's pair list on the third stream, which this schedule leaves idle; the side
+    // work of the first substep waits for it
     cudaStreamWaitEvent(c->evs, c->ev_fork, 0);
     enq_step_pairs(c, c->evs);
   }
-  if (nc) enq_run_shell(c, c->aux, c->fbuf);
+  if (S.Nc > 0) enq_run_shell(c, c->aux, c->fbuf);
   cudaEventRecord(c->ev_join, c->aux);
   launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
   if (sort) enq_sort_scatter(c);
@@ -432,33 +449,9 @@ static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   cudaEventRecord(c->ev_cls, c->stream);
   cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
   cudaStreamWaitEvent(c->nst, c->ev_join, 0);
-  if (nc) launch_on(c, c->nst, "k_run_kick", k_run_kick32, 152 * 4, 256, S, c->fbuf);
-  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE | M_PIPE, 0);
-  cudaEventRecord(c->ev_finp[0], c->nst);
-  cudaStreamWaitEvent(c->evs, c->ev_finp[0], 0);
-  for (int l = 1; l <= n; ++l) {
-    const int flags = (l == n ? (F_STREAM | F_COLLIDE | F_SHELL | F_BINROT) : (F_STREAM | F_COLLIDE)) | F_PIPE;
-    // the finish of l-2 (the colloid kick, earlier on this stream, for l = 2): the colloid
-    // positions of l-1 and the cell table of l
-    if (l >= 3) cudaStreamWaitEvent(c->nst, c->ev_finp[l & 1], 0);
-    launch_on(c, c->nst, l == n ? "k_stream_near_last" : "k_stream_near", stream_kernel32_near(flags), c->n_sm * 8,
-              256, S, l, c->fbuf);
-    cudaEventRecord(c->ev_str, c->nst);
-    if (nc) {
-      // the side work of l after the finish of l-1
-      cudaStreamWaitEvent(c->aux, c->ev_finp[(l - 1) & 1], 0);
-      if (l == 1 && S.vlist) cudaStreamWaitEvent(c->aux, c->ev_list, 0);
-      launch_on(c, c->aux, "k_aux", k_aux, S.Nc, 32 * S.aux_nw, S, l, l >= 2 ? 1 : 0, S.vlist);
-      cudaEventRecord(c->ev_aux, c->aux);
-    }
-    cudaStreamWaitEvent(c->evs, c->ev_str, 0);
-    launch_on(c, c->evs, "k_events", event_kernel32(flags), c->ev_grid > 0 ? c->ev_grid : c->n_sm, c->ev_block, S, l,
-              c->fbuf);
-    if (nc) cudaStreamWaitEvent(c->evs, c->ev_aux, 0);
-    enq_fin_on(c, c->evs, (l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT)) | M_PIPE, l);
-    cudaEventRecord(c->ev_finp[l & 1], c->evs);
-  }
-  cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
+  if (S.Nc > 0) launch_on(c, c->nst, "k_run_kick", k_run_kick32, 152 * 4, 256, S, c->fbuf);
+  enq_fin_on(c, c->nst, M_KICK | M_ADVANCE, 0);
+  for (int l = 1; l <= n; ++l) enq_substep_near32(c, c->nst, l);
   cudaEventRecord(c->ev_end, c->nst);
   launch(c, "k_free_flight", k_free_flight32, free_blocks(c), 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
@@ -685,12 +678,11 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.max_per_cell = p.max_per_cell > 0 ? p.max_per_cell : 128;
   c->sort_every = p.sort_every > 0 ? p.sort_every : (p.sort_every < 0 ? 0 : 10);
   S.precision = p.precision;
-  // the colloid finish builds the cell tables (a block per colloid), so the side kernel
-  // needs two warps per colloid (forces; orientation); the batched ensemble's descriptors
-  // turn this off (a warp per colloid in its finish, the tables in its side kernel)
-  S.fin_table = 1;
+  // the FP64 form builds the cell tables in the colloid finish: its side kernel
+  // needs two warps per colloid (forces; orientation), the FP32 form's four
+  S.fin_table = p.precision == MPCD_FP64 ? 1 : 0;
   S.physics = p.physics == MPCD_PHYSICS_FIXED ? 1 : 0;
-  S.aux_nw = 2;
+  S.aux_nw = S.fin_table ? 2 : 4;
   S.dtf = (float)dt;
   S.kick32 = (float)(p.mass_colloid * p.v0 / p.mass_fl);
   S.vmaxf = (float)vmax;
@@ -755,8 +747,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
   S.shell_cap = (int)(est < (double)S.N ? est : (double)S.N) + 1024;
   S.shell = m.get<ShellRec>(S.shell_cap);
   S.events_cap = S.N / 16 + 65536;
-  // (FP32 form: two lists, by substep parity, for the overlapped near substeps)
-  S.events = m.get<int>((size_t)S.events_cap * (S.precision == MPCD_FP64 ? 1 : 2));
+  S.events = m.get<int>(S.events_cap);
   S.near = m.get<int>(N);
   S.fnear = m.get<uint8_t>(N);
   S.ftab = m.get<FlightCell>(S.C);
@@ -766,9 +757,6 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
     S.pend_cap = S.events_cap;
     S.prec = m.get<EventRec>(S.pend_cap);
     S.pend = m.get<uint8_t>(S.N);
-  } else {
-    S.pend_cap = S.events_cap;
-    S.plist = m.get<int>(S.pend_cap);
   }
   S.ss = m.get<StepState>(1);
   c->insw_n = m.get<double>(S.max_per_cell + 1);
@@ -1055,7 +1043,7 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
   if (which == MPCD_LAUNCH_AUX) {
     if (grid > 0 && block != 64 && block != 128 && block != 256)
       return fail(c, MPCD_ERR_PARAM, "colloid side work: 64, 128 or 256 threads per colloid");
-    c->S.aux_nw = grid > 0 ? block / 32 : 2;
+    c->S.aux_nw = grid > 0 ? block / 32 : (c->S.fin_table ? 2 : 4);
     return drop_graph(c);
   }
   if (which == MPCD_LAUNCH_FREE) {

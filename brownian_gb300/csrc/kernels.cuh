@@ -5,9 +5,7 @@
 namespace bgb {
 
 enum : int { F_STREAM = 1, F_COLLIDE = 2, F_SHELL = 4, F_BINROT = 8, F_PIPE = 16 };
-// M_PIPE: the FP32 form's overlapped substeps (pending list and event lists by substep
-// parity, as the FP64 form's)
-enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8, M_COLL = 16, M_PIPE = 32 };
+enum : int { M_FINISH = 1, M_KICK = 2, M_ADVANCE = 4, M_ACT = 8, M_COLL = 16 };
 
 // k_stream<FLAGS> instantiations, by flag set (nullptr for a set not built)
 using StreamKernel = void (*)(const SysF64, int, int);

@@ -300,17 +300,11 @@ static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int
   const Fluid32 F = fluid32_at(S, fb);
   const int i0 = chunk * (256 * U) + threadIdx.x;
   const int buf = (int)(gs & 1);
-  // F_PIPE (the near list's passes overlapped with the event passes): the colloid positions
-  // of the previous substep (this substep's are being computed meanwhile) with the
-  // displacement bound as margin; pending particles (fnear 2) belong to the event passes
-  const int xb = (flags & F_PIPE) ? (int)((gs - 1) & 1) : buf;
-  const float mg = (flags & F_PIPE) ? S.ss->cm : 0.f;
   int cx[U], cy[U], cz[U], pp[U];
   float ox[U], oy[U], oz[U], vx[U], vy[U], vz[U];
   bool valid[U], ev[U];
   unsigned members[U];
   int cnt[U], lin[U];
-  uint8_t pd[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int i = i0 + 256 * u;
@@ -320,17 +314,13 @@ static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int
     cnt[u] = 0;
     lin[u] = 0;
     pp[u] = i;
-    pd[u] = 0;
     if (valid[u]) {
       const int p = NEAR ? S.near[i] : i;
       pp[u] = p;
       unpack(F.q[p], cx[u], cy[u], cz[u], ox[u], oy[u], oz[u]);
       vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
-      if (flags & F_PIPE) pd[u] = S.fnear[p];
     }
   }
-#pragma unroll
-  for (int u = 0; u < U; ++u) valid[u] = valid[u] && pd[u] != 2;
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     if (!valid[u]) continue;
@@ -350,13 +340,8 @@ static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int
     if (valid[u] && (flags & (F_COLLIDE | F_SHELL)) && cnt[u] > 0) {
       cnt[u] = cnt[u] < TCAP ? cnt[u] : TCAP;
       const uint16_t *lst = S.Tlist[buf] + (size_t)lin[u] * TCAP;
-      const float4 *Xq = S.Xcq[xb], *Xo = S.Xco[xb];
-      // F_PIPE: the exact tests of the event pass, widened by the colloids' move in a substep
-      // (and 1e-3 for rounding): a particle the margin leaves undecided goes to the event pass
-      const float rc = (flags & F_PIPE) ? S.r_coll + 1e-3f + mg : S.r_coll;
-      const float rsl = (flags & F_PIPE) ? S.r_shell - 1e-3f - mg : S.r_shell;
-      const float rsh = S.r_shell + 1e-3f + mg;
-      const float rc2 = rc * rc, rs2 = rsl * rsl, rh2 = rsh * rsh;
+      const float4 *Xq = S.Xcq[buf], *Xo = S.Xco[buf];
+      const float rc2 = S.r_coll * S.r_coll, rs2 = S.r_shell * S.r_shell;
       for (int k = 0; k < cnt[u]; ++k) {
         const int j = lst[k];
         const float4 cq = Xq[j], co = Xo[j];
@@ -364,14 +349,7 @@ static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int
                     dz = rel(cz[u], oz[u], cq.z, co.z, S.Lz);
         const float d2 = dx * dx + dy * dy + dz * dz;
         if (flags & F_COLLIDE) ev[u] |= d2 <= rc2;
-        if (flags & F_PIPE) {
-          if (flags & F_SHELL) {
-            if (d2 < rs2) members[u] |= 1u << k;
-            else ev[u] |= d2 <= rh2;
-          }
-        } else if ((flags & F_SHELL) && d2 <= rs2) {
-          members[u] |= 1u << k;
-        }
+        if ((flags & F_SHELL) && d2 <= rs2) members[u] |= 1u << k;
       }
     }
     const int p = pp[u];
@@ -400,20 +378,12 @@ static __device__ __forceinline__ void stream32_chunk(const SysF64 &S, const int
     const bool has_rec = (mrec >> lane) & 1u;
     const unsigned mev = __ballot_sync(FULL, ev[u]);
     int bev = 0;
-    if (lane == 0 && mev) bev = atomicAdd((flags & F_PIPE) ? &S.ss->nnew[buf] : &S.ss->nevents, __popc(mev));
+    if (lane == 0 && mev) bev = atomicAdd(&S.ss->nevents, __popc(mev));
     bev = __shfl_sync(FULL, bev, 0);
     if (ev[u]) {
       const int i = bev + __popc(mev & lt);
-      if (i < S.events_cap) {
-        if (flags & F_PIPE) {
-          S.events[(size_t)buf * S.events_cap + i] = p;
-          S.fnear[p] = 2;  // pending: the event passes carry it to the end of the step
-        } else {
-          S.events[i] = p;
-        }
-      } else {
-        atomicOr(&S.ss->err, ERRB_EVENTS);
-      }
+      if (i < S.events_cap) S.events[i] = p;
+      else atomicOr(&S.ss->err, ERRB_EVENTS);
     }
     if (has_rec) {
       const int i = brec + __popc(mrec & lt);
@@ -665,9 +635,8 @@ StreamKernelB stream_kernel32_near_b(int flags) {
 
 StreamKernel stream_kernel32_near(int flags) {
   switch (flags) {
-    case F_STREAM | F_COLLIDE | F_PIPE: return k_stream32_near<F_STREAM | F_COLLIDE | F_PIPE>;
-    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE:
-      return k_stream32_near<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
+    case F_STREAM | F_COLLIDE: return k_stream32_near<F_STREAM | F_COLLIDE>;
+    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_stream32_near<F_STREAM | F_COLLIDE | F_SHELL | F_BINROT>;
   }
   return nullptr;
 }
@@ -681,24 +650,13 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
   const long long gs = step * S.n_sub + (l - 1);
   const int buf = (int)(gs & 1);
   const Fluid32 F = fluid32_at(S, fb);
-  // F_PIPE: items 0..np-1 are the particles pending from earlier substeps of this step
-  // (their streaming of this substep is done here), items np.. the ones this substep's
-  // near pass listed, which join the pending list
-  const int nn = min((flags & F_PIPE) ? S.ss->nnew[buf] : S.ss->nevents, S.events_cap);
-  const int np = (flags & F_PIPE) ? S.ss->npend : 0;
-  int n = np + nn;
-  if ((flags & F_PIPE) && n > S.pend_cap) {
-    if (VB == 0 && threadIdx.x == 0) atomicOr(&S.ss->err, ERRB_EVENTS);
-    n = S.pend_cap;
-  }
-  const int *evl = S.events + ((flags & F_PIPE) ? (size_t)buf * S.events_cap : 0);
+  const int n = min(S.ss->nevents, S.events_cap);
   const int k0 = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   for (int base = 0;; base += blockDim.x) {
     const int i = VB + NVB * (k0 + base);
     const bool valid = i < n;
     if (!__any_sync(FULL, valid)) break;
-    const bool old = (flags & F_PIPE) && i < np;
-    const int p = valid ? (old ? S.plist[i] : evl[i - np]) : 0;
+    const int p = valid ? S.events[i] : 0;
     int cx = 0, cy = 0, cz = 0;
     float ox = 0.f, oy = 0.f, oz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
     int cnt = 0, id = 0;
@@ -706,11 +664,6 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
       unpack(F.q[p], cx, cy, cz, ox, oy, oz);
       vx = F.vx[p]; vy = F.vy[p]; vz = F.vz[p];
       id = F.id[p];
-      if (old) {
-        // update_pos_mpcd of a pending particle (as the near pass does it)
-        ox = fmaf(vx, S.dtf, ox); oy = fmaf(vy, S.dtf, oy); oz = fmaf(vz, S.dtf, oz);
-        carry(cx, ox, S.Lx); carry(cy, oy, S.Ly); carry(cz, oz, S.Lz);
-      }
     }
     const int lin = cx + S.Lx * (cy + S.Ly * cz);
     if (valid) {
@@ -723,7 +676,6 @@ static __device__ __forceinline__ void k_events32_body(const SysF64 &S, const in
     if (flags & F_COLLIDE) collide32_warp<FLAGS>(S, gs, buf, valid, id, cnt, lst, cx, cy, cz, ox, oy, oz, vx, vy, vz);
     if (!valid) continue;
     finish32<FLAGS>(S, F, p, id, buf, cnt, lst, cx0, cy0, cz0, ox0, oy0, oz0, cx, cy, cz, ox, oy, oz, vx, vy, vz);
-    if ((flags & F_PIPE) && !old) S.plist[i] = p;
   }
 }
 
@@ -750,8 +702,6 @@ StreamKernel stream_kernel32(int flags) {
 
 EventKernel event_kernel32(int flags) {
   switch (flags) {
-    case F_STREAM | F_COLLIDE | F_PIPE: return k_events32<F_COLLIDE | F_PIPE>;
-    case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT | F_PIPE: return k_events32<F_COLLIDE | F_SHELL | F_BINROT | F_PIPE>;
     case F_STREAM | F_COLLIDE: return k_events32<F_COLLIDE>;
     case F_STREAM | F_COLLIDE | F_SHELL | F_BINROT: return k_events32<F_COLLIDE | F_SHELL | F_BINROT>;
     case F_SHELL | F_BINROT: return k_events32<F_SHELL | F_BINROT>;

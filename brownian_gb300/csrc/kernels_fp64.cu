@@ -867,7 +867,7 @@ static __device__ __forceinline__ void k_fin_body(const SysF64 &S, const int VB,
   const long long g = step * S.n_sub + (l - 1);  // substep finished (l >= 1)
   const long long gn = g + 1;                    // substep advanced to
   if (VB == 0 && threadIdx.x == 0) {
-    if (S.precision == MPCD_FP64 || (mode & M_PIPE)) {
+    if (S.precision == MPCD_FP64) {
       // the list substep g's streaming pass filled has been taken over by the event
       // pass (into the pending list, empty again after the last substep); its
       // buffer serves substep g+2.  The grid shift of the next step's binning is

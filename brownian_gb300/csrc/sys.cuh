@@ -158,13 +158,12 @@ struct SysF64 {
   // changing at the same time
   EventRec *newrec[2];
   EventRec *prec;
-  int *plist;  // FP32 form, overlapped near substeps: slots of the pending particles (pend_cap)
   int pend_cap;
   uint8_t *pend;    // [N]
   int physics;      // MPCD_PHYSICS_FIXED: own box among the candidates, 2-D tangential reflection
   float cmarginf;   // the margin (the bound cmargin2 checks), FP32
-  int fin_table;    // the colloid finish of substep g builds the cell table of g+2 (a single
-                    // system; else, in the batched ensemble, the side kernel of g+1 does)
+  int fin_table;    // FP64 form: the colloid finish of substep g builds the cell table of
+                    // g+2 (else the side kernel of g+1 does)
   // FP32-compensated fluid (precision MPCD_FP32C): per particle one 16-byte record
   // {cell x | y << 10 | z << 20, offset x, offset y, offset z} with offsets in
   // [0, 1) (positions exact to 2^-24 of a cell anywhere in the box) and FP32

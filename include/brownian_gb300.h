@@ -207,17 +207,18 @@ int64_t mpcd_launch_count(const mpcd_ctx *c);
 
 /* ---- launch shapes (no counterpart in the reference: tuning of this implementation) -- */
 enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, multiple of 32) */
-       MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32); a single
-                                  system runs one block of 256 per colloid (it also builds the
+       MPCD_LAUNCH_FIN = 1,    /* colloid finish: grid, block (<= 128, multiple of 32); the FP64
+                                  form runs one block of 256 per colloid (it also builds the
                                   cell tables) and ignores this shape */
-       MPCD_LAUNCH_AUX = 2,    /* colloid side work (forces, orientation; a kernel on a second
-                                  stream beside the streaming and event passes): grid > 0 sets,
-                                  block = threads per colloid (64, 128 or 256) */
+       MPCD_LAUNCH_AUX = 2,    /* colloid side work (forces, cell table, orientation; a kernel on a
+                                  second stream beside the streaming and event passes): grid > 0
+                                  sets, block = threads per colloid (64, 128 or 256) */
        MPCD_LAUNCH_FREE = 3 }; /* free-flight pass (a persistent grid beside the substeps): grid
                                   blocks of 256 threads; block ignored */
-/* grid <= 0 restores the default (events: one block of 128 threads per SM; side work: 64
- * threads per colloid; free flight: two blocks per SM); results do not depend on the shape (every sum is exact); drops the
- * captured step graphs */
+/* grid <= 0 restores the default (events: one block of 128 threads per SM; finish: one block of
+ * 32 per SM; side work: 128 threads per colloid, 64 in the FP64 form, whose colloid finish builds
+ * the cell tables; free flight: two blocks per SM); results do not depend on the shape (every
+ * sum is exact); drops the captured step graphs */
 int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block);
 
 /* ---- exchange record (no counterpart in the reference) ------------------------------- */

@@ -164,9 +164,7 @@ def test_free_flight_schedule_gives_the_same_bits(sort_every):
     for k in sa:
         assert np.array_equal(sa[k], sb[k]), k
     da, db = a.diag(), b.diag()
-    # (the free-flight schedule's near passes overlap the event passes: they test against
-    # the colloids' previous positions with a margin, so they list more candidates)
-    assert da["events"] >= db["events"] > 0
+    assert da["events"] == db["events"] > 0
     assert da["shell_records"] == db["shell_records"] > 0
     # some particles near the colloids, most in free flight
     assert 0 < max(near) < 0.6 * 138240, near
