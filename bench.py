@@ -664,7 +664,9 @@ def run_ours(args, rank, world, dist):
                   pinned["ang_vel_colloid"], pinned["ra"])
     sim.setup()
     for _ in range(args.steps):
-        sim.step(1)
+        # the step enqueued, then its diagnostics read back: one round trip per step, which
+        # also reports the step's device error bits (mpcd_diag checks them)
+        sim.step_async(1)
         dd = sim.diag()
     sim.get_state(out=out)  # into the page-locked host buffers
     _barrier(dist)
@@ -674,7 +676,8 @@ def run_ours(args, rank, world, dist):
     e2e = {"value": world * N * args.steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": state_bytes / args.steps,
            "d2h_bytes_per_step": (state_bytes + host["f"].nbytes) / args.steps + diag_bytes,
-           "timed": "set_state + setup + K x (step + diag) + get_state, host pinned buffers"}
+           "timed": "set_state + setup + K x (mpcd_step_async + mpcd_diag, one round trip per step, the "
+                    "step's error bits checked by the diag) + get_state, host pinned buffers"}
     d = sim.diag()
     sim.close()
     stats = (form_statistics(args.stat_replicas, args.stat_steps)
@@ -720,6 +723,34 @@ def run_ours(args, rank, world, dist):
     return line
 
 
+def ensemble_demo(nrep, steps):
+    """`nrep` replicas of the ensemble workload, `steps` batched free-flight steps with the
+    default launch shapes (one graph per step; for launch lists)."""
+    import brownian_gb300 as bg
+    ens = bg.Ensemble(ensemble_params(nrep))
+    for s in ens:
+        s.initialize(bg.INIT_PHYSICAL)
+        s.setup()
+    ens.step(steps)
+    print("ok", nrep, "replicas", steps, "steps", ens.launch_count, "launches")
+    ens.close()
+
+
+def trace_steps(warmup):
+    """One traced step of each form on the headline workload, after `warmup` steps: every
+    launch's start and end (us from the step's start) on the graph's own timeline, in order of
+    start (a traced step runs 20-30 % slower than an untraced one; its shape is the step's)."""
+    for precision in ("fp64", "fp32c"):
+        sim, _ = make_sim(precision, 0)
+        sim.step(max(warmup, 1))
+        sim.trace_step()
+        tr = sim.trace_step()
+        print("== %s: %d launches, step %.1f us (traced)" % (precision, len(tr), max(t for _, _, t in tr) * 1e3))
+        for name, a, b in sorted(tr, key=lambda x: x[1]):
+            print("%-22s %8.1f %8.1f %7.1f" % (name, a * 1e3, b * 1e3, (b - a) * 1e3))
+        sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -740,7 +771,18 @@ def main():
                     help="steps per activity of the closure's training runs (500 colloids each; 0: skip)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps timed for cpu_baseline (0: skip)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="fluid particles in the CPU sample (0: full 64^3 system)")
+    ap.add_argument("--trace", action="store_true",
+                    help="instead of the bench line: the timeline of one step of each form (mpcd_trace_step)")
+    ap.add_argument("--ensemble-demo", type=int, default=0,
+                    help="instead of the bench line: this many replicas of the ensemble workload stepped "
+                         "--steps times with the default launch shapes (profiling)")
     args = ap.parse_args()
+    if args.trace:
+        trace_steps(args.warmup)
+        return
+    if args.ensemble_demo > 0:
+        ensemble_demo(args.ensemble_demo, args.steps)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     n_full = L ** 3 * DENSITY
