@@ -464,44 +464,84 @@ __global__ void __launch_bounds__(256) k_rotate_classify(const SysF64 S, int fb)
 // While an exact sum x + w lies inside that binade, the nearest double to it is x plus the
 // multiple of u nearest to w, k u with k = round(Mw 2^-s), the same k at every addition
 // unless w/u is exactly halfway between two integers (then ties-to-even would depend on x).
-// So if the n results x + j k u (j = 0..n) all stay at least u inside the binade (the exact
-// sums then lie inside it) and inside [2^-30 L, L), where mod is the identity, the n
-// additions give x + n k u, built here on the integer pipe from the bits (the FP64 units
-// stay free for the substeps' chains).  Otherwise, or on a tie, the additions one by one.
-static __device__ __forceinline__ double free_stream(double x, double w, int n, const Dim &D) {
+// So while the results x + j k u stay at least u inside the binade (the exact sums then lie
+// inside it) and inside [2^-30 L, L), where mod is the identity, j additions give x + j k u,
+// built here on the integer pipe from the bits (the FP64 units stay free for the substeps'
+// chains).  free_stream takes such a run of steps, then the one addition that crosses a
+// binade or the box edge as the reference does it (mod(x + w, L) in FP64), then the next run
+// from the new x (a few crossings at most; a coordinate crosses one in a few per cent of the
+// steps of a step); on a tie, or past the crossings it allows, the additions one by one.
+
+// the largest j in [0, left] with j step <= room (step > 0; room < 2^53 and left <= 2^10, so
+// no product below overflows once step <= room)
+static __device__ __forceinline__ int seg_steps(long long room, long long step, int left) {
+  if (room < step) return 0;
+  if ((long long)left * step <= room) return left;
+  int j = (int)((float)room / (float)step);  // within one of the quotient (j < left < 2^23)
+  j = j < 0 ? 0 : (j > left ? left : j);
+  while (j < left && (long long)(j + 1) * step <= room) ++j;
+  while (j > 0 && (long long)j * step > room) --j;
+  return j;
+}
+
+// a run of up to `left` integer steps from x: false where the step does not apply (then x
+// is left as it is); else *j steps taken (0 when x sits at the edge it moves towards)
+static __device__ __forceinline__ bool free_run(double &x, double w, int left, const Dim &D, int *j) {
   const long long bx = dbits(x), bw = dbits(w);
   const long long aw = bw & 0x7FFFFFFFFFFFFFFFll;
   const int ex = (int)((bx >> 52) & 0x7FF), ew = (int)((aw >> 52) & 0x7FF);
-  bool fast = bx >= D.lo_bits && bx < D.L_bits && ex > 0 && (aw == 0 || ew > 0);
+  if (!(bx >= D.lo_bits && bx < D.L_bits && ex > 0 && (aw == 0 || ew > 0))) return false;
   long long k = 0;
-  if (fast && aw != 0) {
+  if (aw != 0) {
     const long long mw = (aw & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
     const int sh = ex - ew;
     if (sh <= 0) {
-      fast = sh > -8;  // w a multiple of u (a w that large leaves the binade anyway)
-      k = fast ? (mw << -sh) : 0;
+      if (sh <= -8) return false;  // (a w that large leaves the binade at once)
+      k = mw << -sh;
     } else if (sh <= 53) {
       k = mw >> sh;
       const long long rem = mw & ((1ll << sh) - 1), half = 1ll << (sh - 1);
-      fast = rem != half;  // a tie: the additions one by one
+      if (rem == half) return false;  // a tie
       k += rem > half ? 1 : 0;
     }  // sh > 53: |w| < u/2, every sum rounds back to x (k = 0)
     if (bw < 0) k = -k;
   }
-  // (n |k| >= 2^52 leaves the binade; the bound also keeps n k from overflowing)
-  fast = fast && n > 0 && (k < 0 ? -k : k) < 0x10000000000000ll / n;
-  if (fast) {
-    const long long mx = (bx & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
-    const long long mn = mx + (long long)n * k;
-    const long long lo = 0x10000000000000ll + 1, hi = 0x20000000000000ll - 1;
-    fast = mx >= lo && mx <= hi && mn >= lo && mn <= hi;
-    if (fast) {
-      const long long bn = ((long long)ex << 52) | (mn & 0xFFFFFFFFFFFFFll);
-      fast = bn >= D.lo_bits && bn < D.L_bits;
-      if (fast) return __longlong_as_double(bn);
+  if (left < 1 || left > 1024) return false;
+  const long long mx = (bx & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
+  const long long lo = 0x10000000000000ll + 1, hi = 0x20000000000000ll - 1;
+  int n;
+  if (k == 0) {
+    n = left;
+  } else if (k > 0) {
+    long long room = hi - mx;  // inside the binade, and below L where L lies in it
+    if ((int)((D.L_bits >> 52) & 0x7FF) == ex) {
+      const long long rl = ((D.L_bits & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll) - 1 - mx;
+      room = rl < room ? rl : room;
     }
+    n = seg_steps(room, k, left);
+  } else {
+    long long room = mx - lo;  // inside the binade, and at or above 2^-30 L where it lies in it
+    if ((int)((D.lo_bits >> 52) & 0x7FF) == ex) {
+      const long long rl = mx - ((D.lo_bits & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll);
+      room = rl < room ? rl : room;
+    }
+    n = seg_steps(room, -k, left);
   }
-  for (int l = 0; l < n; ++l) x = ref_mod(__dadd_rn(x, w), D);
+  if (n > 0) x = __longlong_as_double(((long long)ex << 52) | ((mx + (long long)n * k) & 0xFFFFFFFFFFFFFll));
+  *j = n;
+  return true;
+}
+
+static __device__ __forceinline__ double free_stream(double x, double w, int n, const Dim &D) {
+  for (int seg = 0; seg < 3 && n > 0; ++seg) {
+    int j;
+    if (!free_run(x, w, n, D, &j)) break;
+    n -= j;
+    if (n == 0) return x;
+    x = ref_mod(__dadd_rn(x, w), D);  // the crossing step, as the reference does it
+    n -= 1;
+  }
+  for (; n > 0; --n) x = ref_mod(__dadd_rn(x, w), D);
   return x;
 }
 
