@@ -445,7 +445,7 @@ static void enq_step_flight32(mpcd_ctx *c, bool sort) {
   launch(c, "k_cell_prep", k_cell_prep32, prep_blocks(S), 256, S);
   if (sort) enq_sort_scatter(c);
   cudaStreamWaitEvent(c->stream, c->ev_tab, 0);
-  launch(c, "k_rotate_classify", classify_kernel32(!sort), blocks_for(S.N, 256), 256, S, c->fbuf);
+  launch(c, "k_rotate_classify", classify_kernel32(!sort), blocks_for(S.N, 256 * CLASSIFY32_U), 256, S, c->fbuf);
   cudaEventRecord(c->ev_cls, c->stream);
   cudaStreamWaitEvent(c->nst, c->ev_cls, 0);
   cudaStreamWaitEvent(c->nst, c->ev_join, 0);

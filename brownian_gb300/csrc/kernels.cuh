@@ -42,7 +42,9 @@ __global__ void k_rotate_sort32(__grid_constant__ const SysF64 S, int src, int d
 // the FP32 free-flight schedule: flight table, rotation with the classification, the free
 // particles' whole step, per-substep passes over the near list
 __global__ void k_flight_table32(__grid_constant__ const SysF64 S);
-// the rotation with the classification (rotate false: after a counting-sort scatter)
+// the rotation with the classification (rotate false: after a counting-sort scatter); the
+// FP32 form's takes CLASSIFY32_U particles per thread (grid: N / (256 CLASSIFY32_U) blocks)
+constexpr int CLASSIFY32_U = 2;
 using ClassifyKernel = void (*)(const SysF64, int);
 ClassifyKernel classify_kernel32(bool rotate);
 __global__ void k_free_flight32(__grid_constant__ const SysF64 S, int fb);

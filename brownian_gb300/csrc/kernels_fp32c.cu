@@ -501,31 +501,48 @@ __global__ void __launch_bounds__(128) k_flight_table32_b(const SysF64 *Ss, cons
 // rotation_mpcd of one particle (the SRD map of its cell; ROT false: a counting-sort step,
 // whose scatter rotated it) and its classification: a near particle is flagged and appended to
 // the near list (one atomic per block).
-template <bool ROT>
+// U particles per thread (thread t of virtual block b: particles b 256 U + t + 256 u), their
+// loads issued together so that more gathers are in flight
+template <bool ROT, int U>
 static __device__ __forceinline__ void k_rotate_classify32_body(const SysF64 &S, const int VB, int fb) {
-  const int p = VB * blockDim.x + threadIdx.x;
-  const bool valid = p < S.N;
   const Fluid32 F = fluid32_at(S, fb);
   const long long step = S.ss->step;
   const int b0 = (int)((step * S.n_sub - 1) & 1);
-  bool near = false;
-  if (valid) {
-    const int c = ROT ? S.rotcell[p] : S.C;
-    float vx = F.vx[p], vy = F.vy[p], vz = F.vz[p];
+  int pp[U], cc[U];
+  bool valid[U], near[U];
+  float vx[U], vy[U], vz[U];
+  uint4 qq[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    pp[u] = VB * (256 * U) + (int)threadIdx.x + 256 * u;
+    valid[u] = pp[u] < S.N;
+    near[u] = false;
+    if (valid[u]) {
+      const int p = pp[u];
+      cc[u] = ROT ? S.rotcell[p] : S.C;
+      vx[u] = F.vx[p]; vy[u] = F.vy[p]; vz[u] = F.vz[p];
+      qq[u] = F.q[p];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (!valid[u]) continue;
+    const int p = pp[u];
     int cx, cy, cz;
     float ox, oy, oz;
-    unpack(F.q[p], cx, cy, cz, ox, oy, oz);
+    unpack(qq[u], cx, cy, cz, ox, oy, oz);
     const bool inb = cx < S.Lx && cy < S.Ly && cz < S.Lz;  // (a record within the box)
     const FlightCell *fc = S.ftab + (inb ? cx + S.Lx * (cy + S.Ly * cz) : 0);
     const uint4 w0 = reinterpret_cast<const uint4 *>(fc)[0], w1 = reinterpret_cast<const uint4 *>(fc)[1];
     if (ROT) {
-      if (c < S.C) apply_map32(S.cell_ab32 + (size_t)c * 12, vx, vy, vz);
-      F.vx[p] = vx; F.vy[p] = vy; F.vz[p] = vz;
+      if (cc[u] < S.C) apply_map32(S.cell_ab32 + (size_t)cc[u] * 12, vx[u], vy[u], vz[u]);
+      F.vx[p] = vx[u]; F.vy[p] = vy[u]; F.vz[p] = vz[u];
     }
-    const float travel = (float)S.n_sub * S.dtf * sqrtf(vx * vx + vy * vy + vz * vz);
+    const float travel = (float)S.n_sub * S.dtf * sqrtf(vx[u] * vx[u] + vy[u] * vy[u] + vz[u] * vz[u]);
     const int cnt = tcount(((unsigned long long)w0.y << 32) | w0.x, step);
+    bool nr = false;
     if (!inb || !(travel <= S.flight_rv) || cnt > FLIGHT_CAP) {
-      near = true;  // faster than the table allows (or not finite), or a crowded cell
+      nr = true;  // faster than the table allows (or not finite), or a crowded cell
     } else if (cnt > 0) {
       const float r = S.r_shell + travel + (float)S.n_sub * S.ss->cm + 0.01f, r2 = r * r;
       const unsigned ids[6] = {w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
@@ -535,27 +552,40 @@ static __device__ __forceinline__ void k_rotate_classify32_body(const SysF64 &S,
         const float4 cq = Xq[j], co = Xo[j];
         const float dx = rel(cx, ox, cq.x, co.x, S.Lx), dy = rel(cy, oy, cq.y, co.y, S.Ly),
                     dz = rel(cz, oz, cq.z, co.z, S.Lz);
-        near = near || !(dx * dx + dy * dy + dz * dz > r2);
+        nr = nr || !(dx * dx + dy * dy + dz * dz > r2);
       }
     }
-    S.fnear[p] = near ? 1 : 0;
+    near[u] = nr;
+    S.fnear[p] = nr ? 1 : 0;
   }
+  // the near list: one atomic per block for all U rounds
   const int lane = threadIdx.x & 31;
-  const unsigned m = __ballot_sync(FULL, near);
-  const int base = block_base_n(&S.ss->nnear, __popc(m), lane);
-  if (near) S.near[base + __popc(m & ((1u << lane) - 1u))] = p;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned m[U];
+  int tot = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    m[u] = __ballot_sync(FULL, near[u]);
+    tot += __popc(m[u]);
+  }
+  int base = block_base_n(&S.ss->nnear, tot, lane);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (near[u]) S.near[base + __popc(m[u] & lt)] = pp[u];
+    base += __popc(m[u]);
+  }
 }
 
 template <bool ROT>
 __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ const SysF64 S, int fb) {
-  k_rotate_classify32_body<ROT>(S, blockIdx.x, fb);
+  k_rotate_classify32_body<ROT, CLASSIFY32_U>(S, blockIdx.x, fb);
 }
 
 // the same over a batch of systems (persistent: batch_for)
 template <bool ROT>
 __global__ void __launch_bounds__(256) k_rotate_classify32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
   __shared__ SysF64 sS;
-  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_rotate_classify32_body<ROT>(sS, VB, fb); });
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_rotate_classify32_body<ROT, 1>(sS, VB, fb); });
 }
 
 // the free particles' whole step: n_sub streaming substeps (update_pos_mpcd, the
