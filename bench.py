@@ -517,9 +517,12 @@ def run_large(steps, warmup=3):
     sim.profile(False)
     peak = measured_peak_hbm()[0]
     # algorithmic bytes per fluid particle, FP32 form (the free-flight pass: the flag of every
-    # particle and the free particles' record, velocity, record and cell)
+    # particle and the free particles' record, velocity, record and cell; the cell pass: 88 B per
+    # cell at density 10; a near pass: index, record read and written, velocity of the near
+    # particles)
     per_particle = {"k_stream": 44, "k_rotate": 28, "k_rotate_sort": 64, "k_rotate_classify": 45,
-                    "k_free_flight": 1.0 + (1.0 - near_frac) * FREE_BYTES["fp32c"]}
+                    "k_free_flight": 1.0 + (1.0 - near_frac) * FREE_BYTES["fp32c"], "k_cell_prep": 8.8,
+                    "k_stream_near": 48.0 * near_frac}
     kernels = {}
     for k, (n, tms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
         us = tms / max(n, 1) * 1e3
@@ -761,7 +764,7 @@ def main():
     ap.add_argument("--both", type=int, default=1, help="also time the other precision form (sub-object)")
     ap.add_argument("--stat-steps", type=int, default=2000,
                     help="steps per system of the FP32c-vs-FP64 statistics (MSD at lag 100; <=100: skip)")
-    ap.add_argument("--stat-replicas", type=int, default=16,
+    ap.add_argument("--stat-replicas", type=int, default=24,
                     help="independent systems per form of the FP32c-vs-FP64 statistics (<2: skip)")
     ap.add_argument("--ensemble", type=int, default=256, help="replicas of the batched-ensemble sub-object (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=50)
