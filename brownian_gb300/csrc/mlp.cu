@@ -844,7 +844,11 @@ extern "C" int mpcd_mlp_grad(mpcd_mlp *nn, const float *x, const float *y, int n
   int te = 0;
   if (cudaMemcpy(&te, nn->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return mfail(nn, MPCD_ERR_CUDA, "status download");
-  if (te) return mfail(nn, MPCD_ERR_CUDA, "a tensor-core product did not complete within its time limit");
+  if (te) {
+    // reported once; the next call starts afresh
+    cudaMemset(nn->tc_err, 0, sizeof(int));
+    return mfail(nn, MPCD_ERR_CUDA, "a tensor-core product did not complete within its time limit");
+  }
   if (loss) *loss = l / n;
   return MPCD_OK;
 }
