@@ -33,7 +33,7 @@ EXPORTS = ["mpcd_create", "mpcd_destroy", "mpcd_last_error", "mpcd_set_stream", 
            "mpcd_ensemble_set_flight", "mpcd_ensemble_get_flight",
            "mpcd_exchange_read", "mpcd_mlp_create", "mpcd_mlp_destroy", "mpcd_mlp_last_error", "mpcd_mlp_param_count",
            "mpcd_mlp_set_normalisation", "mpcd_mlp_get_params", "mpcd_mlp_set_params", "mpcd_mlp_forward",
-           "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
+           "mpcd_mlp_grad", "mpcd_mlp_train_step", "mpcd_mlp_set_fault", "mpcd_surrogate_create", "mpcd_surrogate_destroy",
            "mpcd_surrogate_last_error", "mpcd_surrogate_set_state", "mpcd_surrogate_get_state",
            "mpcd_surrogate_features", "mpcd_surrogate_outputs", "mpcd_surrogate_fast_steps", "mpcd_surrogate_step",
            "mpcd_surrogate_set_fault", "mpcd_surrogate_set_noise", "mpcd_updown_velocity", "mpcd_traj_create",

@@ -94,6 +94,7 @@ class Network:
         L.mpcd_mlp_forward.argtypes = [vp, vp, C.c_int, vp, vp]
         L.mpcd_mlp_grad.argtypes = [vp, vp, vp, C.c_int, fp, C.POINTER(C.c_double)]
         L.mpcd_mlp_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_float, C.POINTER(C.c_double)]
+        L.mpcd_mlp_set_fault.argtypes = [vp, C.c_int]
         self.max_batch = max_batch
         h = vp()
         r = L.mpcd_mlp_create(max_batch, seed, C.byref(h))
@@ -139,6 +140,10 @@ class Network:
         self._ck(lib().mpcd_mlp_grad(self.h, C.c_void_p(x_dev), C.c_void_p(y_dev), rows,
                                      g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
         return loss.value, g
+
+    def set_fault(self, on=True):
+        """Test hook: the training products issue nothing, so their bounded waits run out."""
+        self._ck(lib().mpcd_mlp_set_fault(self.h, 1 if on else 0))
 
     def train_step(self, x_dev, y_dev, rows, lr):
         loss = C.c_double()

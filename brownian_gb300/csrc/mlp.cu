@@ -289,7 +289,7 @@ __host__ __device__ inline TcSmem tc_smem_layout(const Gemm &g, int ntile) {
   return L;
 }
 
-__global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int ntile, int *err) {
+__global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int ntile, int *err, int fault) {
   extern __shared__ __align__(1024) uint8_t tc_smem[];
   // this CTA: rows m0.. (128), columns n0.. (ntile of them, a multiple of 16)
   const int n0 = blockIdx.y * ntile;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int ntile, int *e
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  if (tid == 0) {
+  if (tid == 0 && !fault) {  // (fault: the test hook, nothing issued, every wait runs out)
     // instruction descriptor: FP32 accumulator (bit 4), A and B BF16 (bits 7, 10), both
     // K-major, N / 8 at bit 17, M / 16 at bit 24
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
@@ -556,6 +556,7 @@ struct mpcd_mlp {
   bf16 *w[4] = {nullptr, nullptr, nullptr, nullptr};               // padded BF16 weights [k][n]
   bf16 *wt[4] = {nullptr, nullptr, nullptr, nullptr};              // the same transposed, [n][k]
   int *tc_err = nullptr;                                           // a tcgen05 wait ran out
+  int tc_fault = 0;                                                // test hook (mpcd_mlp_set_fault)
   float *bias = nullptr;                                           // padded biases [H][H][H][OUTP]
   float *xmean = nullptr, *xistd = nullptr, *ymean = nullptr, *yistd = nullptr;
   bf16 *X = nullptr, *Z[3] = {nullptr, nullptr, nullptr}, *A[3] = {nullptr, nullptr, nullptr};
@@ -609,7 +610,7 @@ void gemm_tc(mpcd_mlp *nn, cudaStream_t s, const Gemm &g) {
     cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 + TC_M * 256 * 2 + 256 * 256 * 2);
     attr = true;
   }
-  k_gemm_tc<<<dim3((unsigned)mt, (unsigned)(g.N / ntile)), 128, smem, s>>>(g, ntile, nn->tc_err);
+  k_gemm_tc<<<dim3((unsigned)mt, (unsigned)(g.N / ntile)), 128, smem, s>>>(g, ntile, nn->tc_err, nn->tc_fault);
 }
 
 void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
@@ -850,6 +851,12 @@ extern "C" int mpcd_mlp_grad(mpcd_mlp *nn, const float *x, const float *y, int n
     return mfail(nn, MPCD_ERR_CUDA, "a tensor-core product did not complete within its time limit");
   }
   if (loss) *loss = l / n;
+  return MPCD_OK;
+}
+
+extern "C" int mpcd_mlp_set_fault(mpcd_mlp *nn, int on) {
+  if (!nn) return MPCD_ERR_PARAM;
+  nn->tc_fault = on ? 1 : 0;
   return MPCD_OK;
 }
 

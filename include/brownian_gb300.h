@@ -316,6 +316,11 @@ int mpcd_mlp_forward(mpcd_mlp *n, const float *x, int rows, float *out, void *st
 int mpcd_mlp_grad(mpcd_mlp *n, const float *x, const float *y, int rows, float *grad_host, double *loss_host);
 /* one Adam step (beta 0.9, 0.999) on the batch; loss_host receives the batch loss before the step */
 int mpcd_mlp_train_step(mpcd_mlp *n, const float *x, const float *y, int rows, float lr, double *loss_host);
+/* Training's layer products wait for their tensor-core results with a bound (100 ms); one that
+ * runs out makes mpcd_mlp_grad / mpcd_mlp_train_step fail with MPCD_ERR_CUDA ("did not complete
+ * within its time limit"), and the next call starts afresh.  For tests of that path this hook
+ * (on = 1) makes the products issue nothing, so that every wait runs out; 0 clears it. */
+int mpcd_mlp_set_fault(mpcd_mlp *n, int on);
 
 /* ---- colloid-only dynamics with the learned closure (no counterpart in the reference) -- */
 /* The colloids of p (box, n_colloid <= MPCD_SURROGATE_MAX_COLLOIDS, n_sub <= 32, ndt, masses, WCA

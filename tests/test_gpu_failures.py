@@ -121,3 +121,29 @@ def test_surrogate_weight_copy_that_never_arrives():
     assert not np.array_equal(st["pos_colloid"], before["pos_colloid"])
     sur.close()
     net.close()
+
+
+def test_closure_training_product_that_never_completes():
+    """The tcgen05 layer products of training wait for their results with a bound; with the
+    test hook they issue nothing, every wait runs out, and the call fails with its status and
+    message; cleared, the next call runs."""
+    import torch
+
+    import brownian_gb300 as bg
+    from brownian_gb300 import closure
+    rng = np.random.default_rng(4)
+    net = closure.Network(max_batch=512, seed=4)
+    net.set_normalisation(np.zeros(81), np.ones(81), np.zeros(6), np.ones(6))
+    x = torch.from_numpy(rng.normal(0, 1, (300, 81)).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.normal(0, 1, (300, 6)).astype(np.float32)).cuda()
+    l0, g0 = net.grad(x.data_ptr(), y.data_ptr(), 300)
+    net.set_fault(True)
+    with pytest.raises(bg.MPCDError) as e:
+        net.grad(x.data_ptr(), y.data_ptr(), 300)
+    assert e.value.code == bg.ERR_CUDA
+    assert "time limit" in str(e.value)
+    net.set_fault(False)
+    l1, g1 = net.grad(x.data_ptr(), y.data_ptr(), 300)
+    assert np.isfinite(l1) and abs(l1 - l0) <= 1e-6 * abs(l0)
+    assert np.array_equal(np.isfinite(g1), np.ones_like(g1, dtype=bool))
+    net.close()
