@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(256) k_rotate_classify32(__grid_constant__ con
 template <bool ROT>
 __global__ void __launch_bounds__(256) k_rotate_classify32_b(const SysF64 *Ss, const int *boff, int nrep, int fb) {
   __shared__ SysF64 sS;
-  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_rotate_classify32_body<ROT, 1>(sS, VB, fb); });
+  batch_for(Ss, boff, nrep, sS, [&](int VB, int) { k_rotate_classify32_body<ROT, CLASSIFY32_U>(sS, VB, fb); });
 }
 
 // the free particles' whole step: n_sub streaming substeps (update_pos_mpcd, the
