@@ -15,11 +15,11 @@
 // loads (the next tile prefetched into registers), four warps of 32 x 16 each,
 // and a fused epilogue (bias, SiLU, the SiLU derivative of the
 // backward pass, BF16 / FP32 stores, FP32 atomic accumulation for split-K
-// weight gradients).  Training runs its layer products (forward x W and backward
-// dZ W^T, K and N <= 256) on the 5th-generation tensor cores instead: k_gemm_tc,
-// tcgen05.mma with the accumulator in tensor memory (TMEM); inference
-// (mpcd_mlp_forward) keeps the warp-level kernel, whose arithmetic the colloid-only
-// step's network reproduces bit for bit.
+// weight gradients).  Training runs every product on the 5th-generation tensor cores
+// instead (tcgen05.mma with the accumulator in tensor memory, TMEM): the layer products
+// (forward x W and backward dZ W^T, K and N <= 256) on k_gemm_tc, the weight gradients (a
+// reduction over the batch) on k_gemm_tc_wgrad; inference (mpcd_mlp_forward) keeps the
+// warp-level kernel, whose arithmetic the colloid-only step's network reproduces bit for bit.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -427,6 +427,154 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const Gemm g, int ntile, int *e
   }
 }
 
+// The weight-gradient products on the tcgen05 path: C[M x N] += A[M x K] B[K x N] with A and B
+// contiguous along M and N (sam = 1, sbn = 1: the reduction runs over the batch rows, K; N
+// padded to a multiple of 16, the columns past it zero), the
+// K range split over blockIdx.z (kchunk each) and the results added to C with FP32 atomics.
+// The operands are staged row-major by 16-byte asynchronous copies, then transposed in shared
+// memory into the canonical K-major layout (a thread gathers 8 consecutive k of one row into
+// one 16-byte slot).  K runs in stages of 64 through two buffers; a buffer is staged
+// again only after the MMAs that read it have completed (one mbarrier per buffer, every wait
+// bounded).  fault: the test hook, nothing issued.
+constexpr int TCW_K = 64;
+
+__host__ __device__ inline size_t tcw_smem(int ntile) {
+  // two canonical buffers (A, B), then the row-major tiles the copies land in
+  return 1024 + 3 * ((size_t)TC_M * TCW_K * 2 + (size_t)ntile * TCW_K * 2);
+}
+
+__global__ void __launch_bounds__(128) k_gemm_tc_wgrad(const Gemm g, int ntile, int *err, int fault) {
+  extern __shared__ __align__(1024) uint8_t tc_smem[];
+  const int N = ntile, n0 = blockIdx.y * ntile, m0 = blockIdx.x * TC_M;
+  const int kbeg = blockIdx.z * g.kchunk, kend = min(g.K, kbeg + g.kchunk);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tc_smem);  // one per buffer
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(tc_smem + 16);
+  const size_t a_bytes = (size_t)TC_M * TCW_K * 2, b_bytes = (size_t)N * TCW_K * 2;
+  const uint32_t sbo = (TCW_K / 8) * 128u;
+  const uint32_t ncols = N <= 32 ? 32u : (N <= 64 ? 64u : (N <= 128 ? 128u : 256u));
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + 1)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+  const int nst = kbeg < kend ? (kend - kbeg + TCW_K - 1) / TCW_K : 0;
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  for (int st = 0; st < nst; ++st) {
+    const int q = st & 1;
+    uint8_t *As = tc_smem + 1024 + q * (a_bytes + b_bytes), *Bs = As + a_bytes;
+    if (st >= 2) {  // the MMAs of stage st - 2 read this buffer
+      if (ok) ok = tc_wait_bounded(smem_addr(bar + q), phase[q]);
+      phase[q] ^= 1u;
+    }
+    const int k0 = kbeg + st * TCW_K;
+    // the row-major tiles (64 k rows of 128 m, of N n) by 16-byte asynchronous copies, the
+    // bytes past M, N or the K range zero-filled
+    {
+      bf16 *Ra = reinterpret_cast<bf16 *>(tc_smem + 1024 + 2 * (a_bytes + b_bytes));
+      bf16 *Rb = Ra + TC_M * TCW_K;
+      for (int v = tid; v < TCW_K * (TC_M / 8); v += 128) {
+        const int k = v / (TC_M / 8), mv = (v - k * (TC_M / 8)) * 8, m = m0 + mv;
+        const int valid = (k0 + k < kend) ? max(0, min(8, g.M - m)) : 0;
+        const bf16 *src = valid ? g.A + (long long)(k0 + k) * g.sak + m : g.A;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(Ra + k * TC_M + mv)), "l"(src),
+                     "r"(valid * 2)
+                     : "memory");
+      }
+      for (int v = tid; v < TCW_K * (N / 8); v += 128) {
+        const int k = v / (N / 8), nv = (v - k * (N / 8)) * 8, n = n0 + nv;
+        const int valid = (k0 + k < kend) ? max(0, min(8, g.N - n)) : 0;
+        const bf16 *src = valid ? g.B + (long long)(k0 + k) * g.sbk + n : g.B;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(Rb + k * N + nv)), "l"(src),
+                     "r"(valid * 2)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncthreads();
+      // transposed into the canonical K-major layout: 8 consecutive k of one row per 16 bytes
+      // (consecutive threads on consecutive rows: the shared-memory reads share words)
+      for (int v = tid; v < TC_M * (TCW_K / 8); v += 128) {
+        const int j = v / TC_M, r = v - j * TC_M;
+        bf16 e[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) e[t] = Ra[(j * 8 + t) * TC_M + r];
+        *reinterpret_cast<uint4 *>(As + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = *reinterpret_cast<const uint4 *>(e);
+      }
+      for (int v = tid; v < N * (TCW_K / 8); v += 128) {
+        const int j = v / N, r = v - j * N;
+        bf16 e[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) e[t] = Rb[(j * 8 + t) * N + r];
+        *reinterpret_cast<uint4 *>(Bs + (r >> 3) * sbo + j * 128 + (r & 7) * 16) = *reinterpret_cast<const uint4 *>(e);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0 && !fault) {
+      const uint32_t a0 = smem_addr(As), b0 = smem_addr(Bs);
+      for (int kk = 0; kk < TCW_K / 16; ++kk) {
+        const uint64_t ad = tc_desc(a0 + kk * 256, 128, sbo), bd = tc_desc(b0 + kk * 256, 128, sbo);
+        const uint32_t accumulate = (st > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+            ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar + q))
+                   : "memory");
+    }
+  }
+  // the last commit arrives when every MMA issued before it has completed
+  if (nst > 0) {
+    const int q = (nst - 1) & 1;
+    if (ok) ok = tc_wait_bounded(smem_addr(bar + q), phase[q]);
+  }
+  if (!ok && lane == 0) atomicExch(err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool all_ok = __syncthreads_and(ok) != 0;
+  if (all_ok && nst > 0) {
+    const int m = m0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (m < g.M) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (n0 + c0 + q < g.N) atomicAdd(&g.Cacc[(long long)m * g.ldca + n0 + c0 + q], __uint_as_float(r[q]));
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+  }
+}
+
 // raw features [n][IN] -> normalised BF16 [n][INP] (zero padded), clipped to six
 // standard deviations so that inputs far outside the training data (a colloid the
 // dynamics has thrown) meet the network's behaviour at the edge of that data
@@ -613,6 +761,27 @@ void gemm_tc(mpcd_mlp *nn, cudaStream_t s, const Gemm &g) {
   k_gemm_tc<<<dim3((unsigned)mt, (unsigned)(g.N / ntile)), 128, smem, s>>>(g, ntile, nn->tc_err, nn->tc_fault);
 }
 
+// a weight-gradient product on the tcgen05 path (A and B contiguous along M and N, K the batch)
+void gemm_tc_wgrad(mpcd_mlp *nn, cudaStream_t s, Gemm g) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gemm_tc_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcw_smem(256));
+    attr = true;
+  }
+  const int mt = (g.M + TC_M - 1) / TC_M;
+  // (N padded to the MMA's multiple of 16; the columns past N read as zero and are not stored)
+  const int np = (g.N + 15) & ~15;
+  const int ntile = (np % 32 == 0 && np >= 64) ? np / 2 : np;
+  // about 32 K slices of at least one stage each
+  const int per = (g.K + 31) / 32;
+  g.kchunk = ((per + TCW_K - 1) / TCW_K) * TCW_K;
+  const int kz = (g.K + g.kchunk - 1) / g.kchunk;
+  const size_t need = tcw_smem(ntile);
+  const size_t smem = need > 80 * 1024 ? need : 80 * 1024;  // (two CTAs per SM at most: TMEM fits)
+  k_gemm_tc_wgrad<<<dim3((unsigned)mt, (unsigned)(np / ntile), (unsigned)kz), 128, smem, s>>>(g, ntile, nn->tc_err,
+                                                                                           nn->tc_fault);
+}
+
 void gemm(cudaStream_t s, Gemm g, int ksplit = 1) {
   if (g.K <= 256 && ksplit == 1) {
     // whole K in one staging, 32 x 32 tiles: many blocks for inference-sized M
@@ -686,7 +855,7 @@ void backward(mpcd_mlp *nn, int n, cudaStream_t s) {
     gw.B = dcur; gw.sbk = ldd; gw.sbn = 1;
     gw.M = kin; gw.N = nout; gw.K = n;
     gw.Cacc = nn->g + nn->L.w[l]; gw.ldca = nout;
-    gemm(s, gw, n >= 4096 ? 16 : 1);
+    gemm_tc_wgrad(nn, s, gw);
     dim3 cg((nout + 127) / 128, n >= 4096 ? 32 : 1);
     k_colsum<<<cg, 128, 0, s>>>(dcur, n, nout, ldd, nn->g + nn->L.b[l]);
     if (l == 0) break;
