@@ -252,18 +252,26 @@ def cpu_baseline(processes, steps, n_fluid):
 
 def _barrier(dist):
     import torch
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
 
 
 def _max_over_ranks(x, dist):
+    """The largest of the ranks' x (a time: the job's time is its slowest rank's)."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(world, units_per_rank, steps, seconds):
+    """Whole-job throughput: the units every rank processed (replicas: each rank runs its own
+    system, so the work grows with the ranks) over the slowest rank's time."""
+    return world * units_per_rank * steps / seconds
 
 
 def make_sim(precision, rank):
@@ -298,7 +306,7 @@ def measure_resident(sim, stream, precision, args, world, dist, with_clocks=True
     clk = clocks.stop(int(os.environ.get("LOCAL_RANK", "0"))) if with_clocks else None
     ms = _max_over_ranks(e0.elapsed_time(e1), dist)
     gpu_launches = sim.launch_count - launches0
-    value = world * N * args.steps / (ms / 1e3)
+    value = aggregate_rate(world, N, args.steps, ms / 1e3)
     # B: the same steps, each kernel bracketed by CUDA events on the library's stream
     sim.profile(True)
     _barrier(dist)
@@ -676,7 +684,7 @@ def run_ours(args, rank, world, dist):
     e2e_s = _max_over_ranks(time.perf_counter() - t0, dist)
     state_bytes = sum(v.nbytes for k, v in host.items() if k != "f")
     diag_bytes = 8 * 14
-    e2e = {"value": world * N * args.steps / e2e_s, "unit": "particle-steps/s",
+    e2e = {"value": aggregate_rate(world, N, args.steps, e2e_s), "unit": "particle-steps/s",
            "h2d_bytes_per_step": state_bytes / args.steps,
            "d2h_bytes_per_step": (state_bytes + host["f"].nbytes) / args.steps + diag_bytes,
            "timed": "set_state + setup + K x (mpcd_step_async + mpcd_diag, one round trip per step, the "
