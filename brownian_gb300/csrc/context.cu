@@ -56,7 +56,7 @@ struct mpcd_ctx {
   // free-flight schedule (mpcd_step): the near particles' substeps run
   // on nst (high priority) beside the free particles' pass on the context's stream
   cudaStream_t nst = nullptr;
-  cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr, ev_list = nullptr;
+  cudaEvent_t ev_tab = nullptr, ev_cls = nullptr, ev_end = nullptr, ev_list = nullptr, ev_free = nullptr;
   bool flight = true;
   cudaStream_t evs = nullptr;    // third stream (FP64 form): event passes and colloid finish
   cudaEvent_t ev_start = nullptr, ev_str = nullptr, ev_aux = nullptr, ev_finp[2] = {nullptr, nullptr};
@@ -504,9 +504,13 @@ static void enq_step_flight64(mpcd_ctx *c, bool sort) {
               l >= 2 ? 1 : 0);
     enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
     cudaEventRecord(c->ev_finp[l & 1], c->evs);
+    if (l == 1) cudaEventRecord(c->ev_free, c->evs);
   }
   cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
   cudaEventRecord(c->ev_end, c->nst);
+  // the free pass after the first substep's finish: the chain's first event pass then has the
+  // SMs to itself (the free pass holds half of every SM's registers)
+  if (n >= 2) cudaStreamWaitEvent(c->stream, c->ev_free, 0);
   launch(c, "k_free_flight", k_free_flight, free_blocks(c), 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
@@ -804,6 +808,7 @@ extern "C" int mpcd_create(const mpcd_params *pp, mpcd_ctx **out) {
       cudaEventCreateWithFlags(&c->ev_cls, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_end, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_list, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_free, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess ||
@@ -844,7 +849,7 @@ extern "C" int mpcd_destroy(mpcd_ctx *c) {
   for (void *q : {(void *)c->ud_Tc, (void *)c->ud_Tl, (void *)c->ud_cnt, (void *)c->ud_acc, (void *)c->box_cell,
                   (void *)c->box_occ, (void *)c->box_nn})
     if (q) cudaFree(q);
-  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_tab, c->ev_cls, c->ev_end, c->ev_list, c->ev_start, c->ev_str,
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join, c->ev_tab, c->ev_cls, c->ev_end, c->ev_list, c->ev_free, c->ev_start, c->ev_str,
                         c->ev_aux, c->ev_finp[0], c->ev_finp[1]})
     if (e) cudaEventDestroy(e);
   delete c;
