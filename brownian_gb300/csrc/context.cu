@@ -96,6 +96,8 @@ struct mpcd_ctx {
   long long ud_epoch = -1;
   int fin_grid = 0, fin_block = 32;  // k_fin launch shape (grid 0: one block per SM)
   int free_grid = 0;                 // free-flight pass blocks of 256 (0: the form's default)
+  int free_after = -1;               // the substep after whose colloid finish the free pass starts
+                                     // (0: after the classification; -1: the form's default)
   // routine-by-routine substep: the next routine of the substep body (0: update_pos_md)
   int rseq = 0;
   // neighbour_list_mpcd observables (allocated on first use): box of each particle,
@@ -275,6 +277,13 @@ static unsigned prep_blocks(const SysF64 &S) { return blocks_for(S.Cpad > S.Nc ?
 static unsigned free_blocks(const mpcd_ctx *c) {
   if (c->free_grid > 0) return (unsigned)c->free_grid;
   return (unsigned)(c->n_sm * 2);
+}
+
+// the substep after whose colloid finish the FP64 free pass starts (0: after the
+// classification); below n_sub
+static int free_after(const mpcd_ctx *c) {
+  const int a = c->free_after >= 0 ? c->free_after : 1;
+  return a < c->S.n_sub ? a : 0;
 }
 
 static bool sorts_at(const mpcd_ctx *c, long long step) { return c->sort_every > 0 && step % c->sort_every == 0; }
@@ -504,13 +513,13 @@ static void enq_step_flight64(mpcd_ctx *c, bool sort) {
               l >= 2 ? 1 : 0);
     enq_fin_on(c, c->evs, l < n ? (M_FINISH | M_ADVANCE) : (M_FINISH | M_ACT), l);
     cudaEventRecord(c->ev_finp[l & 1], c->evs);
-    if (l == 1) cudaEventRecord(c->ev_free, c->evs);
+    if (l == free_after(c)) cudaEventRecord(c->ev_free, c->evs);
   }
   cudaStreamWaitEvent(c->nst, c->ev_finp[n & 1], 0);
   cudaEventRecord(c->ev_end, c->nst);
-  // the free pass after the first substep's finish: the chain's first event pass then has the
-  // SMs to itself (the free pass holds half of every SM's registers)
-  if (n >= 2) cudaStreamWaitEvent(c->stream, c->ev_free, 0);
+  // the free pass after the first substep's finish (by default): the chain's first event pass
+  // then has the SMs to itself (the free pass holds half of every SM's registers)
+  if (free_after(c) >= 1) cudaStreamWaitEvent(c->stream, c->ev_free, 0);
   launch(c, "k_free_flight", k_free_flight, free_blocks(c), 256, S, c->fbuf);
   cudaStreamWaitEvent(c->stream, c->ev_end, 0);
   launch(c, "k_end_step", k_end_step, 1, 256, S);
@@ -1053,7 +1062,10 @@ extern "C" int mpcd_set_launch(mpcd_ctx *c, int which, int grid, int block) {
   }
   if (which == MPCD_LAUNCH_FREE) {
     if (grid > 65535) return fail(c, MPCD_ERR_PARAM, "free-flight pass: grid <= 65535");
+    if (grid > 0 && (block < 0 || block > c->S.n_sub - 1))
+      return fail(c, MPCD_ERR_PARAM, "free-flight pass: block = the substep it follows, 0..n_sub-1");
     c->free_grid = grid > 0 ? grid : 0;
+    c->free_after = grid > 0 ? block : -1;
     return drop_graph(c);
   }
   if (grid > 65535 || (grid > 0 && (block < 32 || block > 128 || block % 32)))

@@ -214,7 +214,9 @@ enum { MPCD_LAUNCH_EVENTS = 0, /* wall-collision events: grid, block (<= 128, mu
                                   second stream beside the streaming and event passes): grid > 0
                                   sets, block = threads per colloid (64, 128 or 256) */
        MPCD_LAUNCH_FREE = 3 }; /* free-flight pass (a persistent grid beside the substeps): grid
-                                  blocks of 256 threads; block ignored */
+                                  blocks of 256 threads; block = in the FP64 form the substep
+                                  after whose colloid finish it starts (0: right after the
+                                  classification; the default is 1) */
 /* grid <= 0 restores the default (events: one block of 128 threads per SM; finish: one block of
  * 32 per SM; side work: 128 threads per colloid, 64 in the FP64 form, whose colloid finish builds
  * the cell tables; free flight: two blocks per SM); results do not depend on the shape (every
