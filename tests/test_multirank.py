@@ -63,3 +63,24 @@ def test_aggregate_rate_is_weak_scaling():
     import bench
     one = bench.aggregate_rate(1, 2_621_440, 50, 0.0315)
     assert bench.aggregate_rate(4, 2_621_440, 50, 0.0315) == pytest.approx(4 * one)
+
+
+def test_reference_arm_line_contract():
+    """The reference arm's one JSON line on rank 0: the reference's CPU path (its own cpp/ step
+    loop where it was compiled here, else the oracle port) on a bounded sample, with the
+    line's own metric, its cpu_baseline and an e2e without copies."""
+    import json
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1",
+                        "--cpu-sample", "20000"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "MPCD fluid particle-steps/s"
+    assert d["unit"] == "particle-steps/s" and d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert "20000 fluid particles" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
